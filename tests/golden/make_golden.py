@@ -1,0 +1,82 @@
+"""Generate the golden fixtures by running the UNCHANGED reference (compiled
+from its own sources by oracle/ref/Makefile into oracle/_ref) on small cases.
+
+Run in a container that has the reference tree:  python tests/golden/make_golden.py
+The outputs (*.npz) are committed; the tests never need the reference itself.
+
+Fixtures
+  small_tdep.npz   9x13x9 nodes (mgunit 2,3,2; 3 levels; box 1 x 1.5 x 1),
+                   T-dependent viscosity eta = exp(ln(100) (0 - T)), Ra 1e4,
+                   seeded conductive T0, accuracy 1e-8.  Operator probes on
+                   every level plus 3 time steps (FP64-promoted build).
+  cfg1_16.npz      16^3 elements, 3 levels, isoviscous, Ra 1e4, the deck's own
+                   sinusoidal IC, accuracy 1e-6, 5 steps (FP64-promoted build;
+                   per-step scalars from the stock float build alongside).
+"""
+from __future__ import annotations
+
+import os
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle.decks import Case, conductive_T0  # noqa: E402
+from oracle.oracle import build_reference, run_reference  # noqa: E402
+
+
+def small_case() -> Case:
+    return Case(name="small_tdep", mgunit=(2, 3, 2), levels=3, dimen=(1.0, 1.5, 1.0),
+                rayleigh=1e4, tdepv=True, visc0=(1.0,), viscE=(4.605170185988092,), viscT=(0.0,),
+                accuracy=1e-8, maxstep=3)
+
+
+def cfg1_case() -> Case:
+    return Case(name="cfg1_16", mgunit=(4, 4, 4), levels=3, rayleigh=1e4, accuracy=1e-6,
+                perturbmag=0.01, perturbk=1.0, maxstep=5)
+
+
+def _steps(R, n, keys=("T", "V1", "V2", "V3", "U", "P", "Tdot")):
+    out = {}
+    for s in range(n + 1):
+        for k in keys:
+            nm = f"s{s}_{k}"
+            if nm in R:
+                out[nm] = R[nm]
+        out[f"s{s}_scalars"] = R[f"s{s}_scalars"]
+    return out
+
+
+def main():
+    if not build_reference(quiet=True):
+        raise SystemExit("reference sources not present; fixtures cannot be regenerated here")
+    with tempfile.TemporaryDirectory() as tmp:
+        c = small_case()
+        T0 = conductive_T0(c, amp=0.01, seed=0)
+        R = run_reference(c, os.path.join(tmp, "small"), nsteps=3, T0=T0, probe=True)
+        keep = {k: v for k, v in R.items() if not k.startswith("s")}
+        keep.update(_steps(R, 3))
+        keep["s0_F"] = R["s0_F"]
+        keep["T0_input"] = T0
+        np.savez_compressed(os.path.join(HERE, "small_tdep.npz"), **keep)
+
+        c = cfg1_case()
+        R = run_reference(c, os.path.join(tmp, "cfg1"), nsteps=5)
+        R32 = run_reference(c, os.path.join(tmp, "cfg1_32"), nsteps=5, precision="f32")
+        keep = {"dims": R["dims"], "T0": R["T0"]}
+        for s in range(6):
+            keep[f"s{s}_scalars"] = R[f"s{s}_scalars"]
+            keep[f"s{s}_scalars_f32"] = R32[f"s{s}_scalars"]
+        for k in ("T", "V1", "V2", "V3", "P"):
+            keep[f"s5_{k}"] = R[f"s5_{k}"]
+        np.savez_compressed(os.path.join(HERE, "cfg1_16.npz"), **keep)
+    for f in ("small_tdep.npz", "cfg1_16.npz"):
+        print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")
+
+
+if __name__ == "__main__":
+    main()
