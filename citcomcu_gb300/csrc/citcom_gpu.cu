@@ -1,0 +1,1133 @@
+// Host driver of the GB300 Stokes / SUPG path behind the C ABI of
+// include/citcom_gb300.h.
+//
+// One handle owns every device buffer of one problem (allocated in
+// citcom_gpu_create, nothing allocated afterwards) and one CUDA stream.  The
+// Uzawa loop (solve_Ahat_p_fhat) and the solve_del2_u loop run on the host and
+// read back a few scalars per iteration; one full-multigrid pass (multi_grid)
+// is a fixed kernel sequence and is replayed as a captured CUDA graph.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "../../include/citcom_gb300.h"
+#include "kernels.h"
+
+namespace {
+
+enum Slot
+{
+	S_RES = 0,    // r.r of the solve_del2_u residual after a multigrid pass
+	S_LS = 2,     // line search (AU.res, AU.AU)
+	S_R0 = 4,     // scratch dots
+	S_DOT = 8,    // 4 dots
+	S_NU = 16,    // Nut, Nub sums
+	S_VRMS = 18,
+	S_MIN = 20,
+	S_MAX = 21,
+	S_COUNT = 32
+};
+
+template <typename T> struct MG
+{
+	T *vel[CITCOM_MAX_LEVELS], *res[CITCOM_MAX_LEVELS], *rhs[CITCOM_MAX_LEVELS], *fl[CITCOM_MAX_LEVELS],
+		*del[CITCOM_MAX_LEVELS], *AU[CITCOM_MAX_LEVELS];
+	T *K[CITCOM_MAX_LEVELS], *BI[CITCOM_MAX_LEVELS];
+};
+
+} // namespace
+
+struct citcom_gpu
+{
+	citcom_gpu_config cfg;
+	int L;
+	Lvl lv[CITCOM_MAX_LEVELS];
+	Geo *geo[CITCOM_MAX_LEVELS];
+	double *evi[CITCOM_MAX_LEVELS];
+	double *K64[CITCOM_MAX_LEVELS];
+	double *BI64[CITCOM_MAX_LEVELS];
+	float *K32[CITCOM_MAX_LEVELS];
+	float *BI32[CITCOM_MAX_LEVELS];
+	double *BPI;
+	MG<double> mg64;
+	MG<float> mg32;
+	double *visc_work[2];
+	// fine-level fields
+	double *U, *P, *F, *T, *Tdot, *V, *buoy;
+	double *r0, *r1, *r2, *z0, *z1, *s1, *s2, *Ah, *u1;
+	double *r64;           // FP64 residual of the refinement loop (mixed mode)
+	double *Eres, *DTdot, *T1, *Tdot1, *hf_work;
+	double *dscal;
+	double *hscal;         // pinned mirror of dscal
+	Red red;
+	cudaStream_t st;
+	cudaEvent_t ev0, ev1;
+	cudaGraphExec_t mg_exec;
+	bool stiffness_ready;
+	bool visc_ready;
+	citcom_gpu_stats stats;
+	std::vector<void *> allocs;
+	char err[512];
+};
+
+namespace {
+
+int fail(citcom_gpu *h, int code, const char *fmt, ...)
+{
+	if(h)
+	{
+		va_list ap;
+		va_start(ap, fmt);
+		vsnprintf(h->err, sizeof(h->err), fmt, ap);
+		va_end(ap);
+	}
+	return code;
+}
+
+#define CK(call)                                                                                                   \
+	do                                                                                                             \
+	{                                                                                                              \
+		cudaError_t e_ = (call);                                                                                   \
+		if(e_ != cudaSuccess)                                                                                      \
+			return fail(h, CITCOM_GPU_ERR_CUDA, "%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_)); \
+	} while(0)
+
+#define TRY(call)               \
+	do                          \
+	{                           \
+		int r_ = (call);        \
+		if(r_ != CITCOM_GPU_OK) \
+			return r_;          \
+	} while(0)
+
+template <typename T> int dalloc(citcom_gpu *h, T **p, size_t n)
+{
+	void *q = nullptr;
+	cudaError_t e = cudaMalloc(&q, (n ? n : 1) * sizeof(T));
+	if(e != cudaSuccess)
+		return fail(h, CITCOM_GPU_ERR_CUDA, "cudaMalloc of %zu bytes: %s", n * sizeof(T), cudaGetErrorString(e));
+	cudaMemset(q, 0, (n ? n : 1) * sizeof(T));
+	h->allocs.push_back(q);
+	*p = (T *)q;
+	return CITCOM_GPU_OK;
+}
+
+void make_level(const citcom_gpu_config &c, int l, Lvl &L)
+{
+	memset(&L, 0, sizeof(L));
+	L.nox = c.mgunit[0] * (1 << l) + 1;
+	L.noy = c.mgunit[1] * (1 << l) + 1;
+	L.noz = c.mgunit[2] * (1 << l) + 1;
+	L.elx = L.nox - 1;
+	L.ely = L.noy - 1;
+	L.elz = L.noz - 1;
+	L.nno = L.nox * L.noy * L.noz;
+	L.nel = L.elx * L.ely * L.elz;
+	L.neq = 3 * L.nno;
+	L.npad = (L.nno + 31) / 32 * 32;
+	const int N[3] = {L.nox, L.noy, L.noz};
+	for(int a = 0; a < 3; ++a)
+		for(int p = 0; p < 2; ++p)
+			L.cnt[a][p] = (N[a] - p + 1) / 2;
+	L.coff[0] = 0;
+	for(int col = 0; col < 8; ++col)
+		L.coff[col + 1] = L.coff[col] + L.cnt[2][col & 1] * L.cnt[0][(col >> 1) & 1] * L.cnt[1][(col >> 2) & 1];
+	L.h[0] = c.dimen[0] / L.elx;
+	L.h[1] = c.dimen[1] / L.ely;
+	L.h[2] = c.dimen[2] / L.elz;
+	L.J = L.h[0] * L.h[1] * L.h[2] / 8.0;
+}
+
+Red red_of(citcom_gpu *h) { return h->red; }
+
+int readback(citcom_gpu *h, int slot, int n)
+{
+	CK(cudaMemcpyAsync(h->hscal + slot, h->dscal + slot, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+	CK(cudaStreamSynchronize(h->st));
+	return CITCOM_GPU_OK;
+}
+
+Rheo rheo_of(const citcom_gpu_config &c)
+{
+	Rheo r;
+	memset(&r, 0, sizeof(r));
+	r.tdepv = c.tdepv;
+	r.num_mat = c.num_mat < 1 ? 1 : (c.num_mat > 8 ? 8 : c.num_mat);
+	for(int i = 0; i < 8; ++i)
+	{
+		r.visc0[i] = c.visc0[i];
+		r.viscE[i] = c.viscE[i];
+		r.viscT[i] = c.viscT[i];
+		r.z_layer[i] = c.z_layer[i];
+	}
+	r.vmin_on = c.vmin_on;
+	r.vmax_on = c.vmax_on;
+	r.vmin = c.vmin;
+	r.vmax = c.vmax;
+	return r;
+}
+
+// ---------------------------------------------------------------- gauss_seidel
+
+template <typename T> void gs(citcom_gpu *h, MG<T> &B, int lev, T *d, const T *F, int cycles, int zero_start)
+{
+	const Lvl &L = h->lv[lev];
+	if(gs_small_fits(L))
+	{
+		launch_gs_small<T>(h->st, L, B.K[lev], B.BI[lev], F, d, cycles, zero_start);
+		return;
+	}
+	if(zero_start)
+		cudaMemsetAsync(d, 0, sizeof(T) * L.neq, h->st);
+	for(int c = 0; c < cycles; ++c)
+		for(int col = 0; col < 8; ++col)
+			launch_gs_colour<T>(h->st, L, B.K[lev], B.BI[lev], F, d, col);
+}
+
+// ---------------------------------------------------------------- multi_grid
+
+// One full-multigrid pass (multi_grid, General_matrix_functions.c:525-653).
+// Input: fl[lmax].  Output: vel[lmax] (the correction) and res[lmax].
+template <typename T> void mg_pass(citcom_gpu *h, MG<T> &B)
+{
+	const citcom_gpu_config &c = h->cfg;
+	const int lmax = h->L - 1, lmin = 0;
+	cudaStream_t st = h->st;
+	for(int lev = lmax; lev > lmin; --lev)
+		launch_project<T>(st, h->lv[lev], h->lv[lev - 1], B.fl[lev], B.fl[lev - 1]);
+	gs<T>(h, B, lmin, B.vel[lmin], B.fl[lmin], c.vlowstep, 1);
+	for(int lev = lmin + 1; lev <= lmax; ++lev)
+	{
+		launch_interp<T>(st, h->lv[lev - 1], h->lv[lev], B.vel[lev - 1], B.vel[lev]);
+		for(int Vn = 1; Vn <= c.mg_cycle; ++Vn)
+		{
+			for(int dlev = lev; dlev >= lmin + 1; --dlev)
+			{
+				const int cyc = (dlev == lmax) ? c.vhighstep : c.down_heavy;
+				const T *rhs = (dlev == lev) ? B.fl[lev] : B.rhs[dlev];
+				gs<T>(h, B, dlev, B.vel[dlev], rhs, cyc, dlev != lev);
+				launch_residual<T>(st, h->lv[dlev], B.K[dlev], rhs, B.vel[dlev], B.res[dlev]);
+				launch_project<T>(st, h->lv[dlev], h->lv[dlev - 1], B.res[dlev], B.rhs[dlev - 1]);
+			}
+			gs<T>(h, B, lmin, B.vel[lmin], B.rhs[lmin], c.vlowstep, 1);
+			for(int ulev = lmin + 1; ulev <= lev; ++ulev)
+			{
+				const int cyc = (ulev == lmax) ? c.vhighstep : c.up_heavy;
+				const Lvl &Lu = h->lv[ulev];
+				launch_interp<T>(st, h->lv[ulev - 1], Lu, B.vel[ulev - 1], B.del[ulev]);
+				gs<T>(h, B, ulev, B.del[ulev], B.res[ulev], cyc, 0);
+				launch_kmul_linesearch<T>(st, Lu, B.K[ulev], B.del[ulev], B.res[ulev], B.AU[ulev], red_of(h), h->dscal + S_LS);
+				launch_vel_update<T>(st, Lu.neq, B.vel[ulev], B.del[ulev], B.res[ulev], B.AU[ulev], h->dscal + S_LS,
+				                     ulev == lmax);
+			}
+		}
+	}
+}
+
+// the pass plus solve_del2_u's bookkeeping; FP64: r (= fl[lmax]) <- res, d0 += vel;
+// mixed: FP32 pass on (float) r, d0 += vel, r = F - K64 d0 in FP64
+int record_pass(citcom_gpu *h)
+{
+	const Lvl &Lf = h->lv[h->L - 1];
+	const int lmax = h->L - 1;
+	if(h->cfg.precision == CITCOM_GPU_FP64)
+	{
+		mg_pass<double>(h, h->mg64);
+		launch_axpby(h->st, Lf.neq, h->u1, 1.0, h->mg64.vel[lmax], 1.0);
+		CK(cudaMemcpyAsync(h->mg64.fl[lmax], h->mg64.res[lmax], sizeof(double) * Lf.neq, cudaMemcpyDeviceToDevice, h->st));
+		launch_dot(h->st, Lf.neq, h->mg64.res[lmax], h->mg64.res[lmax], red_of(h), h->dscal + S_RES);
+	}
+	else
+	{
+		launch_copy_d2f(h->st, Lf.neq, h->mg32.fl[lmax], h->r64);
+		mg_pass<float>(h, h->mg32);
+		launch_add_f2d(h->st, Lf.neq, h->u1, h->mg32.vel[lmax]);
+		launch_residual64(h->st, Lf, h->K64[lmax], h->Ah, h->u1, h->r64, red_of(h), h->dscal + S_RES);
+	}
+	return CITCOM_GPU_OK;
+}
+
+int run_pass(citcom_gpu *h)
+{
+	if(!h->mg_exec)
+	{
+		cudaGraph_t g;
+		CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+		int r = record_pass(h);
+		cudaError_t e = cudaStreamEndCapture(h->st, &g);
+		if(r != CITCOM_GPU_OK)
+			return r;
+		CK(e);
+		CK(cudaGraphInstantiate(&h->mg_exec, g, 0));
+		CK(cudaGraphDestroy(g));
+	}
+	CK(cudaGraphLaunch(h->mg_exec, h->st));
+	return CITCOM_GPU_OK;
+}
+
+// solve_del2_u (General_matrix_functions.c:368-520) for K d0 = F with
+// d0 = h->u1 and F = h->Ah (the only pair the Uzawa solver passes).
+int solve_del2_u(citcom_gpu *h, double acc, int *valid)
+{
+	const Lvl &Lf = h->lv[h->L - 1];
+	const int neq = Lf.neq;
+	double *r = (h->cfg.precision == CITCOM_GPU_FP64) ? h->mg64.fl[h->L - 1] : h->r64;
+	CK(cudaMemcpyAsync(r, h->Ah, sizeof(double) * neq, cudaMemcpyDeviceToDevice, h->st));
+	CK(cudaMemsetAsync(h->u1, 0, sizeof(double) * (neq + 2), h->st));
+	launch_dot(h->st, neq, r, r, red_of(h), h->dscal + S_RES);
+	TRY(readback(h, S_RES, 1));
+	const double r0 = std::sqrt(h->hscal[S_RES] / neq);
+	double residual = r0;
+	if(r0 * h->cfg.accuracy > acc)
+		acc = r0 * h->cfg.accuracy;
+	*valid = (residual < acc) ? 0 : 1;
+	int count = 0;
+	while(residual > acc)
+	{
+		if(count >= 1000)
+			return fail(h, CITCOM_GPU_ERR_NOCONV, "solve_del2_u: no convergence after %d multigrid passes (residual %g > %g)",
+			            count, residual, acc);
+		TRY(run_pass(h));
+		TRY(readback(h, S_RES, 1));
+		residual = std::sqrt(h->hscal[S_RES] / neq);
+		if(!(residual == residual))
+			return fail(h, CITCOM_GPU_ERR_NOCONV, "solve_del2_u: residual is NaN");
+		++count;
+	}
+	h->stats.mg_passes += count;
+	h->stats.del2_calls += 1;
+	return CITCOM_GPU_OK;
+}
+
+// ---------------------------------------------------------------- Uzawa
+
+// solve_Ahat_p_fhat (Stokes_flow_Incomp.c:295-497) on device buffers.
+int uzawa(citcom_gpu *h, double *V, double *P, const double *F, double imp, int *steps_max, double *initial_residual)
+{
+	const int lmax = h->L - 1;
+	const Lvl &Lf = h->lv[lmax];
+	const int neq = Lf.neq, npno = Lf.nel;
+	const Geo *geo = h->geo[lmax];
+	cudaStream_t st = h->st;
+	double *r0 = h->r0, *r1 = h->r1, *r2 = h->r2, *z0 = h->z0, *z1 = h->z1, *s1 = h->s1, *s2 = h->s2, *sh;
+	double *Ah = h->Ah, *u1 = h->u1;
+	int valid;
+	if(!h->stiffness_ready)
+		return fail(h, CITCOM_GPU_ERR_STATE, "construct_stiffness_B_matrix has not been called");
+
+	launch_dot(st, neq, F, F, red_of(h), h->dscal + S_R0);
+	TRY(readback(h, S_R0, 1));
+	const double v_res = std::sqrt(h->hscal[S_R0] / neq);
+
+	launch_grad(st, Lf, geo, P, Ah);
+	launch_kmul<double>(st, Lf, h->K64[lmax], V, u1);
+	launch_sub3(st, neq, Ah, F, Ah, u1);
+	launch_strip(st, Lf, Ah);
+	TRY(solve_del2_u(h, imp * v_res, &valid));
+	launch_strip(st, Lf, u1);
+	launch_axpby(st, neq, V, 1.0, u1, 1.0);
+	launch_div(st, Lf, geo, V, r1);
+	launch_dot(st, npno, r1, r1, red_of(h), h->dscal + S_R0);
+	TRY(readback(h, S_R0, 1));
+	const double residual = std::sqrt(h->hscal[S_R0] / npno);
+
+	int count = 0;
+	double dpressure = 1.0, dvelocity = 1.0, r1dotz1, r0dotz0 = 0.0;
+	while(count < *steps_max && (dpressure >= imp || dvelocity >= imp))
+	{
+		launch_mul(st, npno, z1, h->BPI, r1);
+		launch_dots4(st, npno, r1, z1, count ? r0 : nullptr, z0, nullptr, nullptr, nullptr, nullptr, red_of(h), h->dscal + S_DOT);
+		TRY(readback(h, S_DOT, 2));
+		r1dotz1 = h->hscal[S_DOT];
+		if(count == 0)
+			CK(cudaMemcpyAsync(s2, z1, sizeof(double) * npno, cudaMemcpyDeviceToDevice, st));
+		else
+		{
+			r0dotz0 = h->hscal[S_DOT + 1];
+			if(r0dotz0 == 0.0)
+				return fail(h, CITCOM_GPU_ERR_NOCONV, "solve_Ahat_p_fhat: division by zero in head of incompressibility iteration");
+			launch_lin2(st, npno, s2, 1.0, z1, r1dotz1 / r0dotz0, s1);
+		}
+		launch_grad(st, Lf, geo, s2, Ah);
+		TRY(solve_del2_u(h, imp * v_res, &valid));
+		launch_strip(st, Lf, u1);
+		launch_div(st, Lf, geo, u1, Ah);
+		launch_dot(st, npno, s2, Ah, red_of(h), h->dscal + S_R0);
+		TRY(readback(h, S_R0, 1));
+		const double alpha = valid ? r1dotz1 / h->hscal[S_R0] : 0.0;
+		launch_lin2(st, npno, r2, 1.0, r1, -alpha, Ah);
+		launch_axpby(st, npno, P, 1.0, s2, alpha);
+		launch_axpby(st, neq, V, 1.0, u1, -alpha);
+		launch_dots4(st, neq, V, V, u1, u1, nullptr, nullptr, nullptr, nullptr, red_of(h), h->dscal + S_DOT);
+		launch_dots4(st, npno, P, P, s2, s2, nullptr, nullptr, nullptr, nullptr, red_of(h), h->dscal + S_DOT + 4);
+		TRY(readback(h, S_DOT, 8));
+		const double vdotv = h->hscal[S_DOT], u1u1 = h->hscal[S_DOT + 1];
+		const double pdotp = h->hscal[S_DOT + 4], s2s2 = h->hscal[S_DOT + 5];
+		dpressure = alpha * std::sqrt(s2s2 / (1.0e-32 + pdotp));
+		dvelocity = alpha * std::sqrt(u1u1 / (1.0e-32 + vdotv));
+		++count;
+		sh = s1; s1 = s2; s2 = sh;
+		sh = r0; r0 = r1; r1 = r2; r2 = sh;
+		sh = z0; z0 = z1; z1 = sh;
+	}
+	h->r0 = r0; h->r1 = r1; h->r2 = r2; h->z0 = z0; h->z1 = z1; h->s1 = s1; h->s2 = s2;
+	*steps_max = count;
+	if(initial_residual)
+		*initial_residual = residual;
+	h->stats.uzawa_iterations = count;
+	h->stats.initial_residual = residual;
+	return CITCOM_GPU_OK;
+}
+
+int construct_stiffness(citcom_gpu *h)
+{
+	const citcom_gpu_config &c = h->cfg;
+	const int lmax = h->L - 1;
+	for(int l = 0; l < h->L; ++l)
+	{
+		const bool need64 = (c.precision == CITCOM_GPU_FP64) || l == lmax;
+		const bool need32 = (c.precision == CITCOM_GPU_MIXED);
+		launch_assemble(h->st, h->lv[l], h->geo[l], h->evi[l], c.aug_lagr, c.aug_number, need64 ? h->K64[l] : nullptr,
+		                need32 ? h->K32[l] : nullptr, need64 ? h->BI64[l] : nullptr, need32 ? h->BI32[l] : nullptr);
+	}
+	launch_bpi(h->st, h->lv[lmax], h->geo[lmax], h->BI64[lmax], h->BPI, c.precond);
+	CK(cudaGetLastError());
+	h->stiffness_ready = true;
+	return CITCOM_GPU_OK;
+}
+
+int project_viscosity(citcom_gpu *h)
+{
+	for(int l = h->L - 1; l > 0; --l)
+		launch_project_viscosity(h->st, h->lv[l], h->lv[l - 1], h->geo[l - 1], h->evi[l], h->evi[l - 1], h->visc_work[0],
+		                         h->visc_work[1]);
+	CK(cudaGetLastError());
+	h->visc_ready = true;
+	return CITCOM_GPU_OK;
+}
+
+int viscosity_from_device_T(citcom_gpu *h)
+{
+	const int lmax = h->L - 1;
+	launch_visc_from_T(h->st, h->lv[lmax], h->geo[lmax], rheo_of(h->cfg), h->T, h->evi[lmax]);
+	return project_viscosity(h);
+}
+
+int forces_from_device_T(citcom_gpu *h)
+{
+	const int lmax = h->L - 1;
+	launch_buoyancy(h->st, h->lv[lmax], h->cfg.rayleigh, h->T, h->buoy);
+	launch_forces(h->st, h->lv[lmax], h->geo[lmax], h->buoy, h->F);
+	CK(cudaGetLastError());
+	return CITCOM_GPU_OK;
+}
+
+// general_stokes_solver on the resident T, U, P (Drive_solvers.c:45-165)
+int stokes_resident(citcom_gpu *h)
+{
+	const int lmax = h->L - 1;
+	const Lvl &Lf = h->lv[lmax];
+	CK(cudaEventRecord(h->ev0, h->st));
+	h->stats.del2_calls = 0;
+	h->stats.mg_passes = 0;
+	launch_strip(h->st, Lf, h->U);  // velocities_conform_bcs with VB = 0
+	TRY(forces_from_device_T(h));
+	if(h->cfg.tdepv || !h->visc_ready)
+		TRY(viscosity_from_device_T(h));
+	if(h->cfg.tdepv || !h->stiffness_ready)
+		TRY(construct_stiffness(h));
+	int steps = h->cfg.piterations;
+	double r0;
+	TRY(uzawa(h, h->U, h->P, h->F, h->cfg.accuracy, &steps, &r0));
+	launch_v_from_vector(h->st, Lf, h->U, h->V);
+	CK(cudaEventRecord(h->ev1, h->st));
+	CK(cudaEventSynchronize(h->ev1));
+	float ms = 0.f;
+	CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+	h->stats.stokes_ms = ms;
+	return CITCOM_GPU_OK;
+}
+
+// PG_timestep (Advection_diffusion.c:251-345) on the resident T, Tdot, V
+int pg_timestep(citcom_gpu *h, citcom_gpu_advection *adv)
+{
+	const int lmax = h->L - 1;
+	const Lvl &Lf = h->lv[lmax];
+	const Geo *geo = h->geo[lmax];
+	const citcom_gpu_config &c = h->cfg;
+	cudaStream_t st = h->st;
+	const double gamma = 0.5;
+	double dt;
+	// std_timestep (:737-810)
+	if(c.fixed_timestep != 0.0)
+		dt = c.fixed_timestep;
+	else
+	{
+		double diff_ts = 1.0e8;
+		for(int d = 0; d < 3; ++d)
+			diff_ts = std::fmin(diff_ts, Lf.h[d] * Lf.h[d]);
+		diff_ts *= 0.5;
+		launch_adv_timestep(st, Lf, h->V, red_of(h), h->dscal + S_MIN);
+		TRY(readback(h, S_MIN, 1));
+		const double adv_ts = c.finetunedt * h->hscal[S_MIN];
+		dt = 1.0e-32 + (adv_ts < diff_ts ? adv_ts : diff_ts);
+	}
+	CK(cudaMemcpyAsync(h->T1, h->T, sizeof(double) * Lf.nno, cudaMemcpyDeviceToDevice, st));
+	CK(cudaMemcpyAsync(h->Tdot1, h->Tdot, sizeof(double) * Lf.nno, cudaMemcpyDeviceToDevice, st));
+	launch_tmax(st, Lf.nno, h->T, red_of(h), h->dscal + S_MAX);
+	TRY(readback(h, S_MAX, 1));
+	const double T_interior1 = h->hscal[S_MAX];
+	double dt_reduced = 1.0, T_interior;
+	int sub = 1, iredo;
+	do
+	{
+		dt *= dt_reduced;
+		iredo = 0;
+		launch_predictor(st, Lf, h->T, h->Tdot, dt, gamma);
+		for(int pass = 0; pass < c.adv_sub_iterations; ++pass)
+		{
+			launch_pg_residual(st, Lf, geo, h->T, h->Tdot, h->V, c.Q0, h->Eres);
+			launch_pg_gather(st, Lf, h->Eres, h->DTdot);
+			launch_corrector(st, Lf, h->T, h->Tdot, h->DTdot, dt, gamma);
+		}
+		launch_tmax(st, Lf.nno, h->T, red_of(h), h->dscal + S_MAX);
+		TRY(readback(h, S_MAX, 1));
+		T_interior = h->hscal[S_MAX];
+		if(T_interior / T_interior1 > 1.01)
+		{
+			CK(cudaMemcpyAsync(h->T, h->T1, sizeof(double) * Lf.nno, cudaMemcpyDeviceToDevice, st));
+			CK(cudaMemcpyAsync(h->Tdot, h->Tdot1, sizeof(double) * Lf.nno, cudaMemcpyDeviceToDevice, st));
+			iredo = 1;
+			dt_reduced *= 0.5;
+			++sub;
+		}
+	} while(iredo == 1 && sub <= 5);
+	launch_conform_T(st, Lf, h->T);
+	CK(cudaGetLastError());
+	if(adv)
+	{
+		adv->timestep = dt;
+		adv->elapsed_time += dt;
+		adv->T_interior = T_interior;
+		adv->last_sub_iterations = 1;
+	}
+	return CITCOM_GPU_OK;
+}
+
+int check_handle(const citcom_gpu *h) { return h ? CITCOM_GPU_OK : CITCOM_GPU_ERR_ARG; }
+
+int check_level(citcom_gpu *h, int lev)
+{
+	if(lev < 0 || lev >= h->L)
+		return fail(h, CITCOM_GPU_ERR_ARG, "level %d outside 0..%d", lev, h->L - 1);
+	return CITCOM_GPU_OK;
+}
+
+int h2d(citcom_gpu *h, void *dst, const void *src, size_t bytes)
+{
+	if(!src)
+		return fail(h, CITCOM_GPU_ERR_ARG, "null input pointer");
+	CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->st));
+	return CITCOM_GPU_OK;
+}
+
+int d2h(citcom_gpu *h, void *dst, const void *src, size_t bytes)
+{
+	if(!dst)
+		return CITCOM_GPU_OK;
+	CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, h->st));
+	return CITCOM_GPU_OK;
+}
+
+int sync(citcom_gpu *h)
+{
+	CK(cudaStreamSynchronize(h->st));
+	CK(cudaGetLastError());
+	return CITCOM_GPU_OK;
+}
+
+template <typename T> int alloc_mg(citcom_gpu *h, MG<T> &B)
+{
+	for(int l = 0; l < h->L; ++l)
+	{
+		const size_t n = h->lv[l].neq + 2;
+		TRY(dalloc(h, &B.vel[l], n));
+		TRY(dalloc(h, &B.res[l], n));
+		TRY(dalloc(h, &B.rhs[l], n));
+		TRY(dalloc(h, &B.fl[l], n));
+		TRY(dalloc(h, &B.del[l], n));
+		TRY(dalloc(h, &B.AU[l], n));
+	}
+	return CITCOM_GPU_OK;
+}
+
+} // namespace
+
+// ====================================================================== C ABI
+
+extern "C" {
+
+int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
+{
+	if(!cfg || !out)
+		return CITCOM_GPU_ERR_ARG;
+	*out = nullptr;
+	if(cfg->levels < 1 || cfg->levels > CITCOM_MAX_LEVELS || cfg->mgunit[0] < 1 || cfg->mgunit[1] < 1 || cfg->mgunit[2] < 1 ||
+	   cfg->precision < CITCOM_GPU_FP64 || cfg->precision > CITCOM_GPU_MIXED || cfg->num_mat < 1 || cfg->num_mat > 8)
+		return CITCOM_GPU_ERR_ARG;
+	int ndev = 0;
+	if(cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1)
+		return CITCOM_GPU_ERR_CUDA;
+	citcom_gpu *h = new citcom_gpu();
+	memset(h->err, 0, sizeof(h->err));
+	h->cfg = *cfg;
+	h->L = cfg->levels;
+	h->mg_exec = nullptr;
+	h->stiffness_ready = false;
+	h->visc_ready = false;
+	memset(&h->stats, 0, sizeof(h->stats));
+	int r = CITCOM_GPU_OK;
+#define TRYC(call)                  \
+	do                              \
+	{                               \
+		r = (call);                 \
+		if(r != CITCOM_GPU_OK)      \
+			goto failed;            \
+	} while(0)
+	{
+		if(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess ||
+		   cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess)
+		{
+			r = fail(h, CITCOM_GPU_ERR_CUDA, "stream/event creation failed");
+			goto failed;
+		}
+		for(int l = 0; l < h->L; ++l)
+			make_level(*cfg, l, h->lv[l]);
+		const int lmax = h->L - 1;
+		const Lvl &Lf = h->lv[lmax];
+		for(int l = 0; l < h->L; ++l)
+		{
+			const Lvl &L = h->lv[l];
+			Geo g;
+			geo_fill_host(L, &g);
+			TRYC(dalloc(h, &h->geo[l], 1));
+			if(cudaMemcpy(h->geo[l], &g, sizeof(Geo), cudaMemcpyHostToDevice) != cudaSuccess)
+			{
+				r = fail(h, CITCOM_GPU_ERR_CUDA, "geometry upload failed");
+				goto failed;
+			}
+			TRYC(dalloc(h, &h->evi[l], (size_t)L.nel * 8));
+			const bool need64 = (cfg->precision == CITCOM_GPU_FP64) || l == lmax;
+			const bool need32 = (cfg->precision == CITCOM_GPU_MIXED);
+			h->K64[l] = nullptr;
+			h->BI64[l] = nullptr;
+			h->K32[l] = nullptr;
+			h->BI32[l] = nullptr;
+			if(need64)
+			{
+				TRYC(dalloc(h, &h->K64[l], (size_t)243 * L.npad));
+				TRYC(dalloc(h, &h->BI64[l], (size_t)3 * L.npad));
+			}
+			if(need32)
+			{
+				TRYC(dalloc(h, &h->K32[l], (size_t)243 * L.npad));
+				TRYC(dalloc(h, &h->BI32[l], (size_t)3 * L.npad));
+			}
+			h->mg64.K[l] = h->K64[l];
+			h->mg64.BI[l] = h->BI64[l];
+			h->mg32.K[l] = h->K32[l];
+			h->mg32.BI[l] = h->BI32[l];
+		}
+		if(cfg->precision == CITCOM_GPU_FP64)
+			TRYC(alloc_mg(h, h->mg64));
+		else
+			TRYC(alloc_mg(h, h->mg32));
+		TRYC(dalloc(h, &h->BPI, Lf.nel));
+		TRYC(dalloc(h, &h->visc_work[0], Lf.nno));
+		TRYC(dalloc(h, &h->visc_work[1], Lf.nno));
+		TRYC(dalloc(h, &h->U, Lf.neq + 2));
+		TRYC(dalloc(h, &h->P, Lf.nel));
+		TRYC(dalloc(h, &h->F, Lf.neq + 2));
+		TRYC(dalloc(h, &h->T, Lf.nno));
+		TRYC(dalloc(h, &h->Tdot, Lf.nno));
+		TRYC(dalloc(h, &h->V, (size_t)3 * Lf.nno));
+		TRYC(dalloc(h, &h->buoy, Lf.nno + Lf.noz));
+		TRYC(dalloc(h, &h->r0, Lf.nel));
+		TRYC(dalloc(h, &h->r1, Lf.nel));
+		TRYC(dalloc(h, &h->r2, Lf.nel));
+		TRYC(dalloc(h, &h->z0, Lf.nel));
+		TRYC(dalloc(h, &h->z1, Lf.nel));
+		TRYC(dalloc(h, &h->s1, Lf.nel));
+		TRYC(dalloc(h, &h->s2, Lf.nel));
+		TRYC(dalloc(h, &h->Ah, Lf.neq + 2));
+		TRYC(dalloc(h, &h->u1, Lf.neq + 2));
+		TRYC(dalloc(h, &h->r64, Lf.neq + 2));
+		TRYC(dalloc(h, &h->Eres, (size_t)8 * Lf.nel));
+		TRYC(dalloc(h, &h->DTdot, Lf.nno));
+		TRYC(dalloc(h, &h->T1, Lf.nno));
+		TRYC(dalloc(h, &h->Tdot1, Lf.nno));
+		TRYC(dalloc(h, &h->hf_work, Lf.nno + Lf.nel));
+		TRYC(dalloc(h, &h->dscal, S_COUNT));
+		TRYC(dalloc(h, &h->red.partials, (size_t)RED_MAX_BLOCKS * 8));
+		TRYC(dalloc(h, &h->red.counter, 1));
+		if(cudaMallocHost((void **)&h->hscal, S_COUNT * sizeof(double)) != cudaSuccess)
+		{
+			r = fail(h, CITCOM_GPU_ERR_CUDA, "pinned scalar buffer");
+			goto failed;
+		}
+		if(cudaDeviceSynchronize() != cudaSuccess)
+		{
+			r = fail(h, CITCOM_GPU_ERR_CUDA, "initialisation failed");
+			goto failed;
+		}
+	}
+#undef TRYC
+	*out = h;
+	return CITCOM_GPU_OK;
+failed:
+	citcom_gpu_destroy(h);
+	return r;
+}
+
+void citcom_gpu_destroy(citcom_gpu *h)
+{
+	if(!h)
+		return;
+	if(h->st)
+		cudaStreamSynchronize(h->st);
+	if(h->mg_exec)
+		cudaGraphExecDestroy(h->mg_exec);
+	for(void *p : h->allocs)
+		cudaFree(p);
+	if(h->hscal)
+		cudaFreeHost(h->hscal);
+	if(h->ev0)
+		cudaEventDestroy(h->ev0);
+	if(h->ev1)
+		cudaEventDestroy(h->ev1);
+	if(h->st)
+		cudaStreamDestroy(h->st);
+	delete h;
+}
+
+const char *citcom_gpu_error_string(const citcom_gpu *h) { return h ? h->err : "null handle"; }
+
+int citcom_gpu_level_dims(const citcom_gpu *h, int lev, int dims[6])
+{
+	if(!h || !dims || lev < 0 || lev >= h->L)
+		return CITCOM_GPU_ERR_ARG;
+	const Lvl &L = h->lv[lev];
+	dims[0] = L.nox;
+	dims[1] = L.noy;
+	dims[2] = L.noz;
+	dims[3] = L.nno;
+	dims[4] = L.nel;
+	dims[5] = L.neq;
+	return CITCOM_GPU_OK;
+}
+
+int citcom_gpu_get_system_viscosity(citcom_gpu *h, const double *T)
+{
+	TRY(check_handle(h));
+	const Lvl &Lf = h->lv[h->L - 1];
+	TRY(h2d(h, h->T, T, sizeof(double) * Lf.nno));
+	TRY(viscosity_from_device_T(h));
+	return sync(h);
+}
+
+int citcom_gpu_set_viscosity(citcom_gpu *h, int lev, const double *evi)
+{
+	TRY(check_handle(h));
+	TRY(check_level(h, lev));
+	TRY(h2d(h, h->evi[lev], evi, sizeof(double) * 8 * h->lv[lev].nel));
+	h->visc_ready = true;
+	return sync(h);
+}
+
+int citcom_gpu_get_viscosity(citcom_gpu *h, int lev, double *evi)
+{
+	TRY(check_handle(h));
+	TRY(check_level(h, lev));
+	TRY(d2h(h, evi, h->evi[lev], sizeof(double) * 8 * h->lv[lev].nel));
+	return sync(h);
+}
+
+int citcom_gpu_construct_stiffness_B_matrix(citcom_gpu *h)
+{
+	TRY(check_handle(h));
+	TRY(construct_stiffness(h));
+	return sync(h);
+}
+
+int citcom_gpu_assemble_forces(citcom_gpu *h, const double *T, double *F, double *buoyancy)
+{
+	TRY(check_handle(h));
+	const Lvl &Lf = h->lv[h->L - 1];
+	TRY(h2d(h, h->T, T, sizeof(double) * Lf.nno));
+	TRY(forces_from_device_T(h));
+	TRY(d2h(h, F, h->F, sizeof(double) * Lf.neq));
+	TRY(d2h(h, buoyancy, h->buoy, sizeof(double) * Lf.nno));
+	return sync(h);
+}
+
+int citcom_gpu_solve_Ahat_p_fhat_device(citcom_gpu *h, double *dV, double *dP, const double *dF, double imp, int *steps_max,
+                                        double *initial_residual)
+{
+	TRY(check_handle(h));
+	if(!dV || !dP || !dF || !steps_max)
+		return fail(h, CITCOM_GPU_ERR_ARG, "null argument");
+	h->stats.del2_calls = 0;
+	h->stats.mg_passes = 0;
+	CK(cudaEventRecord(h->ev0, h->st));
+	TRY(uzawa(h, dV, dP, dF, imp, steps_max, initial_residual));
+	CK(cudaEventRecord(h->ev1, h->st));
+	TRY(sync(h));
+	float ms = 0.f;
+	CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+	h->stats.stokes_ms = ms;
+	return CITCOM_GPU_OK;
+}
+
+int citcom_gpu_solve_Ahat_p_fhat(citcom_gpu *h, double *V, double *P, const double *F, double imp, int *steps_max,
+                                 double *initial_residual)
+{
+	TRY(check_handle(h));
+	const Lvl &Lf = h->lv[h->L - 1];
+	TRY(h2d(h, h->U, V, sizeof(double) * Lf.neq));
+	TRY(h2d(h, h->P, P, sizeof(double) * Lf.nel));
+	TRY(h2d(h, h->F, F, sizeof(double) * Lf.neq));
+	TRY(citcom_gpu_solve_Ahat_p_fhat_device(h, h->U, h->P, h->F, imp, steps_max, initial_residual));
+	TRY(d2h(h, V, h->U, sizeof(double) * Lf.neq));
+	TRY(d2h(h, P, h->P, sizeof(double) * Lf.nel));
+	return sync(h);
+}
+
+int citcom_gpu_solve_constrained_flow_iterative(citcom_gpu *h, double *U, double *P, const double *F, double *V)
+{
+	TRY(check_handle(h));
+	const Lvl &Lf = h->lv[h->L - 1];
+	int steps = h->cfg.piterations;
+	double r0;
+	TRY(h2d(h, h->U, U, sizeof(double) * Lf.neq));
+	TRY(h2d(h, h->P, P, sizeof(double) * Lf.nel));
+	TRY(h2d(h, h->F, F, sizeof(double) * Lf.neq));
+	TRY(citcom_gpu_solve_Ahat_p_fhat_device(h, h->U, h->P, h->F, h->cfg.accuracy, &steps, &r0));
+	launch_v_from_vector(h->st, Lf, h->U, h->V);
+	TRY(d2h(h, U, h->U, sizeof(double) * Lf.neq));
+	TRY(d2h(h, P, h->P, sizeof(double) * Lf.nel));
+	TRY(d2h(h, V, h->V, sizeof(double) * 3 * Lf.nno));
+	return sync(h);
+}
+
+int citcom_gpu_general_stokes_solver(citcom_gpu *h, const double *T, double *U, double *P, double *V)
+{
+	TRY(check_handle(h));
+	const Lvl &Lf = h->lv[h->L - 1];
+	TRY(h2d(h, h->T, T, sizeof(double) * Lf.nno));
+	TRY(h2d(h, h->U, U, sizeof(double) * Lf.neq));
+	TRY(h2d(h, h->P, P, sizeof(double) * Lf.nel));
+	TRY(stokes_resident(h));
+	TRY(d2h(h, U, h->U, sizeof(double) * Lf.neq));
+	TRY(d2h(h, P, h->P, sizeof(double) * Lf.nel));
+	TRY(d2h(h, V, h->V, sizeof(double) * 3 * Lf.nno));
+	return sync(h);
+}
+
+int citcom_gpu_PG_timestep(citcom_gpu *h, double *T, double *Tdot, const double *V, citcom_gpu_advection *adv)
+{
+	TRY(check_handle(h));
+	const Lvl &Lf = h->lv[h->L - 1];
+	TRY(h2d(h, h->T, T, sizeof(double) * Lf.nno));
+	TRY(h2d(h, h->Tdot, Tdot, sizeof(double) * Lf.nno));
+	TRY(h2d(h, h->V, V, sizeof(double) * 3 * Lf.nno));
+	TRY(pg_timestep(h, adv));
+	TRY(d2h(h, T, h->T, sizeof(double) * Lf.nno));
+	TRY(d2h(h, Tdot, h->Tdot, sizeof(double) * Lf.nno));
+	return sync(h);
+}
+
+int citcom_gpu_heat_flux(citcom_gpu *h, const double *T, const double *V, double *nut, double *nub)
+{
+	TRY(check_handle(h));
+	const int lmax = h->L - 1;
+	const Lvl &Lf = h->lv[lmax];
+	const double *dT = h->T, *dV = h->V;
+	if(T)
+		TRY(h2d(h, h->T, T, sizeof(double) * Lf.nno));
+	if(V)
+		TRY(h2d(h, h->V, V, sizeof(double) * 3 * Lf.nno));
+	launch_heat_flux(h->st, Lf, h->geo[lmax], dT, dV, h->hf_work, red_of(h), h->dscal + S_NU);
+	TRY(readback(h, S_NU, 2));
+	const double ns = 4.0 * (double)Lf.elx * (double)Lf.ely;
+	if(nut)
+		*nut = h->hscal[S_NU] / ns;
+	if(nub)
+		*nub = h->hscal[S_NU + 1] / ns;
+	return CITCOM_GPU_OK;
+}
+
+int citcom_gpu_vrms(citcom_gpu *h, const double *V, double *vrms)
+{
+	TRY(check_handle(h));
+	const int lmax = h->L - 1;
+	const Lvl &Lf = h->lv[lmax];
+	if(V)
+		TRY(h2d(h, h->V, V, sizeof(double) * 3 * Lf.nno));
+	launch_vrms(h->st, Lf, h->geo[lmax], h->V, red_of(h), h->dscal + S_VRMS);
+	TRY(readback(h, S_VRMS, 1));
+	if(vrms)
+		*vrms = std::sqrt(h->hscal[S_VRMS] / (8.0 * Lf.J * Lf.nel));
+	return CITCOM_GPU_OK;
+}
+
+int citcom_gpu_load_state(citcom_gpu *h, const double *T, const double *Tdot, const double *U, const double *P)
+{
+	TRY(check_handle(h));
+	const Lvl &Lf = h->lv[h->L - 1];
+	if(T)
+		TRY(h2d(h, h->T, T, sizeof(double) * Lf.nno));
+	if(Tdot)
+		TRY(h2d(h, h->Tdot, Tdot, sizeof(double) * Lf.nno));
+	if(U)
+		TRY(h2d(h, h->U, U, sizeof(double) * Lf.neq));
+	if(P)
+		TRY(h2d(h, h->P, P, sizeof(double) * Lf.nel));
+	return sync(h);
+}
+
+int citcom_gpu_store_state(citcom_gpu *h, double *T, double *Tdot, double *U, double *P, double *V)
+{
+	TRY(check_handle(h));
+	const Lvl &Lf = h->lv[h->L - 1];
+	TRY(d2h(h, T, h->T, sizeof(double) * Lf.nno));
+	TRY(d2h(h, Tdot, h->Tdot, sizeof(double) * Lf.nno));
+	TRY(d2h(h, U, h->U, sizeof(double) * Lf.neq));
+	TRY(d2h(h, P, h->P, sizeof(double) * Lf.nel));
+	TRY(d2h(h, V, h->V, sizeof(double) * 3 * Lf.nno));
+	return sync(h);
+}
+
+int citcom_gpu_stokes_resident(citcom_gpu *h)
+{
+	TRY(check_handle(h));
+	TRY(stokes_resident(h));
+	return sync(h);
+}
+
+int citcom_gpu_step_resident(citcom_gpu *h, citcom_gpu_advection *adv)
+{
+	TRY(check_handle(h));
+	TRY(pg_timestep(h, adv));
+	TRY(stokes_resident(h));
+	return sync(h);
+}
+
+int citcom_gpu_last_stats(const citcom_gpu *h, citcom_gpu_stats *s)
+{
+	if(!h || !s)
+		return CITCOM_GPU_ERR_ARG;
+	*s = h->stats;
+	return CITCOM_GPU_OK;
+}
+
+// ------------------------------------------------------------ single operators
+
+int citcom_gpu_op_kmul(citcom_gpu *h, int lev, const double *u, double *Au)
+{
+	TRY(check_handle(h));
+	TRY(check_level(h, lev));
+	if(!h->stiffness_ready)
+		return fail(h, CITCOM_GPU_ERR_STATE, "construct_stiffness_B_matrix has not been called");
+	const Lvl &L = h->lv[lev];
+	double *du, *dA;
+	if(h->cfg.precision == CITCOM_GPU_FP64 || lev == h->L - 1)
+	{
+		du = h->cfg.precision == CITCOM_GPU_FP64 ? h->mg64.del[lev] : h->r64;
+		dA = h->cfg.precision == CITCOM_GPU_FP64 ? h->mg64.AU[lev] : h->Ah;
+		TRY(h2d(h, du, u, sizeof(double) * L.neq));
+		launch_kmul<double>(h->st, L, h->K64[lev], du, dA);
+		TRY(d2h(h, Au, dA, sizeof(double) * L.neq));
+		return sync(h);
+	}
+	// FP32 stencil of a coarse level in mixed mode
+	std::vector<float> uf(L.neq), af(L.neq);
+	for(int i = 0; i < L.neq; ++i)
+		uf[i] = (float)u[i];
+	TRY(h2d(h, h->mg32.del[lev], uf.data(), sizeof(float) * L.neq));
+	launch_kmul<float>(h->st, L, h->K32[lev], h->mg32.del[lev], h->mg32.AU[lev]);
+	TRY(d2h(h, af.data(), h->mg32.AU[lev], sizeof(float) * L.neq));
+	TRY(sync(h));
+	for(int i = 0; i < L.neq; ++i)
+		Au[i] = af[i];
+	return CITCOM_GPU_OK;
+}
+
+int citcom_gpu_op_gauss_seidel(citcom_gpu *h, int lev, double *d0, const double *F, double *Ad, int cycles, int guess)
+{
+	TRY(check_handle(h));
+	TRY(check_level(h, lev));
+	if(h->cfg.precision != CITCOM_GPU_FP64)
+		return fail(h, CITCOM_GPU_ERR_STATE, "op_gauss_seidel is provided for the FP64 configuration");
+	if(!h->stiffness_ready)
+		return fail(h, CITCOM_GPU_ERR_STATE, "construct_stiffness_B_matrix has not been called");
+	const Lvl &L = h->lv[lev];
+	MG<double> &B = h->mg64;
+	TRY(h2d(h, B.rhs[lev], F, sizeof(double) * L.neq));
+	if(guess)
+		TRY(h2d(h, B.vel[lev], d0, sizeof(double) * L.neq));
+	gs<double>(h, B, lev, B.vel[lev], B.rhs[lev], cycles, !guess);
+	launch_kmul<double>(h->st, L, B.K[lev], B.vel[lev], B.AU[lev]);
+	TRY(d2h(h, d0, B.vel[lev], sizeof(double) * L.neq));
+	TRY(d2h(h, Ad, B.AU[lev], sizeof(double) * L.neq));
+	return sync(h);
+}
+
+int citcom_gpu_op_project(citcom_gpu *h, int fine_lev, const double *AU, double *AD)
+{
+	TRY(check_handle(h));
+	TRY(check_level(h, fine_lev));
+	if(fine_lev < 1)
+		return fail(h, CITCOM_GPU_ERR_ARG, "no level below %d", fine_lev);
+	const Lvl &Lf = h->lv[fine_lev], &Lc = h->lv[fine_lev - 1];
+	double *src, *dst;
+	if(h->cfg.precision == CITCOM_GPU_FP64)
+	{
+		src = h->mg64.del[fine_lev];
+		dst = h->mg64.AU[fine_lev - 1];
+	}
+	else
+	{
+		src = h->r64;
+		dst = h->Ah;
+	}
+	TRY(h2d(h, src, AU, sizeof(double) * Lf.neq));
+	launch_project<double>(h->st, Lf, Lc, src, dst);
+	TRY(d2h(h, AD, dst, sizeof(double) * Lc.neq));
+	return sync(h);
+}
+
+int citcom_gpu_op_interp(citcom_gpu *h, int coarse_lev, const double *AD, double *AU)
+{
+	TRY(check_handle(h));
+	TRY(check_level(h, coarse_lev));
+	if(coarse_lev >= h->L - 1)
+		return fail(h, CITCOM_GPU_ERR_ARG, "no level above %d", coarse_lev);
+	const Lvl &Lc = h->lv[coarse_lev], &Lf = h->lv[coarse_lev + 1];
+	double *src, *dst;
+	if(h->cfg.precision == CITCOM_GPU_FP64)
+	{
+		src = h->mg64.del[coarse_lev];
+		dst = h->mg64.AU[coarse_lev + 1];
+	}
+	else
+	{
+		src = h->r64;
+		dst = h->Ah;
+	}
+	TRY(h2d(h, src, AD, sizeof(double) * Lc.neq));
+	launch_interp<double>(h->st, Lc, Lf, src, dst);
+	TRY(d2h(h, AU, dst, sizeof(double) * Lf.neq));
+	return sync(h);
+}
+
+int citcom_gpu_op_div(citcom_gpu *h, int lev, const double *U, double *divU)
+{
+	TRY(check_handle(h));
+	TRY(check_level(h, lev));
+	const Lvl &L = h->lv[lev];
+	TRY(h2d(h, h->r64, U, sizeof(double) * L.neq));
+	launch_div(h->st, L, h->geo[lev], h->r64, h->Eres);
+	TRY(d2h(h, divU, h->Eres, sizeof(double) * L.nel));
+	return sync(h);
+}
+
+int citcom_gpu_op_grad(citcom_gpu *h, int lev, const double *P, double *gradP)
+{
+	TRY(check_handle(h));
+	TRY(check_level(h, lev));
+	const Lvl &L = h->lv[lev];
+	TRY(h2d(h, h->Eres, P, sizeof(double) * L.nel));
+	launch_grad(h->st, L, h->geo[lev], h->Eres, h->r64);
+	TRY(d2h(h, gradP, h->r64, sizeof(double) * L.neq));
+	return sync(h);
+}
+
+int citcom_gpu_op_multi_grid(citcom_gpu *h, double *d1, double *F, double *residual)
+{
+	TRY(check_handle(h));
+	if(h->cfg.precision != CITCOM_GPU_FP64)
+		return fail(h, CITCOM_GPU_ERR_STATE, "op_multi_grid is provided for the FP64 configuration");
+	if(!h->stiffness_ready)
+		return fail(h, CITCOM_GPU_ERR_STATE, "construct_stiffness_B_matrix has not been called");
+	const int lmax = h->L - 1;
+	const Lvl &Lf = h->lv[lmax];
+	TRY(h2d(h, h->mg64.fl[lmax], F, sizeof(double) * Lf.neq));
+	mg_pass<double>(h, h->mg64);
+	launch_dot(h->st, Lf.neq, h->mg64.res[lmax], h->mg64.res[lmax], red_of(h), h->dscal + S_RES);
+	TRY(d2h(h, d1, h->mg64.vel[lmax], sizeof(double) * Lf.neq));
+	TRY(d2h(h, F, h->mg64.res[lmax], sizeof(double) * Lf.neq));
+	TRY(readback(h, S_RES, 1));
+	if(residual)
+		*residual = std::sqrt(h->hscal[S_RES] / Lf.neq);
+	return sync(h);
+}
+
+int citcom_gpu_op_solve_del2_u(citcom_gpu *h, double *d0, const double *F, double acc, int *valid)
+{
+	TRY(check_handle(h));
+	if(!h->stiffness_ready)
+		return fail(h, CITCOM_GPU_ERR_STATE, "construct_stiffness_B_matrix has not been called");
+	const Lvl &Lf = h->lv[h->L - 1];
+	int v = 0;
+	TRY(h2d(h, h->Ah, F, sizeof(double) * Lf.neq));
+	h->stats.mg_passes = 0;
+	h->stats.del2_calls = 0;
+	TRY(solve_del2_u(h, acc, &v));
+	TRY(d2h(h, d0, h->u1, sizeof(double) * Lf.neq));
+	if(valid)
+		*valid = v;
+	return sync(h);
+}
+
+int citcom_gpu_op_diagonals(citcom_gpu *h, int lev, double *BI, double *BPI)
+{
+	TRY(check_handle(h));
+	TRY(check_level(h, lev));
+	if(!h->stiffness_ready)
+		return fail(h, CITCOM_GPU_ERR_STATE, "construct_stiffness_B_matrix has not been called");
+	const Lvl &L = h->lv[lev];
+	if(BI)
+	{
+		std::vector<double> bi(3 * (size_t)L.npad);
+		std::vector<float> bf;
+		if(h->BI64[lev])
+			TRY(d2h(h, bi.data(), h->BI64[lev], sizeof(double) * 3 * L.npad));
+		else
+		{
+			bf.resize(3 * (size_t)L.npad);
+			TRY(d2h(h, bf.data(), h->BI32[lev], sizeof(float) * 3 * L.npad));
+		}
+		TRY(sync(h));
+		for(int y = 0; y < L.noy; ++y)
+			for(int x = 0; x < L.nox; ++x)
+				for(int z = 0; z < L.noz; ++z)
+				{
+					const int n = cg_node(L, x, y, z), p = cg_pos(L, x, y, z);
+					for(int d = 0; d < 3; ++d)
+						BI[3 * n + d] = h->BI64[lev] ? bi[(size_t)d * L.npad + p] : (double)bf[(size_t)d * L.npad + p];
+				}
+	}
+	if(BPI)
+	{
+		if(lev != h->L - 1)
+			return fail(h, CITCOM_GPU_ERR_ARG, "BPI is kept for the finest level only");
+		TRY(d2h(h, BPI, h->BPI, sizeof(double) * L.nel));
+	}
+	return sync(h);
+}
+
+} // extern "C"

@@ -1,0 +1,1406 @@
+// sm_103a kernels for CitcomCU's Stokes / SUPG hot path.
+//
+// Design (one GPU, whole mesh resident in HBM):
+//  * The velocity operator is the node-assembled 27-point block stencil of
+//    the reference (n_assemble_del2_u, Element_calculations.c:552-621, whose
+//    coefficients construct_node_ks, Construct_arrays.c:359-535, builds) but
+//    stored in full (243 coefficients per node) and colour-major
+//    structure-of-arrays, so every kernel streams coalesced coefficients and
+//    gathers its 27 neighbours node-centred: no atomics anywhere.
+//  * The lexicographic node-block Gauss-Seidel (gauss_seidel,
+//    General_matrix_functions.c:1160-1361) becomes an 8-colour sweep with the
+//    same per-node update (the node's 3 dofs relaxed together with 1/diag).
+//  * Restriction / prolongation are node-centred gathers.
+//  * Reductions are deterministic: fixed grids, per-block partials, the last
+//    block sums partials in block order.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+
+#include "kernels.h"
+
+namespace {
+
+constexpr int TPB = 256;
+
+inline int nblocks(long n, int tpb = TPB) { return (int)((n + tpb - 1) / tpb); }
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+__device__ __forceinline__ int colour_of_pos(const Lvl &L, int p)
+{
+	int c = 0;
+#pragma unroll
+	for(int k = 1; k < 8; ++k)
+		c += (p >= L.coff[k]);
+	return c;
+}
+
+template <typename T> __device__ __forceinline__ T ldcs(const T *p) { return __ldcs(p); }
+
+// ---------------------------------------------------------------- reduce
+
+template <int NV>
+__device__ __forceinline__ void block_reduce_store(double (&v)[NV], Red red, double *out)
+{
+	__shared__ double sh[RED_THREADS / 32][NV];
+	__shared__ bool last;
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+	for(int i = 0; i < NV; ++i)
+		for(int o = 16; o > 0; o >>= 1)
+			v[i] += __shfl_down_sync(0xffffffffu, v[i], o);
+	if(lane == 0)
+#pragma unroll
+		for(int i = 0; i < NV; ++i)
+			sh[warp][i] = v[i];
+	__syncthreads();
+	if(threadIdx.x == 0)
+	{
+		for(int i = 0; i < NV; ++i)
+		{
+			double s = 0.0;
+			for(int w = 0; w < (int)(blockDim.x >> 5); ++w)
+				s += sh[w][i];
+			red.partials[blockIdx.x * NV + i] = s;
+		}
+		__threadfence();
+		const unsigned t = atomicAdd(red.counter, 1u);
+		last = (t == gridDim.x - 1);
+	}
+	__syncthreads();
+	if(last)
+	{
+		__threadfence();
+		// fixed-order sum of the partials by the last block
+		for(int i = 0; i < NV; ++i)
+		{
+			double s = 0.0;
+			for(int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+				s += __ldcg(red.partials + b * NV + i);
+			for(int o = 16; o > 0; o >>= 1)
+				s += __shfl_down_sync(0xffffffffu, s, o);
+			if(lane == 0)
+				sh[warp][0] = s;
+			__syncthreads();
+			if(threadIdx.x == 0)
+			{
+				double t = 0.0;
+				for(int w = 0; w < (int)(blockDim.x >> 5); ++w)
+					t += sh[w][0];
+				out[i] = t;
+			}
+			__syncthreads();
+		}
+		if(threadIdx.x == 0)
+			*red.counter = 0u;
+	}
+}
+
+inline int red_grid(long n)
+{
+	int g = nblocks(n, RED_THREADS);
+	return g < 1 ? 1 : (g > RED_MAX_BLOCKS ? RED_MAX_BLOCKS : g);
+}
+
+// ---------------------------------------------------------------- assemble
+
+// One thread per node (colour-major position): builds the node's 27 3x3
+// blocks from the elements it shares with each neighbour.  K_e follows
+// get_elt_k's Cartesian branch (Element_calculations.c:223-247) plus the
+// augmented-Lagrangian term of get_aug_k (:1127-1163); rows of constrained
+// dofs and columns of constrained neighbour dofs are zero
+// (construct_node_ks, Construct_arrays.c:409-505); BI = 1/diag of the
+// unmasked K (build_diagonal_of_K, Element_calculations.c:624-652).
+__global__ void k_assemble(Lvl L, const Geo *__restrict__ geo, const double *__restrict__ evi, int aug, double lambda,
+                           double *__restrict__ K64, float *__restrict__ K32, double *__restrict__ BI64, float *__restrict__ BI32)
+{
+	const int p = blockIdx.x * blockDim.x + threadIdx.x;
+	if(p >= L.nno)
+		return;
+	const int c = colour_of_pos(L, p);
+	int x, y, z;
+	cg_decode(L, c, p - L.coff[c], x, y, z);
+	const unsigned fn = cg_vflag(L, x, y, z);
+	double diag[3] = {0.0, 0.0, 0.0};
+
+	for(int s = 0; s < 27; ++s)
+	{
+		const int dz = s % 3 - 1, dx = (s / 3) % 3 - 1, dy = s / 9 - 1;
+		double blk[9];
+#pragma unroll
+		for(int q = 0; q < 9; ++q)
+			blk[q] = 0.0;
+		const int mx = x + dx, my = y + dy, mz = z + dz;
+		const bool inside = mx >= 0 && mx < L.nox && my >= 0 && my < L.noy && mz >= 0 && mz < L.noz;
+		if(inside)
+		{
+			const unsigned fm = cg_vflag(L, mx, my, mz);
+			// elements holding both n and m: corner (ox,oy,oz) of n with (o+d) in {0,1}
+			for(int oy = 0; oy < 2; ++oy)
+			{
+				if(oy + dy < 0 || oy + dy > 1 || y - oy < 0 || y - oy >= L.ely)
+					continue;
+				for(int ox = 0; ox < 2; ++ox)
+				{
+					if(ox + dx < 0 || ox + dx > 1 || x - ox < 0 || x - ox >= L.elx)
+						continue;
+					for(int oz = 0; oz < 2; ++oz)
+					{
+						if(oz + dz < 0 || oz + dz > 1 || z - oz < 0 || z - oz >= L.elz)
+							continue;
+						const int e = (z - oz) + L.elz * ((x - ox) + L.elx * (y - oy));
+						const int a = cg_local_index(ox, oy, oz);
+						const int b = cg_local_index(ox + dx, oy + dy, oz + dz);
+						double eta[8], mean = 0.0;
+#pragma unroll
+						for(int k = 0; k < 8; ++k)
+						{
+							eta[k] = evi[8 * e + k];
+							mean += eta[k];
+						}
+						mean *= 0.125;
+#pragma unroll
+						for(int q = 0; q < 9; ++q)
+						{
+							double v = 0.0;
+#pragma unroll
+							for(int k = 0; k < 8; ++k)
+								v += eta[k] * geo->Mk[k][a][b][q];
+							if(aug)
+								v += mean * lambda * geo->g[3 * a + q / 3] * geo->g[3 * b + q % 3];
+							blk[q] += v;
+						}
+						if(s == 13)
+						{
+							// unmasked diagonal for BI
+#pragma unroll
+							for(int i = 0; i < 3; ++i)
+							{
+								double v = 0.0;
+#pragma unroll
+								for(int k = 0; k < 8; ++k)
+									v += eta[k] * geo->Mk[k][a][a][4 * i];
+								if(aug)
+									v += mean * lambda * geo->g[3 * a + i] * geo->g[3 * a + i];
+								diag[i] += v;
+							}
+						}
+					}
+				}
+			}
+#pragma unroll
+			for(int i = 0; i < 3; ++i)
+#pragma unroll
+				for(int j = 0; j < 3; ++j)
+					if(((fn >> i) & 1u) || ((fm >> j) & 1u))
+						blk[3 * i + j] = 0.0;
+		}
+#pragma unroll
+		for(int q = 0; q < 9; ++q)
+		{
+			const size_t off = (size_t)(9 * s + q) * L.npad + p;
+			if(K64)
+				K64[off] = blk[q];
+			if(K32)
+				K32[off] = (float)blk[q];
+		}
+	}
+#pragma unroll
+	for(int i = 0; i < 3; ++i)
+	{
+		const double bi = 1.0 / diag[i];
+		if(BI64)
+			BI64[(size_t)i * L.npad + p] = bi;
+		if(BI32)
+			BI32[(size_t)i * L.npad + p] = (float)bi;
+	}
+}
+
+// build_diagonal_of_Ahat / assemble_dAhatp_entry (Element_calculations.c:654-689, 771-829)
+__global__ void k_bpi(Lvl L, const Geo *__restrict__ geo, const double *__restrict__ BI, double *__restrict__ BPI, int precond)
+{
+	const int e = blockIdx.x * blockDim.x + threadIdx.x;
+	if(e >= L.nel)
+		return;
+	if(!precond)
+	{
+		BPI[e] = 1.0;
+		return;
+	}
+	const int ez = e % L.elz, ex = (e / L.elz) % L.elx, ey = e / (L.elz * L.elx);
+	double bu = 0.0;
+	for(int a = 0; a < 8; ++a)
+	{
+		const int p = cg_pos(L, ex + cg_loc(a, 0), ey + cg_loc(a, 1), ez + cg_loc(a, 2));
+#pragma unroll
+		for(int i = 0; i < 3; ++i)
+		{
+			const double g = geo->g[3 * a + i];
+			bu += g * g * BI[(size_t)i * L.npad + p];
+		}
+	}
+	BPI[e] = (bu != 0.0) ? 1.0 / bu : 1.0;
+}
+
+// ---------------------------------------------------------------- stencil
+
+// row product of node (x,y,z) at colour-major position p: out = sum_m K_{n,m} u_m.
+// Neighbours outside the mesh are clamped onto the mesh; their coefficients
+// are zero, so they contribute nothing.
+// `u` is deliberately not __restrict__: the single-CTA smoother reads values
+// that other threads of the block wrote in the previous colour.
+template <typename T>
+__device__ __forceinline__ void row_product(const Lvl &L, const T *__restrict__ K, const T *u, int p, int x, int y,
+                                            int z, T &o0, T &o1, T &o2)
+{
+	T a0 = 0, a1 = 0, a2 = 0;
+	const size_t np = (size_t)L.npad;
+	const T *kp = K + p;
+#pragma unroll
+	for(int dy = -1; dy <= 1; ++dy)
+	{
+		const int yy = clampi(y + dy, 0, L.noy - 1);
+#pragma unroll
+		for(int dx = -1; dx <= 1; ++dx)
+		{
+			const int xx = clampi(x + dx, 0, L.nox - 1);
+			const int base = L.noz * (xx + L.nox * yy);
+#pragma unroll
+			for(int dz = -1; dz <= 1; ++dz)
+			{
+				const int zz = clampi(z + dz, 0, L.noz - 1);
+				const int m = base + zz;
+				const int s = (dz + 1) + 3 * (dx + 1) + 9 * (dy + 1);
+				const T *kc = kp + (size_t)(9 * s) * np;
+				const T u0 = u[3 * m], u1 = u[3 * m + 1], u2 = u[3 * m + 2];
+				a0 += ldcs(kc + 0 * np) * u0 + ldcs(kc + 1 * np) * u1 + ldcs(kc + 2 * np) * u2;
+				a1 += ldcs(kc + 3 * np) * u0 + ldcs(kc + 4 * np) * u1 + ldcs(kc + 5 * np) * u2;
+				a2 += ldcs(kc + 6 * np) * u0 + ldcs(kc + 7 * np) * u1 + ldcs(kc + 8 * np) * u2;
+			}
+		}
+	}
+	o0 = a0;
+	o1 = a1;
+	o2 = a2;
+}
+
+// MODE 0: out = K u;  MODE 1: out = f - K u
+template <typename T, int MODE>
+__global__ void k_kmul(Lvl L, const T *__restrict__ K, const T *__restrict__ u, const T *__restrict__ f, T *__restrict__ out)
+{
+	const int c = blockIdx.y;
+	const int q = blockIdx.x * blockDim.x + threadIdx.x;
+	if(q >= L.coff[c + 1] - L.coff[c])
+		return;
+	int x, y, z;
+	cg_decode(L, c, q, x, y, z);
+	const int p = L.coff[c] + q;
+	const int n = cg_node(L, x, y, z);
+	T r0, r1, r2;
+	row_product(L, K, u, p, x, y, z, r0, r1, r2);
+	if(MODE == 1)
+	{
+		r0 = f[3 * n] - r0;
+		r1 = f[3 * n + 1] - r1;
+		r2 = f[3 * n + 2] - r2;
+	}
+	out[3 * n] = r0;
+	out[3 * n + 1] = r1;
+	out[3 * n + 2] = r2;
+}
+
+// AU = K u together with AU.AU and AU.res (the line search of multi_grid,
+// General_matrix_functions.c:626-630); out2[0] = AU.res, out2[1] = AU.AU
+template <typename T>
+__global__ void k_kmul_ls(Lvl L, const T *__restrict__ K, const T *__restrict__ u, const T *__restrict__ res, T *__restrict__ Au,
+                          Red red, double *out2)
+{
+	double v[2] = {0.0, 0.0};
+	for(int p = blockIdx.x * blockDim.x + threadIdx.x; p < L.nno; p += gridDim.x * blockDim.x)
+	{
+		const int c = colour_of_pos(L, p);
+		int x, y, z;
+		cg_decode(L, c, p - L.coff[c], x, y, z);
+		const int n = cg_node(L, x, y, z);
+		T r0, r1, r2;
+		row_product(L, K, u, p, x, y, z, r0, r1, r2);
+		Au[3 * n] = r0;
+		Au[3 * n + 1] = r1;
+		Au[3 * n + 2] = r2;
+		v[0] += (double)r0 * (double)res[3 * n] + (double)r1 * (double)res[3 * n + 1] + (double)r2 * (double)res[3 * n + 2];
+		v[1] += (double)r0 * (double)r0 + (double)r1 * (double)r1 + (double)r2 * (double)r2;
+	}
+	block_reduce_store<2>(v, red, out2);
+}
+
+// vel += alpha del ; res -= alpha AU (finest level only); alpha = num/den
+template <typename T>
+__global__ void k_vel_update(int n, T *__restrict__ vel, const T *__restrict__ del, T *__restrict__ res, const T *__restrict__ AU,
+                             const double *__restrict__ nd, int update_res)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i >= n)
+		return;
+	const double alpha = nd[0] / nd[1];
+	vel[i] += (T)(alpha * (double)del[i]);
+	if(update_res)
+		res[i] -= (T)(alpha * (double)AU[i]);
+}
+
+// one Gauss-Seidel colour: d_n += (F_n - sum_m K_{n,m} d_m) o BI_n
+template <typename T>
+__global__ void k_gs_colour(Lvl L, const T *__restrict__ K, const T *__restrict__ BI, const T *__restrict__ F, T *d, int c)
+{
+	const int q = blockIdx.x * blockDim.x + threadIdx.x;
+	if(q >= L.coff[c + 1] - L.coff[c])
+		return;
+	int x, y, z;
+	cg_decode(L, c, q, x, y, z);
+	const int p = L.coff[c] + q;
+	const int n = cg_node(L, x, y, z);
+	T r0, r1, r2;
+	row_product(L, K, d, p, x, y, z, r0, r1, r2);
+	const size_t np = (size_t)L.npad;
+	d[3 * n] += (F[3 * n] - r0) * BI[p];
+	d[3 * n + 1] += (F[3 * n + 1] - r1) * BI[np + p];
+	d[3 * n + 2] += (F[3 * n + 2] - r2) * BI[2 * np + p];
+}
+
+// all sweeps and colours of one gauss_seidel call on a small level in one CTA
+constexpr int GS_SMALL_THREADS = 1024;
+template <typename T>
+__global__ void __launch_bounds__(GS_SMALL_THREADS) k_gs_small(Lvl L, const T *__restrict__ K, const T *__restrict__ BI,
+                                                               const T *__restrict__ F, T *d, int cycles, int zero_start)
+{
+	if(zero_start)
+		for(int i = threadIdx.x; i < L.neq; i += blockDim.x)
+			d[i] = 0;
+	__syncthreads();
+	const size_t np = (size_t)L.npad;
+	for(int cyc = 0; cyc < cycles; ++cyc)
+		for(int c = 0; c < 8; ++c)
+		{
+			const int nc = L.coff[c + 1] - L.coff[c];
+			for(int q = threadIdx.x; q < nc; q += blockDim.x)
+			{
+				int x, y, z;
+				cg_decode(L, c, q, x, y, z);
+				const int p = L.coff[c] + q;
+				const int n = cg_node(L, x, y, z);
+				T r0, r1, r2;
+				row_product(L, K, d, p, x, y, z, r0, r1, r2);
+				d[3 * n] += (F[3 * n] - r0) * BI[p];
+				d[3 * n + 1] += (F[3 * n + 1] - r1) * BI[np + p];
+				d[3 * n + 2] += (F[3 * n + 2] - r2) * BI[2 * np + p];
+			}
+			__syncthreads();
+		}
+}
+
+// ---------------------------------------------------------------- transfers
+
+// project_vector (Solver_multigrid.c:72-159) at one coarse node, followed by
+// strip_bcs_from_residual on the coarse level
+template <typename T>
+__global__ void k_project(Lvl Lf, Lvl Lc, const T *__restrict__ AU, T *__restrict__ AD)
+{
+	const int N = blockIdx.x * blockDim.x + threadIdx.x;
+	if(N >= Lc.nno)
+		return;
+	const int Z = N % Lc.noz, X = (N / Lc.noz) % Lc.nox, Y = N / (Lc.noz * Lc.nox);
+	double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+	int cnt = 0;
+	for(int a = 0; a < 8; ++a)
+	{
+		const int ox = cg_loc(a, 0), oy = cg_loc(a, 1), oz = cg_loc(a, 2);
+		const int ex = X - ox, ey = Y - oy, ez = Z - oz;
+		if(ex < 0 || ex >= Lc.elx || ey < 0 || ey >= Lc.ely || ez < 0 || ez >= Lc.elz)
+			continue;
+		++cnt;
+		// fine sub-element at corner a of the coarse element
+		const int fx = 2 * ex + ox, fy = 2 * ey + oy, fz = 2 * ez + oz;
+		double t0 = 0.0, t1 = 0.0, t2 = 0.0;
+		for(int b = 0; b < 8; ++b)
+		{
+			const int m = cg_node(Lf, fx + cg_loc(b, 0), fy + cg_loc(b, 1), fz + cg_loc(b, 2));
+			t0 += (double)AU[3 * m];
+			t1 += (double)AU[3 * m + 1];
+			t2 += (double)AU[3 * m + 2];
+		}
+		s0 += Lc.J * t0;
+		s1 += Lc.J * t1;
+		s2 += Lc.J * t2;
+	}
+	const double mass = 1.0 / ((double)cnt * Lc.J);
+	const unsigned f = cg_vflag(Lc, X, Y, Z);
+	AD[3 * N] = (f & 1u) ? (T)0 : (T)(s0 * mass);
+	AD[3 * N + 1] = (f & 2u) ? (T)0 : (T)(s1 * mass);
+	AD[3 * N + 2] = (f & 4u) ? (T)0 : (T)(s2 * mass);
+}
+
+// interp_vector (Solver_multigrid.c:173-298): injection, then linear fill
+// along x (y,z even), along z (y even) and along y, in that order; evaluated
+// per fine node with the same operation order.  Strips the fine level.
+template <typename T> __device__ __forceinline__ T coarse_at(const Lvl &Lc, const T *AD, int x, int y, int z, int d)
+{
+	return AD[3 * cg_node(Lc, x >> 1, y >> 1, z >> 1) + d];
+}
+template <typename T> __device__ __forceinline__ T fill_x(const Lvl &Lc, const T *AD, int x, int y, int z, int d)
+{
+	if(x & 1)
+		return (T)0.5 * coarse_at(Lc, AD, x - 1, y, z, d) + (T)0.5 * coarse_at(Lc, AD, x + 1, y, z, d);
+	return coarse_at(Lc, AD, x, y, z, d);
+}
+template <typename T> __device__ __forceinline__ T fill_z(const Lvl &Lc, const T *AD, int x, int y, int z, int d)
+{
+	if(z & 1)
+		return (T)0.5 * fill_x(Lc, AD, x, y, z - 1, d) + (T)0.5 * fill_x(Lc, AD, x, y, z + 1, d);
+	return fill_x(Lc, AD, x, y, z, d);
+}
+template <typename T>
+__global__ void k_interp(Lvl Lc, Lvl Lf, const T *__restrict__ AD, T *__restrict__ AU)
+{
+	const int n = blockIdx.x * blockDim.x + threadIdx.x;
+	if(n >= Lf.nno)
+		return;
+	const int z = n % Lf.noz, x = (n / Lf.noz) % Lf.nox, y = n / (Lf.noz * Lf.nox);
+	const unsigned f = cg_vflag(Lf, x, y, z);
+#pragma unroll
+	for(int d = 0; d < 3; ++d)
+	{
+		T v;
+		if(y & 1)
+			v = (T)0.5 * fill_z(Lc, AD, x, y - 1, z, d) + (T)0.5 * fill_z(Lc, AD, x, y + 1, z, d);
+		else
+			v = fill_z(Lc, AD, x, y, z, d);
+		AU[3 * n + d] = ((f >> d) & 1u) ? (T)0 : v;
+	}
+}
+
+// ---------------------------------------------------------------- div / grad
+
+// assemble_div_u (Element_calculations.c:691-722)
+__global__ void k_div(Lvl L, const Geo *__restrict__ geo, const double *__restrict__ U, double *__restrict__ divU)
+{
+	const int e = blockIdx.x * blockDim.x + threadIdx.x;
+	if(e >= L.nel)
+		return;
+	const int ez = e % L.elz, ex = (e / L.elz) % L.elx, ey = e / (L.elz * L.elx);
+	double s = 0.0;
+#pragma unroll
+	for(int a = 0; a < 8; ++a)
+	{
+		const int n = cg_node(L, ex + cg_loc(a, 0), ey + cg_loc(a, 1), ez + cg_loc(a, 2));
+		s += geo->g[3 * a] * U[3 * n] + geo->g[3 * a + 1] * U[3 * n + 1] + geo->g[3 * a + 2] * U[3 * n + 2];
+	}
+	divU[e] = s;
+}
+
+// assemble_grad_p (Element_calculations.c:727-769) as a node-centred gather
+__global__ void k_grad(Lvl L, const Geo *__restrict__ geo, const double *__restrict__ P, double *__restrict__ gradP)
+{
+	const int n = blockIdx.x * blockDim.x + threadIdx.x;
+	if(n >= L.nno)
+		return;
+	const int z = n % L.noz, x = (n / L.noz) % L.nox, y = n / (L.noz * L.nox);
+	double g0 = 0.0, g1 = 0.0, g2 = 0.0;
+	for(int a = 0; a < 8; ++a)
+	{
+		const int ex = x - cg_loc(a, 0), ey = y - cg_loc(a, 1), ez = z - cg_loc(a, 2);
+		if(ex < 0 || ex >= L.elx || ey < 0 || ey >= L.ely || ez < 0 || ez >= L.elz)
+			continue;
+		const double p = P[ez + L.elz * (ex + L.elx * ey)];
+		g0 += geo->g[3 * a] * p;
+		g1 += geo->g[3 * a + 1] * p;
+		g2 += geo->g[3 * a + 2] * p;
+	}
+	const unsigned f = cg_vflag(L, x, y, z);
+	gradP[3 * n] = (f & 1u) ? 0.0 : g0;
+	gradP[3 * n + 1] = (f & 2u) ? 0.0 : g1;
+	gradP[3 * n + 2] = (f & 4u) ? 0.0 : g2;
+}
+
+__global__ void k_strip(Lvl L, double *r)
+{
+	const int n = blockIdx.x * blockDim.x + threadIdx.x;
+	if(n >= L.nno)
+		return;
+	const int z = n % L.noz, x = (n / L.noz) % L.nox, y = n / (L.noz * L.nox);
+	const unsigned f = cg_vflag(L, x, y, z);
+	for(int d = 0; d < 3; ++d)
+		if((f >> d) & 1u)
+			r[3 * n + d] = 0.0;
+}
+
+// ---------------------------------------------------------------- vectors
+
+__global__ void k_dot(int n, const double *__restrict__ a, const double *__restrict__ b, Red red, double *out)
+{
+	double v[1] = {0.0};
+	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+		v[0] += a[i] * b[i];
+	block_reduce_store<1>(v, red, out);
+}
+
+__global__ void k_dots4(int n, const double *a0, const double *b0, const double *a1, const double *b1, const double *a2,
+                        const double *b2, const double *a3, const double *b3, Red red, double *out)
+{
+	double v[4] = {0.0, 0.0, 0.0, 0.0};
+	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+	{
+		if(a0)
+			v[0] += a0[i] * b0[i];
+		if(a1)
+			v[1] += a1[i] * b1[i];
+		if(a2)
+			v[2] += a2[i] * b2[i];
+		if(a3)
+			v[3] += a3[i] * b3[i];
+	}
+	block_reduce_store<4>(v, red, out);
+}
+
+__global__ void k_axpby(int n, double *y, double a, const double *x, double b)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i < n)
+		y[i] = a * y[i] + b * x[i];
+}
+
+__global__ void k_mul(int n, double *z, const double *a, const double *b)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i < n)
+		z[i] = a[i] * b[i];
+}
+
+__global__ void k_lin2(int n, double *z, double a, const double *x, double b, const double *y)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i < n)
+		z[i] = a * x[i] + b * y[i];
+}
+
+__global__ void k_sub3(int n, double *z, const double *f, const double *a, const double *b)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i < n)
+		z[i] = f[i] - a[i] - b[i];
+}
+
+__global__ void k_d2f(int n, float *dst, const double *src)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i < n)
+		dst[i] = (float)src[i];
+}
+
+__global__ void k_add_f2d(int n, double *dst, const float *src)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i < n)
+		dst[i] += (double)src[i];
+}
+
+// r = f - K u in FP64 with r.r
+__global__ void k_residual64(Lvl L, const double *__restrict__ K, const double *__restrict__ f, const double *__restrict__ u,
+                             double *__restrict__ r, Red red, double *out)
+{
+	double v[1] = {0.0};
+	for(int p = blockIdx.x * blockDim.x + threadIdx.x; p < L.nno; p += gridDim.x * blockDim.x)
+	{
+		const int c = colour_of_pos(L, p);
+		int x, y, z;
+		cg_decode(L, c, p - L.coff[c], x, y, z);
+		const int n = cg_node(L, x, y, z);
+		double r0, r1, r2;
+		row_product(L, K, u, p, x, y, z, r0, r1, r2);
+		r0 = f[3 * n] - r0;
+		r1 = f[3 * n + 1] - r1;
+		r2 = f[3 * n + 2] - r2;
+		r[3 * n] = r0;
+		r[3 * n + 1] = r1;
+		r[3 * n + 2] = r2;
+		v[0] += r0 * r0 + r1 * r1 + r2 * r2;
+	}
+	block_reduce_store<1>(v, red, out);
+}
+
+// ---------------------------------------------------------------- viscosity
+
+// visc_from_T, rheol 3 (Viscosity_structures.c:617-646) or visc_from_mat
+// (:477-489), with VMAX/VMIN (:414-427) and the material group of the element
+// centroid (construct_mat_group, Construct_arrays.c:742-800)
+__global__ void k_visc_from_T(Lvl L, const Geo *__restrict__ geo, Rheo r, const double *__restrict__ T, double *__restrict__ evi)
+{
+	const int e = blockIdx.x * blockDim.x + threadIdx.x;
+	if(e >= L.nel)
+		return;
+	const int ez = e % L.elz, ex = (e / L.elz) % L.elx, ey = e / (L.elz * L.elx);
+	const double zc = ((double)ez + 0.5) * L.h[2];
+	int layer = 0;
+	for(int i = 0; i < r.num_mat - 1; ++i)
+		if(zc >= r.z_layer[i])
+		{
+			layer = i + 1;
+			break;
+		}
+	if(!layer)
+		layer = r.num_mat;
+	const int m = layer - 1;
+	double TT[8];
+#pragma unroll
+	for(int a = 0; a < 8; ++a)
+	{
+		const double t = T[cg_node(L, ex + cg_loc(a, 0), ey + cg_loc(a, 1), ez + cg_loc(a, 2))];
+		TT[a] = t > 0.0 ? t : 0.0;
+	}
+#pragma unroll
+	for(int k = 0; k < 8; ++k)
+	{
+		double v;
+		if(r.tdepv)
+		{
+			double t = 1.0e-32;
+#pragma unroll
+			for(int a = 0; a < 8; ++a)
+				t += TT[a] * geo->N[k][a];
+			v = r.visc0[m] * exp(r.viscE[m] * (r.viscT[m] - t));
+		}
+		else
+			v = r.visc0[m];
+		if(r.vmax_on && v > r.vmax)
+			v = r.vmax;
+		if(r.vmin_on && v < r.vmin)
+			v = r.vmin;
+		evi[8 * e + k] = v;
+	}
+}
+
+// visc_from_gint_to_nodes (Nodal_mesh.c:583-615)
+__global__ void k_visc_to_nodes(Lvl L, const double *__restrict__ evi, double *__restrict__ VN)
+{
+	const int n = blockIdx.x * blockDim.x + threadIdx.x;
+	if(n >= L.nno)
+		return;
+	const int z = n % L.noz, x = (n / L.noz) % L.nox, y = n / (L.noz * L.nox);
+	double s = 0.0;
+	int cnt = 0;
+	for(int a = 0; a < 8; ++a)
+	{
+		const int ex = x - cg_loc(a, 0), ey = y - cg_loc(a, 1), ez = z - cg_loc(a, 2);
+		if(ex < 0 || ex >= L.elx || ey < 0 || ey >= L.ely || ez < 0 || ez >= L.elz)
+			continue;
+		const int e = ez + L.elz * (ex + L.elx * ey);
+		double t = 0.0;
+		for(int k = 0; k < 8; ++k)
+			t += evi[8 * e + k];
+		s += L.J * (t / 8.0);
+		++cnt;
+	}
+	VN[n] = s * (1.0 / ((double)cnt * L.J));
+}
+
+// project_scalar (Solver_multigrid.c:338-394)
+__global__ void k_project_scalar(Lvl Lf, Lvl Lc, const double *__restrict__ VN, double *__restrict__ VD)
+{
+	const int N = blockIdx.x * blockDim.x + threadIdx.x;
+	if(N >= Lc.nno)
+		return;
+	const int Z = N % Lc.noz, X = (N / Lc.noz) % Lc.nox, Y = N / (Lc.noz * Lc.nox);
+	double s = 0.0;
+	int cnt = 0;
+	for(int a = 0; a < 8; ++a)
+	{
+		const int ox = cg_loc(a, 0), oy = cg_loc(a, 1), oz = cg_loc(a, 2);
+		const int ex = X - ox, ey = Y - oy, ez = Z - oz;
+		if(ex < 0 || ex >= Lc.elx || ey < 0 || ey >= Lc.ely || ez < 0 || ez >= Lc.elz)
+			continue;
+		++cnt;
+		double t = 0.0;
+		for(int b = 0; b < 8; ++b)
+			t += VN[cg_node(Lf, 2 * ex + ox + cg_loc(b, 0), 2 * ey + oy + cg_loc(b, 1), 2 * ez + oz + cg_loc(b, 2))];
+		s += (t / 8.0) * Lc.J;
+	}
+	VD[N] = s * (1.0 / ((double)cnt * Lc.J));
+}
+
+// visc_from_nodes_to_gint (Nodal_mesh.c:617-640)
+__global__ void k_visc_to_gint(Lvl L, const Geo *__restrict__ geo, const double *__restrict__ VN, double *__restrict__ evi)
+{
+	const int e = blockIdx.x * blockDim.x + threadIdx.x;
+	if(e >= L.nel)
+		return;
+	const int ez = e % L.elz, ex = (e / L.elz) % L.elx, ey = e / (L.elz * L.elx);
+	double v[8];
+#pragma unroll
+	for(int a = 0; a < 8; ++a)
+		v[a] = VN[cg_node(L, ex + cg_loc(a, 0), ey + cg_loc(a, 1), ez + cg_loc(a, 2))];
+#pragma unroll
+	for(int k = 0; k < 8; ++k)
+	{
+		double t = 0.0;
+#pragma unroll
+		for(int a = 0; a < 8; ++a)
+			t += geo->N[k][a] * v[a];
+		evi[8 * e + k] = t;
+	}
+}
+
+// ---------------------------------------------------------------- forces
+
+// return_horiz_ave (Global_operations.c:133-251) of Ra*T, one block per z layer
+__global__ void k_horiz_ave(Lvl L, double Ra, const double *__restrict__ T, double *__restrict__ H)
+{
+	const int z = blockIdx.x;
+	__shared__ double sh[2][TPB / 32];
+	double s = 0.0, w = 0.0;
+	const double dg = L.h[0] * L.h[1] / 4.0;
+	for(int i = threadIdx.x; i < L.elx * L.ely; i += blockDim.x)
+	{
+		const int x = i % L.elx, y = i / L.elx;
+		s += dg * (Ra * T[cg_node(L, x, y, z)] + Ra * T[cg_node(L, x + 1, y, z)] + Ra * T[cg_node(L, x + 1, y + 1, z)] +
+		           Ra * T[cg_node(L, x, y + 1, z)]);
+		w += 4.0 * dg;
+	}
+	for(int o = 16; o > 0; o >>= 1)
+	{
+		s += __shfl_down_sync(0xffffffffu, s, o);
+		w += __shfl_down_sync(0xffffffffu, w, o);
+	}
+	if((threadIdx.x & 31) == 0)
+	{
+		sh[0][threadIdx.x >> 5] = s;
+		sh[1][threadIdx.x >> 5] = w;
+	}
+	__syncthreads();
+	if(threadIdx.x == 0)
+	{
+		double a = 0.0, b = 0.0;
+		for(int k = 0; k < (int)(blockDim.x >> 5); ++k)
+		{
+			a += sh[0][k];
+			b += sh[1][k];
+		}
+		H[z] = a / b;
+	}
+}
+
+// thermal_buoyancy (Pan_problem_misc_functions.c:83-156): Ra*T minus the layer mean
+__global__ void k_buoyancy(Lvl L, double Ra, const double *__restrict__ T, const double *__restrict__ H, double *__restrict__ b)
+{
+	const int n = blockIdx.x * blockDim.x + threadIdx.x;
+	if(n < L.nno)
+		b[n] = Ra * T[n] - H[n % L.noz];
+}
+
+// assemble_forces + get_elt_f (Element_calculations.c:74-125, 989-1075), node-centred, stripped
+__global__ void k_forces(Lvl L, const Geo *__restrict__ geo, const double *__restrict__ buoy, double *__restrict__ F)
+{
+	const int n = blockIdx.x * blockDim.x + threadIdx.x;
+	if(n >= L.nno)
+		return;
+	const int z = n % L.noz, x = (n / L.noz) % L.nox, y = n / (L.noz * L.nox);
+	double fz = 0.0;
+	for(int a = 0; a < 8; ++a)
+	{
+		const int ex = x - cg_loc(a, 0), ey = y - cg_loc(a, 1), ez = z - cg_loc(a, 2);
+		if(ex < 0 || ex >= L.elx || ey < 0 || ey >= L.ely || ez < 0 || ez >= L.elz)
+			continue;
+		double bb[8];
+		for(int b = 0; b < 8; ++b)
+			bb[b] = buoy[cg_node(L, ex + cg_loc(b, 0), ey + cg_loc(b, 1), ez + cg_loc(b, 2))];
+		double s = 0.0;
+		for(int k = 0; k < 8; ++k)
+		{
+			double fg = 0.0;
+			for(int b = 0; b < 8; ++b)
+				fg += bb[b] * geo->N[k][b];
+			s += fg * geo->N[k][a] * L.J;
+		}
+		fz += s;
+	}
+	const unsigned f = cg_vflag(L, x, y, z);
+	F[3 * n] = 0.0;
+	F[3 * n + 1] = 0.0;
+	F[3 * n + 2] = (f & 4u) ? 0.0 : fz;
+}
+
+// v_from_vector (Stokes_flow_Incomp.c:530-553): V[d*nno + n]; constrained dofs take VB = 0
+__global__ void k_v_from_vector(Lvl L, const double *__restrict__ U, double *__restrict__ V)
+{
+	const int n = blockIdx.x * blockDim.x + threadIdx.x;
+	if(n >= L.nno)
+		return;
+	const int z = n % L.noz, x = (n / L.noz) % L.nox, y = n / (L.noz * L.nox);
+	const unsigned f = cg_vflag(L, x, y, z);
+	for(int d = 0; d < 3; ++d)
+		V[(size_t)d * L.nno + n] = ((f >> d) & 1u) ? 0.0 : U[3 * n + d];
+}
+
+// ---------------------------------------------------------------- energy
+
+__device__ __forceinline__ bool t_dirichlet(const Lvl &L, int n) { int z = n % L.noz; return z == 0 || z == L.noz - 1; }
+
+// pg_solver's per-element work: pg_shape_fn (Advection_diffusion.c:448-555)
+// and element_residual (:564-727), Cartesian, diffusivity 1, Q = Q0
+__global__ void k_pg_residual(Lvl L, const Geo *__restrict__ geo, const double *__restrict__ T, const double *__restrict__ Tdot,
+                              const double *__restrict__ V, double Q0, double *__restrict__ Eres)
+{
+	const int e = blockIdx.x * blockDim.x + threadIdx.x;
+	if(e >= L.nel)
+		return;
+	const int ez = e % L.elz, ex = (e / L.elz) % L.elx, ey = e / (L.elz * L.elx);
+	const double diff = 1.0, twodiff = 2.0 * diff;
+	double vn[8][3], tn[8], dtn[8];
+#pragma unroll
+	for(int a = 0; a < 8; ++a)
+	{
+		const int n = cg_node(L, ex + cg_loc(a, 0), ey + cg_loc(a, 1), ez + cg_loc(a, 2));
+		vn[a][0] = V[n];
+		vn[a][1] = V[(size_t)L.nno + n];
+		vn[a][2] = V[2 * (size_t)L.nno + n];
+		tn[a] = T[n];
+		dtn[a] = t_dirichlet(L, n) ? 0.0 : Tdot[n];
+	}
+	double uc[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+	for(int a = 0; a < 8; ++a)
+#pragma unroll
+		for(int d = 0; d < 3; ++d)
+			uc[d] += 0.125 * vn[a][d];
+	double us[3], up[3];
+#pragma unroll
+	for(int d = 0; d < 3; ++d)
+	{
+		us[d] = fabs(uc[d] * L.h[d]);
+		up[d] = (us[d] > twodiff) ? (1.0 - twodiff / us[d]) : 0.0;
+	}
+	const double unorm = uc[0] * uc[0] + uc[1] * uc[1] + uc[2] * uc[2];
+	const double adiff = (unorm > 0.000001) ? ((us[0] * up[0] + us[1] * up[1] + us[2] * up[2]) / (2.0 * unorm)) : 0.0;
+	double er[8];
+#pragma unroll
+	for(int a = 0; a < 8; ++a)
+		er[a] = 0.0;
+#pragma unroll
+	for(int k = 0; k < 8; ++k)
+	{
+		double v0 = 0, v1 = 0, v2 = 0, t0 = 0, t1 = 0, t2 = 0, dT = 0;
+#pragma unroll
+		for(int a = 0; a < 8; ++a)
+		{
+			const double Nk = geo->N[k][a];
+			dT += dtn[a] * Nk;
+			v0 += vn[a][0] * Nk;
+			v1 += vn[a][1] * Nk;
+			v2 += vn[a][2] * Nk;
+			t0 += geo->gnx[k][a][0] * tn[a];
+			t1 += geo->gnx[k][a][1] * tn[a];
+			t2 += geo->gnx[k][a][2] * tn[a];
+		}
+		const double adv = dT - Q0 + v0 * t0 + v1 * t1 + v2 * t2;
+#pragma unroll
+		for(int a = 0; a < 8; ++a)
+		{
+			const double g0 = geo->gnx[k][a][0], g1 = geo->gnx[k][a][1], g2 = geo->gnx[k][a][2];
+			const double pg = geo->N[k][a] + adiff * (v0 * g0 + v1 * g1 + v2 * g2);
+			er[a] -= pg * L.J * adv + diff * L.J * (g0 * t0 + g1 * t1 + g2 * t2);
+		}
+	}
+#pragma unroll
+	for(int a = 0; a < 8; ++a)
+		Eres[8 * (size_t)e + a] = er[a];
+}
+
+// DTdot = (sum of element residuals at the node) / lumped mass
+__global__ void k_pg_gather(Lvl L, const double *__restrict__ Eres, double *__restrict__ DTdot)
+{
+	const int n = blockIdx.x * blockDim.x + threadIdx.x;
+	if(n >= L.nno)
+		return;
+	const int z = n % L.noz, x = (n / L.noz) % L.nox, y = n / (L.noz * L.nox);
+	double s = 0.0;
+	int cnt = 0;
+	for(int a = 0; a < 8; ++a)
+	{
+		const int ex = x - cg_loc(a, 0), ey = y - cg_loc(a, 1), ez = z - cg_loc(a, 2);
+		if(ex < 0 || ex >= L.elx || ey < 0 || ey >= L.ely || ez < 0 || ez >= L.elz)
+			continue;
+		s += Eres[8 * (size_t)(ez + L.elz * (ex + L.elx * ey)) + a];
+		++cnt;
+	}
+	DTdot[n] = s * (1.0 / ((double)cnt * L.J));
+}
+
+// predictor (Advection_diffusion.c:352-367)
+__global__ void k_predictor(Lvl L, double *T, double *Tdot, double dt, double gamma)
+{
+	const int n = blockIdx.x * blockDim.x + threadIdx.x;
+	if(n >= L.nno)
+		return;
+	if(!t_dirichlet(L, n))
+		T[n] += (1.0 - gamma) * dt * Tdot[n];
+	Tdot[n] = 0.0;
+}
+
+// corrector (Advection_diffusion.c:369-386)
+__global__ void k_corrector(Lvl L, double *T, double *Tdot, const double *DTdot, double dt, double gamma)
+{
+	const int n = blockIdx.x * blockDim.x + threadIdx.x;
+	if(n >= L.nno)
+		return;
+	if(!t_dirichlet(L, n))
+		T[n] += gamma * dt * DTdot[n];
+	Tdot[n] += DTdot[n];
+}
+
+// temperatures_conform_bcs (Boundary_conditions.c:949-991): T = 1 at the bottom, 0 at the top
+__global__ void k_conform_T(Lvl L, double *T)
+{
+	const int n = blockIdx.x * blockDim.x + threadIdx.x;
+	if(n >= L.nno)
+		return;
+	const int z = n % L.noz;
+	if(z == 0)
+		T[n] = 1.0;
+	else if(z == L.noz - 1)
+		T[n] = 0.0;
+}
+
+// max (Tmax, Global_operations.c:394-407) reported through the sum machinery as -min(-x)
+__global__ void k_max(int n, const double *__restrict__ T, Red red, double *out)
+{
+	__shared__ double sh[RED_THREADS / 32];
+	__shared__ bool last;
+	double m = -10.0;
+	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+		m = fmax(m, T[i]);
+	for(int o = 16; o > 0; o >>= 1)
+		m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+	if((threadIdx.x & 31) == 0)
+		sh[threadIdx.x >> 5] = m;
+	__syncthreads();
+	if(threadIdx.x == 0)
+	{
+		double t = -10.0;
+		for(int w = 0; w < (int)(blockDim.x >> 5); ++w)
+			t = fmax(t, sh[w]);
+		red.partials[blockIdx.x] = t;
+		__threadfence();
+		last = (atomicAdd(red.counter, 1u) == gridDim.x - 1);
+	}
+	__syncthreads();
+	if(last && threadIdx.x == 0)
+	{
+		__threadfence();
+		double t = -10.0;
+		for(int b = 0; b < (int)gridDim.x; ++b)
+			t = fmax(t, __ldcg(red.partials + b));
+		out[0] = t;
+		*red.counter = 0u;
+	}
+}
+
+// advective part of std_timestep (Advection_diffusion.c:737-810): min over elements of 0.5/uc
+__global__ void k_adv_step(Lvl L, const double *__restrict__ V, Red red, double *out)
+{
+	__shared__ double sh[RED_THREADS / 32];
+	__shared__ bool last;
+	double m = 1.0e8;
+	for(int e = blockIdx.x * blockDim.x + threadIdx.x; e < L.nel; e += gridDim.x * blockDim.x)
+	{
+		const int ez = e % L.elz, ex = (e / L.elz) % L.elx, ey = e / (L.elz * L.elx);
+		double uc[3] = {0.0, 0.0, 0.0};
+		for(int a = 0; a < 8; ++a)
+		{
+			const int n = cg_node(L, ex + cg_loc(a, 0), ey + cg_loc(a, 1), ez + cg_loc(a, 2));
+			for(int d = 0; d < 3; ++d)
+				uc[d] += 0.125 * V[(size_t)d * L.nno + n];
+		}
+		const double u = fabs(uc[0]) / L.h[0] + fabs(uc[1]) / L.h[1] + fabs(uc[2]) / L.h[2];
+		m = fmin(m, 0.5 / u);
+	}
+	for(int o = 16; o > 0; o >>= 1)
+		m = fmin(m, __shfl_down_sync(0xffffffffu, m, o));
+	if((threadIdx.x & 31) == 0)
+		sh[threadIdx.x >> 5] = m;
+	__syncthreads();
+	if(threadIdx.x == 0)
+	{
+		double t = 1.0e8;
+		for(int w = 0; w < (int)(blockDim.x >> 5); ++w)
+			t = fmin(t, sh[w]);
+		red.partials[blockIdx.x] = t;
+		__threadfence();
+		last = (atomicAdd(red.counter, 1u) == gridDim.x - 1);
+	}
+	__syncthreads();
+	if(last && threadIdx.x == 0)
+	{
+		__threadfence();
+		double t = 1.0e8;
+		for(int b = 0; b < (int)gridDim.x; ++b)
+			t = fmin(t, __ldcg(red.partials + b));
+		out[0] = t;
+		*red.counter = 0u;
+	}
+}
+
+// ---------------------------------------------------------------- observables
+
+// heat_flux (Process_buoyancy.c:63-203), step 1: element mean of u_z T - dT/dz
+__global__ void k_hf_elem(Lvl L, const Geo *__restrict__ geo, const double *__restrict__ T, const double *__restrict__ V,
+                          double *__restrict__ uTe)
+{
+	const int e = blockIdx.x * blockDim.x + threadIdx.x;
+	if(e >= L.nel)
+		return;
+	const int ez = e % L.elz, ex = (e / L.elz) % L.elx, ey = e / (L.elz * L.elx);
+	double vz[8], tt[8];
+	for(int a = 0; a < 8; ++a)
+	{
+		const int n = cg_node(L, ex + cg_loc(a, 0), ey + cg_loc(a, 1), ez + cg_loc(a, 2));
+		vz[a] = V[2 * (size_t)L.nno + n];
+		tt[a] = T[n];
+	}
+	double uT = 0.0;
+	for(int k = 0; k < 8; ++k)
+	{
+		double u = 0, t = 0, dz = 0;
+		for(int a = 0; a < 8; ++a)
+		{
+			u += vz[a] * geo->N[k][a];
+			t += tt[a] * geo->N[k][a];
+			dz += tt[a] * geo->gnx[k][a][2];
+		}
+		uT += (u * t - dz) * L.J;
+	}
+	uTe[e] = uT / (8.0 * L.J);
+}
+
+// step 2: nodal flux = TWW-weighted element means / lumped mass
+__global__ void k_hf_node(Lvl L, const double *__restrict__ uTe, double *__restrict__ hf)
+{
+	const int n = blockIdx.x * blockDim.x + threadIdx.x;
+	if(n >= L.nno)
+		return;
+	const int z = n % L.noz, x = (n / L.noz) % L.nox, y = n / (L.noz * L.nox);
+	double s = 0.0;
+	int cnt = 0;
+	for(int a = 0; a < 8; ++a)
+	{
+		const int ex = x - cg_loc(a, 0), ey = y - cg_loc(a, 1), ez = z - cg_loc(a, 2);
+		if(ex < 0 || ex >= L.elx || ey < 0 || ey >= L.ely || ez < 0 || ez >= L.elz)
+			continue;
+		s += L.J * uTe[ez + L.elz * (ex + L.elx * ey)];
+		++cnt;
+	}
+	hf[n] = s * (1.0 / ((double)cnt * L.J));
+}
+
+// step 3: surface extrapolation 2 hf[s] - hf[s-1] and the element-area means; out = (Nut, Nub)
+__global__ void k_hf_surface(Lvl L, const double *__restrict__ hf, Red red, double *out)
+{
+	double v[2] = {0.0, 0.0};
+	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < L.elx * L.ely; i += gridDim.x * blockDim.x)
+	{
+		const int x = i % L.elx, y = i / L.elx;
+		const int xs[4] = {x, x + 1, x + 1, x}, ys[4] = {y, y, y + 1, y + 1};
+		double tt = 0.0, tb = 0.0;
+		for(int j = 0; j < 4; ++j)
+		{
+			const int top = cg_node(L, xs[j], ys[j], L.noz - 1), bot = cg_node(L, xs[j], ys[j], 0);
+			tt += 2.0 * hf[top] - hf[top - 1];
+			tb += 2.0 * hf[bot] - hf[bot + 1];
+		}
+		v[0] += tt;
+		v[1] += tb;
+	}
+	block_reduce_store<2>(v, red, out);
+}
+
+__global__ void k_vrms(Lvl L, const Geo *__restrict__ geo, const double *__restrict__ V, Red red, double *out)
+{
+	double v[1] = {0.0};
+	for(int e = blockIdx.x * blockDim.x + threadIdx.x; e < L.nel; e += gridDim.x * blockDim.x)
+	{
+		const int ez = e % L.elz, ex = (e / L.elz) % L.elx, ey = e / (L.elz * L.elx);
+		double vn[8][3];
+		for(int a = 0; a < 8; ++a)
+		{
+			const int n = cg_node(L, ex + cg_loc(a, 0), ey + cg_loc(a, 1), ez + cg_loc(a, 2));
+			for(int d = 0; d < 3; ++d)
+				vn[a][d] = V[(size_t)d * L.nno + n];
+		}
+		for(int k = 0; k < 8; ++k)
+		{
+			double u0 = 0, u1 = 0, u2 = 0;
+			for(int a = 0; a < 8; ++a)
+			{
+				u0 += geo->N[k][a] * vn[a][0];
+				u1 += geo->N[k][a] * vn[a][1];
+				u2 += geo->N[k][a] * vn[a][2];
+			}
+			v[0] += L.J * (u0 * u0 + u1 * u1 + u2 * u2);
+		}
+	}
+	block_reduce_store<1>(v, red, out);
+}
+
+} // namespace
+
+// ====================================================================== host
+
+void geo_fill_host(const Lvl &L, Geo *g)
+{
+	const double beta = 0.57735026918962576451;
+	double gnx[8][8][3], gnxc[8][3];
+	for(int k = 0; k <= 8; ++k)
+		for(int a = 0; a < 8; ++a)
+			for(int d = 0; d < 3; ++d)
+			{
+				double v = 0.5 * (cg_loc(a, d) ? 1.0 : -1.0) * 2.0 / L.h[d];
+				for(int dd = 0; dd < 3; ++dd)
+					if(dd != d)
+					{
+						const double sa = cg_loc(a, dd) ? 1.0 : -1.0;
+						const double xi = (k == 8) ? 0.0 : (cg_loc(k, dd) ? beta : -beta);
+						v *= 0.5 * (1.0 + sa * xi);
+					}
+				if(k == 8)
+					gnxc[a][d] = v;
+				else
+					gnx[k][a][d] = v;
+			}
+	for(int k = 0; k < 8; ++k)
+		for(int a = 0; a < 8; ++a)
+		{
+			double v = 1.0;
+			for(int d = 0; d < 3; ++d)
+				v *= 0.5 * (1.0 + (cg_loc(a, d) ? 1.0 : -1.0) * (cg_loc(k, d) ? beta : -beta));
+			g->N[k][a] = v;
+			for(int d = 0; d < 3; ++d)
+				g->gnx[k][a][d] = gnx[k][a][d];
+		}
+	for(int k = 0; k < 8; ++k)
+		for(int a = 0; a < 8; ++a)
+			for(int b = 0; b < 8; ++b)
+			{
+				const double s = gnx[k][a][0] * gnx[k][b][0] + gnx[k][a][1] * gnx[k][b][1] + gnx[k][a][2] * gnx[k][b][2];
+				for(int i = 0; i < 3; ++i)
+					for(int j = 0; j < 3; ++j)
+						g->Mk[k][a][b][3 * i + j] = L.J * (gnx[k][a][j] * gnx[k][b][i] + (i == j ? s : 0.0));
+			}
+	for(int a = 0; a < 8; ++a)
+		for(int d = 0; d < 3; ++d)
+			g->g[3 * a + d] = -gnxc[a][d] * 8.0 * L.J;
+}
+
+void launch_assemble(cudaStream_t st, const Lvl &L, const Geo *geo, const double *evi, int aug, double lambda, double *K64,
+                     float *K32, double *BI64, float *BI32)
+{
+	k_assemble<<<nblocks(L.nno, 128), 128, 0, st>>>(L, geo, evi, aug, lambda, K64, K32, BI64, BI32);
+}
+
+void launch_bpi(cudaStream_t st, const Lvl &L, const Geo *geo, const double *BI64, double *BPI, int precond)
+{
+	k_bpi<<<nblocks(L.nel), TPB, 0, st>>>(L, geo, BI64, BPI, precond);
+}
+
+static int max_colour(const Lvl &L)
+{
+	int m = 0;
+	for(int c = 0; c < 8; ++c)
+		m = (L.coff[c + 1] - L.coff[c]) > m ? (L.coff[c + 1] - L.coff[c]) : m;
+	return m;
+}
+
+template <typename T> void launch_kmul(cudaStream_t st, const Lvl &L, const T *K, const T *u, T *Au)
+{
+	dim3 grid(nblocks(max_colour(L)), 8);
+	k_kmul<T, 0><<<grid, TPB, 0, st>>>(L, K, u, (const T *)nullptr, Au);
+}
+
+template <typename T> void launch_residual(cudaStream_t st, const Lvl &L, const T *K, const T *f, const T *u, T *r)
+{
+	dim3 grid(nblocks(max_colour(L)), 8);
+	k_kmul<T, 1><<<grid, TPB, 0, st>>>(L, K, u, f, r);
+}
+
+template <typename T>
+void launch_kmul_linesearch(cudaStream_t st, const Lvl &L, const T *K, const T *u, const T *res, T *Au, Red red, double *out2)
+{
+	k_kmul_ls<T><<<red_grid(L.nno), RED_THREADS, 0, st>>>(L, K, u, res, Au, red, out2);
+}
+
+template <typename T> void launch_gs_colour(cudaStream_t st, const Lvl &L, const T *K, const T *BI, const T *F, T *d, int c)
+{
+	const int n = L.coff[c + 1] - L.coff[c];
+	if(n > 0)
+		k_gs_colour<T><<<nblocks(n), TPB, 0, st>>>(L, K, BI, F, d, c);
+}
+
+bool gs_small_fits(const Lvl &L) { return L.nno <= 4 * GS_SMALL_THREADS; }
+
+template <typename T>
+void launch_gs_small(cudaStream_t st, const Lvl &L, const T *K, const T *BI, const T *F, T *d, int cycles, int zero_start)
+{
+	k_gs_small<T><<<1, GS_SMALL_THREADS, 0, st>>>(L, K, BI, F, d, cycles, zero_start);
+}
+
+template <typename T> void launch_project(cudaStream_t st, const Lvl &Lf, const Lvl &Lc, const T *AU, T *AD)
+{
+	k_project<T><<<nblocks(Lc.nno), TPB, 0, st>>>(Lf, Lc, AU, AD);
+}
+
+template <typename T> void launch_interp(cudaStream_t st, const Lvl &Lc, const Lvl &Lf, const T *AD, T *AU)
+{
+	k_interp<T><<<nblocks(Lf.nno), TPB, 0, st>>>(Lc, Lf, AD, AU);
+}
+
+template <typename T>
+void launch_vel_update(cudaStream_t st, int n, T *vel, const T *del, T *res, const T *AU, const double *nd, int update_res)
+{
+	k_vel_update<T><<<nblocks(n), TPB, 0, st>>>(n, vel, del, res, AU, nd, update_res);
+}
+
+#define INST(T)                                                                                                              \
+	template void launch_kmul<T>(cudaStream_t, const Lvl &, const T *, const T *, T *);                                      \
+	template void launch_residual<T>(cudaStream_t, const Lvl &, const T *, const T *, const T *, T *);                      \
+	template void launch_kmul_linesearch<T>(cudaStream_t, const Lvl &, const T *, const T *, const T *, T *, Red, double *); \
+	template void launch_gs_colour<T>(cudaStream_t, const Lvl &, const T *, const T *, const T *, T *, int);                 \
+	template void launch_gs_small<T>(cudaStream_t, const Lvl &, const T *, const T *, const T *, T *, int, int);             \
+	template void launch_project<T>(cudaStream_t, const Lvl &, const Lvl &, const T *, T *);                                 \
+	template void launch_interp<T>(cudaStream_t, const Lvl &, const Lvl &, const T *, T *);                                  \
+	template void launch_vel_update<T>(cudaStream_t, int, T *, const T *, T *, const T *, const double *, int);
+INST(double)
+INST(float)
+#undef INST
+
+void launch_div(cudaStream_t st, const Lvl &L, const Geo *geo, const double *U, double *divU)
+{
+	k_div<<<nblocks(L.nel), TPB, 0, st>>>(L, geo, U, divU);
+}
+
+void launch_grad(cudaStream_t st, const Lvl &L, const Geo *geo, const double *P, double *gradP)
+{
+	k_grad<<<nblocks(L.nno), TPB, 0, st>>>(L, geo, P, gradP);
+}
+
+void launch_strip(cudaStream_t st, const Lvl &L, double *r) { k_strip<<<nblocks(L.nno), TPB, 0, st>>>(L, r); }
+
+void launch_dot(cudaStream_t st, int n, const double *a, const double *b, Red red, double *out)
+{
+	k_dot<<<red_grid(n), RED_THREADS, 0, st>>>(n, a, b, red, out);
+}
+
+void launch_dots4(cudaStream_t st, int n, const double *a0, const double *b0, const double *a1, const double *b1, const double *a2,
+                  const double *b2, const double *a3, const double *b3, Red red, double *out)
+{
+	k_dots4<<<red_grid(n), RED_THREADS, 0, st>>>(n, a0, b0, a1, b1, a2, b2, a3, b3, red, out);
+}
+
+void launch_axpby(cudaStream_t st, int n, double *y, double a, const double *x, double b)
+{
+	k_axpby<<<nblocks(n), TPB, 0, st>>>(n, y, a, x, b);
+}
+
+void launch_mul(cudaStream_t st, int n, double *z, const double *a, const double *b) { k_mul<<<nblocks(n), TPB, 0, st>>>(n, z, a, b); }
+
+void launch_lin2(cudaStream_t st, int n, double *z, double a, const double *x, double b, const double *y)
+{
+	k_lin2<<<nblocks(n), TPB, 0, st>>>(n, z, a, x, b, y);
+}
+
+void launch_sub3(cudaStream_t st, int n, double *z, const double *f, const double *a, const double *b)
+{
+	k_sub3<<<nblocks(n), TPB, 0, st>>>(n, z, f, a, b);
+}
+
+void launch_copy_d2f(cudaStream_t st, int n, float *dst, const double *src) { k_d2f<<<nblocks(n), TPB, 0, st>>>(n, dst, src); }
+
+void launch_add_f2d(cudaStream_t st, int n, double *dst, const float *src) { k_add_f2d<<<nblocks(n), TPB, 0, st>>>(n, dst, src); }
+
+void launch_residual64(cudaStream_t st, const Lvl &L, const double *K, const double *f, const double *u, double *r, Red red, double *out)
+{
+	k_residual64<<<red_grid(L.nno), RED_THREADS, 0, st>>>(L, K, f, u, r, red, out);
+}
+
+void launch_visc_from_T(cudaStream_t st, const Lvl &L, const Geo *geo, const Rheo &r, const double *T, double *evi)
+{
+	k_visc_from_T<<<nblocks(L.nel), TPB, 0, st>>>(L, geo, r, T, evi);
+}
+
+void launch_project_viscosity(cudaStream_t st, const Lvl &Lf, const Lvl &Lc, const Geo *geoc, const double *evi_f, double *evi_c,
+                              double *work_f, double *work_c)
+{
+	k_visc_to_nodes<<<nblocks(Lf.nno), TPB, 0, st>>>(Lf, evi_f, work_f);
+	k_project_scalar<<<nblocks(Lc.nno), TPB, 0, st>>>(Lf, Lc, work_f, work_c);
+	k_visc_to_gint<<<nblocks(Lc.nel), TPB, 0, st>>>(Lc, geoc, work_c, evi_c);
+}
+
+void launch_buoyancy(cudaStream_t st, const Lvl &L, double Ra, const double *T, double *buoy)
+{
+	// the layer means go into the tail of `buoy`'s companion buffer: buoy + nno (caller sizes it nno + noz)
+	double *H = buoy + L.nno;
+	k_horiz_ave<<<L.noz, TPB, 0, st>>>(L, Ra, T, H);
+	k_buoyancy<<<nblocks(L.nno), TPB, 0, st>>>(L, Ra, T, H, buoy);
+}
+
+void launch_forces(cudaStream_t st, const Lvl &L, const Geo *geo, const double *buoy, double *F)
+{
+	k_forces<<<nblocks(L.nno), TPB, 0, st>>>(L, geo, buoy, F);
+}
+
+void launch_v_from_vector(cudaStream_t st, const Lvl &L, const double *U, double *V)
+{
+	k_v_from_vector<<<nblocks(L.nno), TPB, 0, st>>>(L, U, V);
+}
+
+void launch_pg_residual(cudaStream_t st, const Lvl &L, const Geo *geo, const double *T, const double *Tdot, const double *V, double Q0,
+                        double *Eres)
+{
+	k_pg_residual<<<nblocks(L.nel, 128), 128, 0, st>>>(L, geo, T, Tdot, V, Q0, Eres);
+}
+
+void launch_pg_gather(cudaStream_t st, const Lvl &L, const double *Eres, double *DTdot)
+{
+	k_pg_gather<<<nblocks(L.nno), TPB, 0, st>>>(L, Eres, DTdot);
+}
+
+void launch_predictor(cudaStream_t st, const Lvl &L, double *T, double *Tdot, double dt, double gamma)
+{
+	k_predictor<<<nblocks(L.nno), TPB, 0, st>>>(L, T, Tdot, dt, gamma);
+}
+
+void launch_corrector(cudaStream_t st, const Lvl &L, double *T, double *Tdot, const double *DTdot, double dt, double gamma)
+{
+	k_corrector<<<nblocks(L.nno), TPB, 0, st>>>(L, T, Tdot, DTdot, dt, gamma);
+}
+
+void launch_tmax(cudaStream_t st, int n, const double *T, Red red, double *out)
+{
+	k_max<<<red_grid(n), RED_THREADS, 0, st>>>(n, T, red, out);
+}
+
+void launch_adv_timestep(cudaStream_t st, const Lvl &L, const double *V, Red red, double *out)
+{
+	k_adv_step<<<red_grid(L.nel), RED_THREADS, 0, st>>>(L, V, red, out);
+}
+
+void launch_conform_T(cudaStream_t st, const Lvl &L, double *T) { k_conform_T<<<nblocks(L.nno), TPB, 0, st>>>(L, T); }
+
+void launch_heat_flux(cudaStream_t st, const Lvl &L, const Geo *geo, const double *T, const double *V, double *work, Red red, double *out)
+{
+	// work holds nel element means then nno nodal fluxes
+	k_hf_elem<<<nblocks(L.nel), TPB, 0, st>>>(L, geo, T, V, work);
+	k_hf_node<<<nblocks(L.nno), TPB, 0, st>>>(L, work, work + L.nel);
+	k_hf_surface<<<red_grid((long)L.elx * L.ely), RED_THREADS, 0, st>>>(L, work + L.nel, red, out);
+}
+
+void launch_vrms(cudaStream_t st, const Lvl &L, const Geo *geo, const double *V, Red red, double *out)
+{
+	k_vrms<<<red_grid(L.nel), RED_THREADS, 0, st>>>(L, geo, V, red, out);
+}

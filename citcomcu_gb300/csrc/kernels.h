@@ -1,0 +1,89 @@
+// Launchers for the sm_103a kernels of the Stokes / SUPG hot path.
+// Every launcher enqueues on `st` and returns immediately; none allocates.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "level.h"
+
+// Per-level constant geometry of a uniform box element (device resident).
+struct Geo
+{
+	double Mk[8][8][8][9];  // J * (dNa/dxj dNb/dxi + delta_ij grad Na . grad Nb) at Gauss point k: [k][a][b][3i+j]
+	double g[24];           // divergence operator of one element (get_elt_g, Cartesian)
+	double gnx[8][8][3];    // dN_a/dx_d at Gauss point k: [k][a][d]
+	double N[8][8];         // N_a at Gauss point k: [k][a]
+};
+
+// Deterministic reductions: fixed grid, per-block partials, last block sums
+// the partials in block order and writes `out[0..nv)`.
+struct Red
+{
+	double *partials;   // RED_MAX_BLOCKS * 8
+	unsigned *counter;  // one word, left at 0 after every reduction
+};
+#define RED_MAX_BLOCKS 304
+#define RED_THREADS 256
+
+void geo_fill_host(const Lvl &L, Geo *g);
+
+// set-up
+void launch_assemble(cudaStream_t st, const Lvl &L, const Geo *geo, const double *evi, int aug, double lambda,
+                     double *K64, float *K32, double *BI64, float *BI32);
+void launch_bpi(cudaStream_t st, const Lvl &L, const Geo *geo, const double *BI64, double *BPI, int precond);
+
+// level operators (T = double or float)
+template <typename T> void launch_kmul(cudaStream_t st, const Lvl &L, const T *K, const T *u, T *Au);
+template <typename T> void launch_residual(cudaStream_t st, const Lvl &L, const T *K, const T *f, const T *u, T *r);
+template <typename T>
+void launch_kmul_linesearch(cudaStream_t st, const Lvl &L, const T *K, const T *u, const T *res, T *Au, Red red, double *out2);
+template <typename T> void launch_gs_colour(cudaStream_t st, const Lvl &L, const T *K, const T *BI, const T *F, T *d, int colour);
+template <typename T>
+void launch_gs_small(cudaStream_t st, const Lvl &L, const T *K, const T *BI, const T *F, T *d, int cycles, int zero_start);
+template <typename T> void launch_project(cudaStream_t st, const Lvl &Lf, const Lvl &Lc, const T *AU, T *AD);
+template <typename T> void launch_interp(cudaStream_t st, const Lvl &Lc, const Lvl &Lf, const T *AD, T *AU);
+template <typename T> void launch_vel_update(cudaStream_t st, int n, T *vel, const T *del, T *res, const T *AU, const double *alpha_num_den, int update_res);
+bool gs_small_fits(const Lvl &L);
+
+// FP64 element operators
+void launch_div(cudaStream_t st, const Lvl &L, const Geo *geo, const double *U, double *divU);
+void launch_grad(cudaStream_t st, const Lvl &L, const Geo *geo, const double *P, double *gradP);
+void launch_strip(cudaStream_t st, const Lvl &L, double *r);
+
+// vectors and reductions
+void launch_dot(cudaStream_t st, int n, const double *a, const double *b, Red red, double *out);
+void launch_dots4(cudaStream_t st, int n, const double *a0, const double *b0, const double *a1, const double *b1,
+                  const double *a2, const double *b2, const double *a3, const double *b3, Red red, double *out);
+void launch_axpby(cudaStream_t st, int n, double *y, double a, const double *x, double b);  // y = a*y + b*x
+void launch_mul(cudaStream_t st, int n, double *z, const double *a, const double *b);       // z = a*b
+void launch_lin2(cudaStream_t st, int n, double *z, double a, const double *x, double b, const double *y);  // z = a*x + b*y
+void launch_sub3(cudaStream_t st, int n, double *z, const double *f, const double *a, const double *b);     // z = f - a - b
+void launch_copy_d2f(cudaStream_t st, int n, float *dst, const double *src);
+void launch_add_f2d(cudaStream_t st, int n, double *dst, const float *src);
+void launch_residual64(cudaStream_t st, const Lvl &L, const double *K, const double *f, const double *u, double *r, Red red, double *out_rr);
+
+// viscosity, forces, energy equation, observables (fine level, FP64)
+struct Rheo
+{
+	int tdepv, num_mat;
+	double visc0[8], viscE[8], viscT[8], z_layer[8];
+	int vmin_on, vmax_on;
+	double vmin, vmax;
+};
+void launch_visc_from_T(cudaStream_t st, const Lvl &L, const Geo *geo, const Rheo &r, const double *T, double *evi);
+void launch_project_viscosity(cudaStream_t st, const Lvl &Lf, const Lvl &Lc, const Geo *geoc, const double *evi_f,
+                              double *evi_c, double *work_f, double *work_c);
+void launch_buoyancy(cudaStream_t st, const Lvl &L, double Ra, const double *T, double *buoy);
+void launch_forces(cudaStream_t st, const Lvl &L, const Geo *geo, const double *buoy, double *F);
+void launch_v_from_vector(cudaStream_t st, const Lvl &L, const double *U, double *V);
+void launch_pg_residual(cudaStream_t st, const Lvl &L, const Geo *geo, const double *T, const double *Tdot, const double *V,
+                        double Q0, double *Eres);
+void launch_pg_gather(cudaStream_t st, const Lvl &L, const double *Eres, double *DTdot);
+void launch_predictor(cudaStream_t st, const Lvl &L, double *T, double *Tdot, double dt, double gamma);
+void launch_corrector(cudaStream_t st, const Lvl &L, double *T, double *Tdot, const double *DTdot, double dt, double gamma);
+void launch_tmax(cudaStream_t st, int n, const double *T, Red red, double *out);
+void launch_adv_timestep(cudaStream_t st, const Lvl &L, const double *V, Red red, double *out_min_step);
+void launch_conform_T(cudaStream_t st, const Lvl &L, double *T);
+void launch_heat_flux(cudaStream_t st, const Lvl &L, const Geo *geo, const double *T, const double *V, double *hf_work,
+                      Red red, double *out_nut_nub);
+void launch_vrms(cudaStream_t st, const Lvl &L, const Geo *geo, const double *V, Red red, double *out);

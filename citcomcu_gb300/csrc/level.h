@@ -1,0 +1,73 @@
+// Per-level mesh description shared by the host driver and the kernels.
+//
+// Node numbering follows CitcomCU (Construct_arrays.c:78-81, 0-based here):
+//   n = z + x*noz + y*noz*nox,   velocity equation 3n+d (x, y, z interleaved)
+//   element e = ez + ex*elz + ey*elz*elx (pressure lives on elements)
+// Operator coefficients (the assembled 27-block stencil, 1/diag) are stored
+// "colour-major": nodes are grouped by the parity of (z, x, y) into 8
+// colours, so that one Gauss-Seidel colour sweep streams a contiguous slice
+// of every coefficient array.
+#pragma once
+
+#define CITCOM_MAX_LEVELS 12
+
+struct Lvl
+{
+	int nox, noy, noz;
+	int nno, nel, neq;
+	int elx, ely, elz;
+	int npad;        // stride of the structure-of-arrays coefficient storage
+	int cnt[3][2];   // number of indices of parity p along axis (0 x, 1 y, 2 z)
+	int coff[9];     // colour offsets in colour-major order
+	double h[3];     // element edge lengths (uniform per axis)
+	double J;        // Jacobian determinant hx*hy*hz/8
+};
+
+#ifdef __CUDACC__
+#define CG_HD __host__ __device__ __forceinline__
+#else
+#define CG_HD inline
+#endif
+
+CG_HD int cg_colour(int x, int y, int z) { return (z & 1) | ((x & 1) << 1) | ((y & 1) << 2); }
+
+CG_HD int cg_node(const Lvl &L, int x, int y, int z) { return z + L.noz * (x + L.nox * y); }
+
+CG_HD int cg_pos(const Lvl &L, int x, int y, int z)
+{
+	const int c = cg_colour(x, y, z);
+	return L.coff[c] + (z >> 1) + L.cnt[2][z & 1] * ((x >> 1) + L.cnt[0][x & 1] * (y >> 1));
+}
+
+CG_HD void cg_decode(const Lvl &L, int c, int q, int &x, int &y, int &z)
+{
+	const int nz = L.cnt[2][c & 1], nx = L.cnt[0][(c >> 1) & 1];
+	z = 2 * (q % nz) + (c & 1);
+	const int t = q / nz;
+	x = 2 * (t % nx) + ((c >> 1) & 1);
+	y = 2 * (t / nx) + ((c >> 2) & 1);
+}
+
+// velocity constraint bits of a node: free slip on every wall (the reference's
+// free-slip top/bottom with reflecting sides) constrains exactly the dof
+// normal to each wall; bit 0 x, bit 1 y, bit 2 z
+CG_HD unsigned cg_vflag(const Lvl &L, int x, int y, int z)
+{
+	return (unsigned)(x == 0 || x == L.nox - 1) | ((unsigned)(y == 0 || y == L.noy - 1) << 1) |
+	       ((unsigned)(z == 0 || z == L.noz - 1) << 2);
+}
+
+// local node a (0..7) of an element -> (x, y, z) offset; the same sign
+// pattern orders the 2x2x2 Gauss points (element_definitions.h:139-222)
+CG_HD int cg_loc(int a, int d)
+{
+	// a: 0 (0,0,0) 1 (1,0,0) 2 (1,1,0) 3 (0,1,0) 4 (0,0,1) 5 (1,0,1) 6 (1,1,1) 7 (0,1,1)
+	return d == 0 ? (((a & 3) == 1) || ((a & 3) == 2)) : d == 1 ? ((a & 3) >= 2) : (a >= 4);
+}
+
+CG_HD int cg_local_index(int ox, int oy, int oz)
+{
+	// inverse of cg_loc
+	const int base = oy ? (ox ? 2 : 3) : (ox ? 1 : 0);
+	return base + 4 * oz;
+}

@@ -1,0 +1,172 @@
+/*
+ * citcom_gb300 — GB300 (sm_103a) implementation of CitcomCU's per-timestep
+ * hot path behind a plain C ABI.
+ *
+ * The entry points mirror the reference routines that the CitcomCU driver
+ * calls (Drive_solvers.c:45-165, Citcom.c:111-161); each one names the
+ * routine it replaces.  Arguments are plain pointers and sizes in the
+ * reference's own layouts, all 0-based:
+ *   node     n = z + x*noz + y*noz*nox   (Construct_arrays.c:78-81, minus 1)
+ *   velocity U[3n+d], d = 0 x, 1 y, 2 z (E->U, Construct_arrays.c:158-165)
+ *   pressure P[e], e = ez + ex*elz + ey*elz*elx (E->P + 1)
+ *   nodal    T[n], Tdot[n] (E->T + 1, E->Tdot + 1)
+ *   V        V[d*nno + n] (E->V[d+1] + 1 for d = 0, 1, 2)
+ *   EVI      evi[8e + k], Gauss point k (E->EVI[lev] + 1)
+ * Host pointers are copied to and from the device inside the call; the
+ * *_device variants take device pointers and do no host traffic.
+ *
+ * Every function returns CITCOM_GPU_OK (0) or a negative error code; the
+ * message is available from citcom_gpu_error_string().  There is no CPU
+ * fallback: without a usable CUDA device citcom_gpu_create fails.
+ *
+ * Scope: Cartesian box, uniform spacing per axis on every multigrid level,
+ * free-slip walls (the reference's default reflecting sides), T fixed at the
+ * top (0) and bottom (1), insulating sides, one device.
+ */
+#ifndef CITCOM_GB300_H
+#define CITCOM_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CITCOM_GPU_OK 0
+#define CITCOM_GPU_ERR_ARG -1
+#define CITCOM_GPU_ERR_CUDA -2
+#define CITCOM_GPU_ERR_STATE -3
+#define CITCOM_GPU_ERR_NOCONV -4
+
+#define CITCOM_GPU_FP64 0   /* plain: multigrid, smoothing and transfers in FP64 */
+#define CITCOM_GPU_MIXED 1  /* FP32 multigrid inside FP64 iterative refinement */
+
+typedef struct citcom_gpu citcom_gpu;
+
+/* Problem and solver controls; field names follow E->control / E->mesh /
+ * E->viscosity of the reference (Instructions.c:690-1060). */
+typedef struct citcom_gpu_config
+{
+	int levels;          /* mesh.levels: levmin = 0 .. levmax = levels-1 */
+	int mgunit[3];       /* mgunitx, mgunity, mgunitz */
+	double dimen[3];     /* dimenx, dimeny, dimenz */
+	double rayleigh;     /* control.Atemp */
+	double Q0;           /* rad_heat.total */
+	/* rheology: tdepv 0 -> eta = visc0[mat]; 1 -> rheol 3 */
+	int tdepv, num_mat;
+	double visc0[8], viscE[8], viscT[8], z_layer[8];
+	int vmin_on, vmax_on;
+	double vmin, vmax;
+	/* Stokes solver */
+	int aug_lagr;
+	double aug_number;
+	int precond;
+	int mg_cycle, down_heavy, up_heavy, vlowstep, vhighstep, piterations;
+	double accuracy;
+	/* energy equation */
+	int adv_sub_iterations;
+	double finetunedt, fixed_timestep;
+	/* CITCOM_GPU_FP64 or CITCOM_GPU_MIXED */
+	int precision;
+} citcom_gpu_config;
+
+/* Time-step bookkeeping that PG_timestep updates in E->advection / E->monitor. */
+typedef struct citcom_gpu_advection
+{
+	double timestep;            /* advection.timestep (out) */
+	double elapsed_time;        /* monitor.elapsed_time (in/out) */
+	double T_interior;          /* monitor.T_interior (out) */
+	int last_sub_iterations;    /* advection.last_sub_iterations (out) */
+} citcom_gpu_advection;
+
+/* Counters of the last Stokes solve. */
+typedef struct citcom_gpu_stats
+{
+	int uzawa_iterations;       /* *steps_max of solve_Ahat_p_fhat */
+	int del2_calls;             /* solve_del2_u calls */
+	int mg_passes;              /* multi_grid calls */
+	double initial_residual;    /* return value of solve_Ahat_p_fhat */
+	double stokes_ms;           /* device time of the last solve (CUDA events) */
+} citcom_gpu_stats;
+
+/* Allocates every device buffer the solver will use (on the current
+ * device) and precomputes the mesh geometry.  Replaces the reference's
+ * set-up of the solver arrays (Instructions.c:166-398, construct_* in
+ * Construct_arrays.c). */
+int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out);
+void citcom_gpu_destroy(citcom_gpu *h);
+const char *citcom_gpu_error_string(const citcom_gpu *h);
+/* dims = {nox, noy, noz, nno, nel, neq} of level lev */
+int citcom_gpu_level_dims(const citcom_gpu *h, int lev, int dims[6]);
+
+/* get_system_viscosity (Viscosity_structures.c:369) from nodal T, followed by
+ * project_viscosity (Solver_multigrid.c:398) to every coarser level. */
+int citcom_gpu_get_system_viscosity(citcom_gpu *h, const double *T);
+/* Use the caller's viscosity at the Gauss points of level lev (E->EVI[lev]+1). */
+int citcom_gpu_set_viscosity(citcom_gpu *h, int lev, const double *evi);
+int citcom_gpu_get_viscosity(citcom_gpu *h, int lev, double *evi);
+/* construct_stiffness_B_matrix (Construct_arrays.c:834): assembles the node
+ * stencils, 1/diag(K) on every level and the pressure preconditioner BPI. */
+int citcom_gpu_construct_stiffness_B_matrix(citcom_gpu *h);
+/* thermal_buoyancy (Pan_problem_misc_functions.c:83) + assemble_forces
+ * (Element_calculations.c:74): F (neq) from T (nno); buoyancy optional (nno). */
+int citcom_gpu_assemble_forces(citcom_gpu *h, const double *T, double *F, double *buoyancy);
+
+/* solve_Ahat_p_fhat (Stokes_flow_Incomp.c:295): Uzawa / Schur-complement
+ * PCG with the multigrid velocity solve.  V (neq) and P (npno) are updated
+ * in place; *steps_max is the iteration cap on entry and the iteration
+ * count on return; *initial_residual receives the reference's return value. */
+int citcom_gpu_solve_Ahat_p_fhat(citcom_gpu *h, double *V, double *P, const double *F, double imp, int *steps_max,
+                                 double *initial_residual);
+int citcom_gpu_solve_Ahat_p_fhat_device(citcom_gpu *h, double *dV, double *dP, const double *dF, double imp, int *steps_max,
+                                        double *initial_residual);
+/* solve_constrained_flow_iterative (Stokes_flow_Incomp.c:50) with
+ * v_from_vector: U, P updated in place with control.accuracy and
+ * control.p_iterations; nodal V (3*nno) written. */
+int citcom_gpu_solve_constrained_flow_iterative(citcom_gpu *h, double *U, double *P, const double *F, double *V);
+
+/* general_stokes_solver (Drive_solvers.c:45) for a Newtonian rheology:
+ * forces from T, viscosity from T when tdepv, stiffness, Uzawa, V.
+ * U, P are in/out (warm start), V (3*nno) out. */
+int citcom_gpu_general_stokes_solver(citcom_gpu *h, const double *T, double *U, double *P, double *V);
+
+/* PG_timestep (Advection_diffusion.c:251): T, Tdot (nno) in/out, V (3*nno) in. */
+int citcom_gpu_PG_timestep(citcom_gpu *h, double *T, double *Tdot, const double *V, citcom_gpu_advection *adv);
+
+/* heat_flux (Process_buoyancy.c:63): surface Nusselt numbers; and the
+ * volume-rms velocity sqrt(int |u|^2 dV / V). */
+int citcom_gpu_heat_flux(citcom_gpu *h, const double *T, const double *V, double *nut, double *nub);
+int citcom_gpu_vrms(citcom_gpu *h, const double *V, double *vrms);
+
+/* Whole time step on device-resident state (T, Tdot, U, P, V held by the
+ * handle): PG_timestep then general_stokes_solver, the order of the
+ * reference's time loop (Citcom.c:111-161).  Load/store move the state. */
+int citcom_gpu_load_state(citcom_gpu *h, const double *T, const double *Tdot, const double *U, const double *P);
+int citcom_gpu_store_state(citcom_gpu *h, double *T, double *Tdot, double *U, double *P, double *V);
+int citcom_gpu_stokes_resident(citcom_gpu *h);
+int citcom_gpu_step_resident(citcom_gpu *h, citcom_gpu_advection *adv);
+int citcom_gpu_last_stats(const citcom_gpu *h, citcom_gpu_stats *s);
+
+/* Single operators of level lev, host buffers (the kernels the solver uses;
+ * exposed for parity checks against the reference's routines). */
+/* n_assemble_del2_u (Element_calculations.c:552), stripped */
+int citcom_gpu_op_kmul(citcom_gpu *h, int lev, const double *u, double *Au);
+/* gauss_seidel (General_matrix_functions.c:1160), 8-colour order; d0 in/out
+ * when guess != 0; Ad = K d0 on return */
+int citcom_gpu_op_gauss_seidel(citcom_gpu *h, int lev, double *d0, const double *F, double *Ad, int cycles, int guess);
+/* project_vector (Solver_multigrid.c:72) fine_lev -> fine_lev-1, stripped */
+int citcom_gpu_op_project(citcom_gpu *h, int fine_lev, const double *AU, double *AD);
+/* interp_vector (Solver_multigrid.c:173) coarse_lev -> coarse_lev+1, stripped */
+int citcom_gpu_op_interp(citcom_gpu *h, int coarse_lev, const double *AD, double *AU);
+/* assemble_div_u / assemble_grad_p (Element_calculations.c:691, 727) */
+int citcom_gpu_op_div(citcom_gpu *h, int lev, const double *U, double *divU);
+int citcom_gpu_op_grad(citcom_gpu *h, int lev, const double *P, double *gradP);
+/* multi_grid (General_matrix_functions.c:525): d1 out, F in/out (residual) */
+int citcom_gpu_op_multi_grid(citcom_gpu *h, double *d1, double *F, double *residual);
+/* solve_del2_u (General_matrix_functions.c:368) on the finest level */
+int citcom_gpu_op_solve_del2_u(citcom_gpu *h, double *d0, const double *F, double acc, int *valid);
+/* BI (neq, 1/diag K) and BPI (nel) of level lev as the solver holds them */
+int citcom_gpu_op_diagonals(citcom_gpu *h, int lev, double *BI, double *BPI);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

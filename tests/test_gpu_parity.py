@@ -1,0 +1,218 @@
+"""GPU kernels and solvers (through the C ABI) against the CPU oracle.
+
+The oracle is pinned to the unchanged reference by tests/test_oracle_golden.py.
+Two oracle orderings are used:
+  * 8-colour Gauss-Seidel: the same arithmetic as the GPU, so operators agree
+    to FP64 rounding and whole solves take the same iteration counts;
+  * lexicographic Gauss-Seidel: the reference's own order; whole solves then
+    agree to the solver tolerance, so those comparisons run at tight accuracy.
+Tolerances are written in each test (relative max-norm unless stated).
+"""
+import math
+import os
+
+import numpy as np
+import pytest
+
+from oracle.decks import Case, conductive_T0
+from tests.golden.make_golden import cfg1_case, small_case
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def rel(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def tv(n, a, b):
+    i = np.arange(n, dtype=np.float64)
+    return np.sin(a * i + b) + 0.25 * np.cos(0.013 * i * i)
+
+
+@pytest.fixture(scope="module")
+def cg():
+    import citcomcu_gb300 as cg
+    cg.build()
+    return cg
+
+
+@pytest.fixture(scope="module")
+def olib(oracle_lib):
+    return oracle_lib
+
+
+def pair(cg, olib, case, precision=0, colored=True):
+    s = cg.Solver(cg.Config.like(case, precision=precision))
+    o = olib.Oracle(case, gs_colored=colored)
+    return s, o
+
+
+@pytest.fixture(scope="module")
+def small_ops(cg, olib):
+    case = small_case()
+    T0 = conductive_T0(case, amp=0.01, seed=0)
+    s, o = pair(cg, olib, case)
+    s.get_system_viscosity(T0)
+    s.construct_stiffness_B_matrix()
+    o.set_T(T0)
+    o.setup_operators()
+    return s, o, T0
+
+
+def test_viscosity_all_levels(small_ops):
+    s, o, _ = small_ops
+    for lev in range(3):
+        assert rel(s.get_viscosity(lev), o.EVI(lev)) < 1e-13
+
+
+def test_forces_and_buoyancy(small_ops):
+    s, o, T0 = small_ops
+    F, b = s.assemble_forces(T0)
+    assert rel(b, o.buoyancy()) < 1e-12
+    assert rel(F, o.F()[: o.fine["neq"]]) < 1e-12
+
+
+@pytest.mark.parametrize("lev", [0, 1, 2])
+def test_diagonals(small_ops, lev):
+    s, o, _ = small_ops
+    bi, bpi = s.op_diagonals(lev)
+    assert rel(bi, o.BI(lev)) < 1e-13
+    if bpi is not None:
+        assert rel(bpi, o.BPI(lev)) < 1e-13
+
+
+@pytest.mark.parametrize("lev", [0, 1, 2])
+def test_kmul_div_grad(small_ops, lev):
+    s, o, _ = small_ops
+    u = tv(o.dims[lev]["neq"], 0.37, 0.11)
+    assert rel(s.op_kmul(lev, u), o.kmul(lev, u)) < 1e-13
+    assert rel(s.op_div(lev, u), o.div(lev, u)) < 1e-13
+    p = tv(o.dims[lev]["nel"], 0.21, 0.5)
+    assert rel(s.op_grad(lev, p), o.grad(lev, p)) < 1e-13
+
+
+@pytest.mark.parametrize("lev", [0, 1, 2])
+def test_gauss_seidel_colour_sweeps(small_ops, lev):
+    s, o, _ = small_ops
+    F = o.strip(lev, tv(o.dims[lev]["neq"], 0.19, 0.7))
+    d, ad = s.op_gauss_seidel(lev, F, 2)
+    dr, adr = o.gauss_seidel(lev, F, 2)
+    assert rel(d, dr) < 1e-12 and rel(ad, adr) < 1e-12
+    d2, _ = s.op_gauss_seidel(lev, F, 1, d0=d)
+    d2r, _ = o.gauss_seidel(lev, F, 1, d0=dr)
+    assert rel(d2, d2r) < 1e-12
+
+
+@pytest.mark.parametrize("lev", [1, 2])
+def test_transfers(small_ops, lev):
+    s, o, _ = small_ops
+    u = tv(o.dims[lev]["neq"], 0.29, 0.3)
+    assert rel(s.op_project(lev, u), o.strip(lev - 1, o.project(lev, u))) < 1e-13
+    c = tv(o.dims[lev - 1]["neq"], 0.43, 0.9)
+    assert rel(s.op_interp(lev - 1, c), o.strip(lev, o.interp(lev - 1, c))) < 1e-14
+
+
+def test_multigrid_pass_and_solve(small_ops):
+    s, o, _ = small_ops
+    F = o.F()[: o.fine["neq"]].copy()
+    d1, res, r = s.op_multi_grid(F)
+    d1r, resr, rr = o.multi_grid(F)
+    assert rel(d1, d1r) < 1e-11 and rel(res, resr) < 1e-10
+    assert abs(r - rr) <= 1e-10 * rr
+    acc = 1e-6 * math.sqrt(np.dot(F, F) / F.size)
+    d0, valid = s.op_solve_del2_u(F, acc)
+    d0r, validr, _ = o.solve_del2_u(F, acc)
+    assert valid == validr and rel(d0, d0r) < 1e-10
+
+
+def run_steps(s, o, T0, nsteps):
+    """general_stokes_solver + PG_timestep on both; returns per-step records."""
+    f = s.fine
+    U, P, Tdot = np.zeros(f["neq"]), np.zeros(f["nel"]), np.zeros(f["nno"])
+    T = T0.copy()
+    o.set_T(T0)
+    o.thermal_buoyancy()
+    out = []
+    for step in range(nsteps + 1):
+        if step:
+            s.PG_timestep(T, Tdot, V)
+            o.pg_timestep()
+        V = s.general_stokes_solver(T, U, P)
+        st = s.stats()
+        info = o.stokes()
+        nut, nub = s.heat_flux(T, V)
+        onut, onub = o.heat_flux()
+        out.append(dict(step=step, st=st, info=info, U=rel(U, o.U()[: f["neq"]]), P=rel(P, o.P()),
+                        T=float(np.max(np.abs(T - o.T()))),
+                        V=max(rel(V[d * f["nno"]:(d + 1) * f["nno"]], o.V(d)) for d in range(3)),
+                        nut=(nut, onut), nub=(nub, onub), vrms=(s.vrms(V), o.vrms())))
+    return out
+
+
+def test_time_steps_match_coloured_oracle(cg, olib):
+    """Same arithmetic as the GPU: identical iteration counts, FP64-rounding-level drift."""
+    case = small_case()
+    T0 = conductive_T0(case, amp=0.01, seed=0)
+    s, o = pair(cg, olib, case)
+    for r in run_steps(s, o, T0, 3):
+        assert r["st"]["uzawa"] == r["info"]["uzawa"], r
+        assert r["st"]["mg_passes"] == r["info"]["mg_calls"], r
+        assert r["U"] < 1e-9 and r["V"] < 1e-9 and r["P"] < 1e-8 and r["T"] < 1e-11, r
+        assert abs(r["nut"][0] - r["nut"][1]) < 1e-11 and abs(r["vrms"][0] - r["vrms"][1]) < 1e-9 * r["vrms"][1]
+
+
+def test_time_steps_match_reference_order_at_tight_tolerance(cg, olib):
+    """Against the reference's lexicographic smoother (the oracle pinned to the
+    reference): with both solvers converged to accuracy 1e-11 the per-step
+    velocity, temperature, Nu and Vrms agree to 1e-8 relative."""
+    case = small_case()
+    case.accuracy = 1e-11
+    T0 = conductive_T0(case, amp=0.01, seed=0)
+    s, o = pair(cg, olib, case, colored=False)
+    for r in run_steps(s, o, T0, 3):
+        print(r)
+        assert r["V"] < 1e-8 and r["U"] < 1e-8 and r["T"] < 1e-8, r
+        assert abs(r["nut"][0] - r["nut"][1]) < 1e-8 * abs(r["nut"][1]), r
+        assert abs(r["vrms"][0] - r["vrms"][1]) < 1e-8 * r["vrms"][1], r
+
+
+def test_cfg1_against_reference_fixture(cg):
+    """16^3 isoviscous Ra 1e4 at the reference's accuracy 1e-6: per-step Nu and
+    Vrms of the FP64 GPU path against the reference's own run (fixture)."""
+    G = dict(np.load(os.path.join(GOLD, "cfg1_16.npz")))
+    case = cfg1_case()
+    s = cg.Solver(cg.Config.like(case))
+    f = s.fine
+    U, P, Tdot = np.zeros(f["neq"]), np.zeros(f["nel"]), np.zeros(f["nno"])
+    T = G["T0"].copy()
+    for step in range(6):
+        if step:
+            s.PG_timestep(T, Tdot, V)
+        V = s.general_stokes_solver(T, U, P)
+        nut, _ = s.heat_flux(T, V)
+        sc = G[f"s{step}_scalars"]
+        print(step, nut, sc[0], s.vrms(V), sc[2], s.stats()["uzawa"], sc[6] - 1)
+        assert abs(nut - sc[0]) < 2e-6 * abs(sc[0])
+        assert abs(s.vrms(V) - sc[2]) < 2e-5 * sc[2]
+    assert float(np.max(np.abs(T - G["s5_T"]))) < 1e-5
+
+
+def test_mixed_precision_matches_fp64(cg):
+    """FP32 multigrid inside FP64 refinement against the FP64 path: same
+    problem, accuracy 1e-8; errors stated relative to the FP64 solution."""
+    case = small_case()
+    T0 = conductive_T0(case, amp=0.01, seed=0)
+    res = {}
+    for prec in (0, 1):
+        s = cg.Solver(cg.Config.like(case, precision=prec))
+        f = s.fine
+        U, P = np.zeros(f["neq"]), np.zeros(f["nel"])
+        V = s.general_stokes_solver(T0, U, P)
+        res[prec] = dict(U=U, P=P, V=V, nu=s.heat_flux(T0, V)[0], vrms=s.vrms(V), st=s.stats())
+    print(res[0]["st"], res[1]["st"])
+    assert rel(res[1]["U"], res[0]["U"]) < 1e-6
+    assert abs(res[1]["nu"] - res[0]["nu"]) < 1e-7
+    assert abs(res[1]["vrms"] - res[0]["vrms"]) < 1e-7 * res[0]["vrms"]
