@@ -1,0 +1,353 @@
+"""Benchmark: Stokes ms per time step to a 1e-6 tolerance on one GB300.
+
+Workload (default): 64^3 Q1 elements, 5 multigrid levels (4^3 .. 64^3), unit
+box, eta = exp(-ln(1e3) T) (a 10^3 contrast), Ra = 1e5, free-slip walls, seeded
+initial T = 1 - z + U(-0.01, 0.01) (numpy PCG64 seed 0), Uzawa accuracy 1e-6
+with the reference's own stopping rule (dv/v and dp/p below accuracy, at most
+piterations = 375), multigrid knobs of the reference's example deck.
+
+A step is one time step of the reference's loop: PG_timestep then
+general_stokes_solver, on state resident in HBM.  `value` is the mean device
+time of the Stokes part per step in the headline configuration (FP32
+multigrid inside FP64 refinement); the FP64 plain path is timed on the same
+steps and reported beside it.  `e2e` times the same Stokes solve through the
+C ABI with host buffers (pinned), copies included.
+
+  python bench.py [--steps K] [--warmup W] [--gpus N] [--impl reference]
+                  [--size 64|32] [--no-cpu]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Stokes ms/step to 1e-6 residual: FP64 plain vs FP32 MG + learned warm start"
+UNIT = "ms/step"
+# multigrid passes of one full Stokes solve of the default workload under the
+# reference's stopping rule, counted by running the oracle's complete solve
+# (lexicographic smoother, the reference's order): 376 solve_del2_u calls and
+# 440 multigrid passes (the Uzawa loop stops at its 375-iteration cap).  The
+# CPU baseline times a bounded sample of passes and scales by this count.
+REF_FULL_SOLVE_PASSES = {64: 440, 32: 462}
+
+
+def workload(size: int):
+    from citcomcu_gb300 import Config
+    levels = {64: 5, 32: 4, 128: 6}[size]
+    return Config(mgunit=(4, 4, 4), levels=levels, rayleigh=1e5, tdepv=True, visc0=(1.0,),
+                  viscE=(math.log(1e3),), viscT=(0.0,), accuracy=1e-6, piterations=375)
+
+
+def seeded_T0(case):
+    rng = np.random.Generator(np.random.PCG64(0))
+    z = np.linspace(0.0, case.dimen[2], case.noz)
+    T = np.empty((case.noy, case.nox, case.noz))
+    T[:] = 1.0 - z / case.dimen[2]
+    T += rng.uniform(-0.01, 0.01, size=T.shape)
+    T[:, :, 0] = 1.0
+    T[:, :, -1] = 0.0
+    return T.reshape(-1)
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# --------------------------------------------------------------- GPU arm
+def run_mode(cg, case, precision, T0, steps, warmup):
+    s = cg.Solver(cg.Config.like(case, precision=precision))
+    f = s.fine
+    s.load_state(T=T0, Tdot=np.zeros(f["nno"]), U=np.zeros(f["neq"]), P=np.zeros(f["nel"]))
+    s.stokes_resident()  # the solve before the time loop (Citcom.c:97)
+    elapsed = 0.0
+    for _ in range(warmup):
+        elapsed = s.step_resident(elapsed)["elapsed_time"]
+    recs = []
+    l0 = s.stats()["kernel_launches"]
+    for _ in range(steps):
+        elapsed = s.step_resident(elapsed)["elapsed_time"]
+        recs.append(s.stats())
+    launches = s.stats()["kernel_launches"] - l0
+    res = s.stokes_residuals()
+    nu = s.heat_flux()
+    vr = s.vrms()
+    s.close()
+    return recs, launches, res, nu, vr
+
+
+def bytes_per_sweep(nno: int, word: int) -> int:
+    """Algorithmic bytes of one Gauss-Seidel sweep (8 colour launches) on a
+    level with stored 27-block stencils: the 243 coefficients and 3 inverse
+    diagonals of every node, the right-hand side, one write of d, and the
+    whole d vector read once per colour launch (its 27-neighbourhoods)."""
+    return nno * word * (243 + 3 + 3 + 3 + 8 * 3)
+
+
+def e2e_mode(cg, case, T0, steps, warmup):
+    """Stokes solve through the C ABI with host buffers: each call copies
+    T, U, P host->device and U, P, V device->host."""
+    import torch
+    s = cg.Solver(cg.Config.like(case, precision=cg.MIXED))
+    f = s.fine
+
+    def pinned(n):
+        return torch.zeros(n, dtype=torch.float64, pin_memory=True).numpy()
+
+    T, Tdot = pinned(f["nno"]), pinned(f["nno"])
+    U, P = pinned(f["neq"]), pinned(f["nel"])
+    T[:] = T0
+    V = s.general_stokes_solver(T, U, P)
+    Vp = pinned(3 * f["nno"])
+    Vp[:] = V
+    ms = []
+    for i in range(warmup + steps):
+        s.PG_timestep(T, Tdot, Vp)
+        t0 = time.perf_counter()
+        V = s.general_stokes_solver(T, U, P)
+        t1 = time.perf_counter()
+        Vp[:] = V
+        if i >= warmup:
+            ms.append(1e3 * (t1 - t0))
+    s.close()
+    h2d = 8 * (f["nno"] + f["neq"] + f["nel"])
+    d2h = 8 * (f["neq"] + f["nel"] + 3 * f["nno"])
+    return float(np.mean(ms)), h2d, d2h
+
+
+# --------------------------------------------------------------- CPU side
+def cpu_sample(case, T0, uzawa_sample: int = 3, full_passes=None):
+    """The oracle port (FP64, lexicographic smoother = the reference's
+    algorithm) on the same workload: the set-up of one Stokes solve (forces,
+    viscosity on all levels, stiffness assembly) timed in full, plus the first
+    Uzawa iterations of the solve timed per multigrid pass and scaled to the
+    full solve's pass count."""
+    from oracle import oracle as O
+    from oracle.decks import Case
+    O.build()
+    c = Case(**{k: getattr(case, k) for k in ("mgunit", "levels", "dimen", "rayleigh", "Q0", "tdepv", "visc0",
+                                               "viscE", "viscT", "z_layer", "vmin", "vmax", "aug_lagr",
+                                               "aug_number", "precond", "mg_cycle", "down_heavy", "up_heavy",
+                                               "vlowstep", "vhighstep", "accuracy")})
+    o = O.Oracle(c, gs_colored=False)
+    o.set_T(T0)
+    t0 = time.perf_counter()
+    o.setup_operators()
+    t1 = time.perf_counter()
+    info = o.solve_Ahat_p_fhat(c.accuracy, uzawa_sample)
+    t2 = time.perf_counter()
+    per_pass = (t2 - t1) / max(info["mg_calls"], 1)
+    full = full_passes if full_passes else REF_FULL_SOLVE_PASSES.get(case.nox - 1, info["mg_calls"])
+    value = 1e3 * ((t1 - t0) + per_pass * full)
+    return {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"oracle (C, FP64, lexicographic Gauss-Seidel) on this workload: set-up {t1 - t0:.2f} s timed in "
+                      f"full, then the first {info['del2_calls']} solve_del2_u calls ({info['mg_calls']} multigrid "
+                      f"passes, {t2 - t1:.1f} s) of the first Uzawa solve; {1e3 * per_pass:.1f} ms per pass x "
+                      f"{full} passes of the full solve"}
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    case = workload(args.size)
+    T0 = seeded_T0(case)
+    vals = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_sample(case, T0, uzawa_sample=2)
+        if i >= args.warmup:
+            vals.append(r["value"])
+    v = float(np.mean(vals))
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": v, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": workload_name(case)},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "sample": r["sample"]},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def workload_name(case):
+    return (f"{case.nox - 1}^3 Q1 elements, {case.levels} multigrid levels, eta=exp(-ln(1e3) T), Ra=1e5, free slip, "
+            f"T0=1-z+U(-0.01,0.01) seed 0, accuracy 1e-6, piterations 375")
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=64, choices=[32, 64, 128])
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--modes", default="both", choices=["both", "mixed"],
+                    help="'mixed' skips the FP64 plain comparison (profiling runs)")
+    ap.add_argument("--piterations", type=int, default=375,
+                    help="Uzawa iteration cap; lower values only for short profiling runs")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return reference_arm(args)
+
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    import citcomcu_gb300 as cg
+    cg.build()
+    case = workload(args.size)
+    case.piterations = args.piterations
+    T0 = seeded_T0(case)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    barrier()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        mixed, launches, res_mixed, nu_mixed, vr_mixed = run_mode(cg, case, cg.MIXED, T0, args.steps, args.warmup)
+        t1 = time.perf_counter()
+    barrier()
+    if args.modes == "both":
+        fp64, _, res_fp64, nu_fp64, vr_fp64 = run_mode(cg, case, cg.FP64, T0, args.steps, args.warmup)
+    else:
+        fp64, res_fp64, nu_fp64, vr_fp64 = mixed, res_mixed, nu_mixed, vr_mixed
+    barrier()
+
+    stokes_ms = float(np.mean([r["stokes_ms"] for r in mixed]))
+    step_ms = float(np.mean([r["stokes_ms"] + r["energy_ms"] for r in mixed]))
+    stokes_ms_fp64 = float(np.mean([r["stokes_ms"] for r in fp64]))
+    if world > 1:
+        t = torch.tensor([stokes_ms, step_ms], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        stokes_ms, step_ms = float(t[0]), float(t[1])
+    # whole job: N replicas each ran `steps` steps in the same wall time
+    value = stokes_ms / world
+
+    # dominant kernel: finest-level FP32 Gauss-Seidel colour launches, timed live
+    nno = case.nno
+    sweeps = sum(r["smoother_sweeps"] for r in mixed)
+    sm_ms = sum(r["smoother_ms"] for r in mixed)
+    per_launch_s = sm_ms * 1e-3 / max(8 * sweeps, 1)
+    per_launch_bytes = bytes_per_sweep(nno, 4) / 8.0
+    peak, peak_kind = peaks()
+    achieved = per_launch_bytes / per_launch_s / 1e9 if per_launch_s > 0 else None
+
+    if rank != 0:
+        return 0
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": step_ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": workload_name(case), "mode": "FP32 multigrid + FP64 refinement (headline)",
+                   "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (FP32 stencils 267 MB, FP64 fine 535 MB)",
+                   "timing": "CUDA events around each Stokes solve inside the library, mean over timed steps"},
+        "fp64_plain": {"stokes_ms_per_step": stokes_ms_fp64,
+                       "uzawa_iterations": [r["uzawa"] for r in fp64], "mg_passes": [r["mg_passes"] for r in fp64],
+                       "residuals_final": res_fp64, "nu_top": nu_fp64[0], "vrms": vr_fp64},
+        "mixed": {"stokes_ms_per_step": stokes_ms, "uzawa_iterations": [r["uzawa"] for r in mixed],
+                  "mg_passes": [r["mg_passes"] for r in mixed], "residuals_final": res_mixed,
+                  "nu_top": nu_mixed[0], "vrms": vr_mixed,
+                  "nu_rel_err_vs_fp64": abs(nu_mixed[0] - nu_fp64[0]) / abs(nu_fp64[0]),
+                  "vrms_rel_err_vs_fp64": abs(vr_mixed - vr_fp64) / vr_fp64},
+        "speedup_mixed_vs_fp64": stokes_ms_fp64 / stokes_ms,
+        "roofline": {"bound": "hbm", "kernel": "k_gs_colour<float> (finest level)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": None,
+                     "peak_kind": peak_kind, "bytes_per_launch": per_launch_bytes,
+                     "launch_us": per_launch_s * 1e6},
+        "clocks": clk.summary(),
+        "gpu_launches": int(launches),
+        "wall_s_mixed": t1 - t0,
+    }
+    if not args.no_e2e:
+        e2e_ms, h2d, d2h = e2e_mode(cg, case, T0, min(args.steps, 3), 1)
+        line["e2e"] = {"value": e2e_ms, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_sample(case, T0)
+    print(json.dumps(line))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -62,6 +62,22 @@ class Config:
     fixed_timestep: float = 0.0
     precision: int = FP64
 
+    @property
+    def nox(self):
+        return self.mgunit[0] * 2 ** (self.levels - 1) + 1
+
+    @property
+    def noy(self):
+        return self.mgunit[1] * 2 ** (self.levels - 1) + 1
+
+    @property
+    def noz(self):
+        return self.mgunit[2] * 2 ** (self.levels - 1) + 1
+
+    @property
+    def nno(self):
+        return self.nox * self.noy * self.noz
+
     @classmethod
     def like(cls, other, **overrides) -> "Config":
         """Copy the matching attributes of any parameter object."""
@@ -111,7 +127,9 @@ class _CAdvection(ctypes.Structure):
 
 class _CStats(ctypes.Structure):
     _fields_ = [("uzawa_iterations", ctypes.c_int), ("del2_calls", ctypes.c_int), ("mg_passes", ctypes.c_int),
-                ("initial_residual", ctypes.c_double), ("stokes_ms", ctypes.c_double)]
+                ("initial_residual", ctypes.c_double), ("stokes_ms", ctypes.c_double), ("energy_ms", ctypes.c_double),
+                ("smoother_ms", ctypes.c_double), ("smoother_sweeps", ctypes.c_int),
+                ("kernel_launches", ctypes.c_ulonglong)]
 
 
 # every symbol of include/citcom_gb300.h with its argument types
@@ -141,6 +159,7 @@ _SIGNATURES = {
     "citcom_gpu_stokes_resident": (ctypes.c_int, [_H]),
     "citcom_gpu_step_resident": (ctypes.c_int, [_H, ctypes.POINTER(_CAdvection)]),
     "citcom_gpu_last_stats": (ctypes.c_int, [_H, ctypes.POINTER(_CStats)]),
+    "citcom_gpu_stokes_residuals": (ctypes.c_int, [_H, _D]),
     "citcom_gpu_op_kmul": (ctypes.c_int, [_H, ctypes.c_int, _D, _D]),
     "citcom_gpu_op_gauss_seidel": (ctypes.c_int, [_H, ctypes.c_int, _D, _D, _D, ctypes.c_int, ctypes.c_int]),
     "citcom_gpu_op_project": (ctypes.c_int, [_H, ctypes.c_int, _D, _D]),
@@ -261,7 +280,14 @@ class Solver:
         s = _CStats()
         self._check(self.lib.citcom_gpu_last_stats(self.h, ctypes.byref(s)))
         return dict(uzawa=s.uzawa_iterations, del2_calls=s.del2_calls, mg_passes=s.mg_passes,
-                    initial_residual=s.initial_residual, stokes_ms=s.stokes_ms)
+                    initial_residual=s.initial_residual, stokes_ms=s.stokes_ms, energy_ms=s.energy_ms,
+                    smoother_ms=s.smoother_ms, smoother_sweeps=s.smoother_sweeps, kernel_launches=s.kernel_launches)
+
+    def stokes_residuals(self):
+        """(|F - K U - G P| / |F|, |div U| / (|U| sqrt(npno/neq))) of the resident solution."""
+        out = np.zeros(2)
+        self._check(self.lib.citcom_gpu_stokes_residuals(self.h, _dp(out)))
+        return float(out[0]), float(out[1])
 
     # --------------------------------------------------------- set-up steps
     def get_system_viscosity(self, T):

@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -66,9 +67,14 @@ struct citcom_gpu
 	Red red;
 	cudaStream_t st;
 	cudaEvent_t ev0, ev1;
+	cudaEvent_t ev_gs[8];   // brackets the finest-level smoother calls inside a multigrid pass
+	int n_gs_pairs;         // pairs recorded by the captured pass
 	cudaGraphExec_t mg_exec;
+	unsigned long long pass_kernels;   // kernels in one captured multigrid pass
+	unsigned long long launches;       // kernels this handle has run
 	bool stiffness_ready;
 	bool visc_ready;
+	bool verbose;
 	citcom_gpu_stats stats;
 	std::vector<void *> allocs;
 	char err[512];
@@ -173,7 +179,25 @@ Rheo rheo_of(const citcom_gpu_config &c)
 
 // ---------------------------------------------------------------- gauss_seidel
 
+template <typename T> void gs_inner(citcom_gpu *h, MG<T> &B, int lev, T *d, const T *F, int cycles, int zero_start);
+
+// Gauss-Seidel call; on the finest level the call is bracketed by timing
+// events (captured into the multigrid graph) so that the dominant kernel's
+// device time is measured live during every solve.
 template <typename T> void gs(citcom_gpu *h, MG<T> &B, int lev, T *d, const T *F, int cycles, int zero_start)
+{
+	const bool timed = (lev == h->L - 1) && h->n_gs_pairs < 4 && !gs_small_fits(h->lv[lev]);
+	if(timed)
+		cudaEventRecord(h->ev_gs[2 * h->n_gs_pairs], h->st);
+	gs_inner<T>(h, B, lev, d, F, cycles, zero_start);
+	if(timed)
+	{
+		cudaEventRecord(h->ev_gs[2 * h->n_gs_pairs + 1], h->st);
+		h->n_gs_pairs++;
+	}
+}
+
+template <typename T> void gs_inner(citcom_gpu *h, MG<T> &B, int lev, T *d, const T *F, int cycles, int zero_start)
 {
 	const Lvl &L = h->lv[lev];
 	if(gs_small_fits(L))
@@ -256,9 +280,13 @@ int run_pass(citcom_gpu *h)
 	if(!h->mg_exec)
 	{
 		cudaGraph_t g;
+		h->n_gs_pairs = 0;
+		const unsigned long long k0 = g_kernel_launches;
 		CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
 		int r = record_pass(h);
 		cudaError_t e = cudaStreamEndCapture(h->st, &g);
+		h->pass_kernels = g_kernel_launches - k0;
+		g_kernel_launches = k0;
 		if(r != CITCOM_GPU_OK)
 			return r;
 		CK(e);
@@ -266,6 +294,7 @@ int run_pass(citcom_gpu *h)
 		CK(cudaGraphDestroy(g));
 	}
 	CK(cudaGraphLaunch(h->mg_exec, h->st));
+	g_kernel_launches += h->pass_kernels;
 	return CITCOM_GPU_OK;
 }
 
@@ -294,6 +323,17 @@ int solve_del2_u(citcom_gpu *h, double acc, int *valid)
 		TRY(run_pass(h));
 		TRY(readback(h, S_RES, 1));
 		residual = std::sqrt(h->hscal[S_RES] / neq);
+		for(int k = 0; k < h->n_gs_pairs; ++k)
+		{
+			float ms = 0.f;
+			if(cudaEventElapsedTime(&ms, h->ev_gs[2 * k], h->ev_gs[2 * k + 1]) == cudaSuccess)
+			{
+				h->stats.smoother_ms += ms;
+				h->stats.smoother_sweeps += h->cfg.vhighstep;
+			}
+			else
+				cudaGetLastError();
+		}
 		if(!(residual == residual))
 			return fail(h, CITCOM_GPU_ERR_NOCONV, "solve_del2_u: residual is NaN");
 		++count;
@@ -370,6 +410,9 @@ int uzawa(citcom_gpu *h, double *V, double *P, const double *F, double imp, int 
 		dpressure = alpha * std::sqrt(s2s2 / (1.0e-32 + pdotp));
 		dvelocity = alpha * std::sqrt(u1u1 / (1.0e-32 + vdotv));
 		++count;
+		if(h->verbose)
+			fprintf(stderr, "AhatP (%03d) v %12.6e dv/v %9.3e p %12.6e dp/p %9.3e mg %d\n", count, std::sqrt(vdotv / neq),
+			        dvelocity, std::sqrt(pdotp / npno), dpressure, h->stats.mg_passes);
 		sh = s1; s1 = s2; s2 = sh;
 		sh = r0; r0 = r1; r1 = r2; r2 = sh;
 		sh = z0; z0 = z1; z1 = sh;
@@ -434,6 +477,8 @@ int stokes_resident(citcom_gpu *h)
 	CK(cudaEventRecord(h->ev0, h->st));
 	h->stats.del2_calls = 0;
 	h->stats.mg_passes = 0;
+	h->stats.smoother_ms = 0.0;
+	h->stats.smoother_sweeps = 0;
 	launch_strip(h->st, Lf, h->U);  // velocities_conform_bcs with VB = 0
 	TRY(forces_from_device_T(h));
 	if(h->cfg.tdepv || !h->visc_ready)
@@ -589,6 +634,10 @@ int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 	h->mg_exec = nullptr;
 	h->stiffness_ready = false;
 	h->visc_ready = false;
+	{
+		const char *v = getenv("CITCOM_GPU_VERBOSE");
+		h->verbose = v && v[0] && v[0] != '0';
+	}
 	memset(&h->stats, 0, sizeof(h->stats));
 	int r = CITCOM_GPU_OK;
 #define TRYC(call)                  \
@@ -599,7 +648,10 @@ int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 			goto failed;            \
 	} while(0)
 	{
-		if(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess ||
+		bool ev_ok = true;
+		for(int k = 0; k < 8; ++k)
+			ev_ok = ev_ok && cudaEventCreate(&h->ev_gs[k]) == cudaSuccess;
+		if(!ev_ok || cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess ||
 		   cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess)
 		{
 			r = fail(h, CITCOM_GPU_ERR_CUDA, "stream/event creation failed");
@@ -709,6 +761,9 @@ void citcom_gpu_destroy(citcom_gpu *h)
 		cudaEventDestroy(h->ev0);
 	if(h->ev1)
 		cudaEventDestroy(h->ev1);
+	for(int k = 0; k < 8; ++k)
+		if(h->ev_gs[k])
+			cudaEventDestroy(h->ev_gs[k]);
 	if(h->st)
 		cudaStreamDestroy(h->st);
 	delete h;
@@ -782,6 +837,8 @@ int citcom_gpu_solve_Ahat_p_fhat_device(citcom_gpu *h, double *dV, double *dP, c
 		return fail(h, CITCOM_GPU_ERR_ARG, "null argument");
 	h->stats.del2_calls = 0;
 	h->stats.mg_passes = 0;
+	h->stats.smoother_ms = 0.0;
+	h->stats.smoother_sweeps = 0;
 	CK(cudaEventRecord(h->ev0, h->st));
 	TRY(uzawa(h, dV, dP, dF, imp, steps_max, initial_residual));
 	CK(cudaEventRecord(h->ev1, h->st));
@@ -921,9 +978,39 @@ int citcom_gpu_stokes_resident(citcom_gpu *h)
 int citcom_gpu_step_resident(citcom_gpu *h, citcom_gpu_advection *adv)
 {
 	TRY(check_handle(h));
+	cudaEvent_t a = h->ev_gs[6], b = h->ev_gs[7];
+	CK(cudaEventRecord(a, h->st));
 	TRY(pg_timestep(h, adv));
+	CK(cudaEventRecord(b, h->st));
 	TRY(stokes_resident(h));
-	return sync(h);
+	TRY(sync(h));
+	float ms = 0.f;
+	CK(cudaEventElapsedTime(&ms, a, b));
+	h->stats.energy_ms = ms;
+	return CITCOM_GPU_OK;
+}
+
+int citcom_gpu_stokes_residuals(citcom_gpu *h, double out[2])
+{
+	TRY(check_handle(h));
+	if(!out)
+		return fail(h, CITCOM_GPU_ERR_ARG, "null argument");
+	if(!h->stiffness_ready)
+		return fail(h, CITCOM_GPU_ERR_STATE, "construct_stiffness_B_matrix has not been called");
+	const int lmax = h->L - 1;
+	const Lvl &Lf = h->lv[lmax];
+	// momentum: F - K U - G P, with the FP64 operator
+	launch_grad(h->st, Lf, h->geo[lmax], h->P, h->Ah);
+	launch_kmul<double>(h->st, Lf, h->K64[lmax], h->U, h->u1);
+	launch_sub3(h->st, Lf.neq, h->r64, h->F, h->Ah, h->u1);
+	launch_div(h->st, Lf, h->geo[lmax], h->U, h->Eres);
+	launch_dots4(h->st, Lf.neq, h->r64, h->r64, h->F, h->F, h->U, h->U, nullptr, nullptr, red_of(h), h->dscal + S_DOT);
+	launch_dot(h->st, Lf.nel, h->Eres, h->Eres, red_of(h), h->dscal + S_DOT + 4);
+	TRY(readback(h, S_DOT, 5));
+	const double rr = h->hscal[S_DOT], ff = h->hscal[S_DOT + 1], uu = h->hscal[S_DOT + 2], dd = h->hscal[S_DOT + 4];
+	out[0] = std::sqrt(rr / (ff > 0.0 ? ff : 1.0));
+	out[1] = std::sqrt(dd) / (std::sqrt(uu) * std::sqrt((double)Lf.nel / (double)Lf.neq) + 1e-300);
+	return CITCOM_GPU_OK;
 }
 
 int citcom_gpu_last_stats(const citcom_gpu *h, citcom_gpu_stats *s)
@@ -931,6 +1018,7 @@ int citcom_gpu_last_stats(const citcom_gpu *h, citcom_gpu_stats *s)
 	if(!h || !s)
 		return CITCOM_GPU_ERR_ARG;
 	*s = h->stats;
+	s->kernel_launches = g_kernel_launches;
 	return CITCOM_GPU_OK;
 }
 
@@ -1066,7 +1154,10 @@ int citcom_gpu_op_multi_grid(citcom_gpu *h, double *d1, double *F, double *resid
 	const int lmax = h->L - 1;
 	const Lvl &Lf = h->lv[lmax];
 	TRY(h2d(h, h->mg64.fl[lmax], F, sizeof(double) * Lf.neq));
+	const int pairs = h->n_gs_pairs;
+	h->n_gs_pairs = 4;  // no smoother timing outside the captured pass
 	mg_pass<double>(h, h->mg64);
+	h->n_gs_pairs = pairs;
 	launch_dot(h->st, Lf.neq, h->mg64.res[lmax], h->mg64.res[lmax], red_of(h), h->dscal + S_RES);
 	TRY(d2h(h, d1, h->mg64.vel[lmax], sizeof(double) * Lf.neq));
 	TRY(d2h(h, F, h->mg64.res[lmax], sizeof(double) * Lf.neq));

@@ -1153,6 +1153,8 @@ __global__ void k_vrms(Lvl L, const Geo *__restrict__ geo, const double *__restr
 
 // ====================================================================== host
 
+unsigned long long g_kernel_launches = 0;
+
 void geo_fill_host(const Lvl &L, Geo *g)
 {
 	const double beta = 0.57735026918962576451;
@@ -1202,11 +1204,13 @@ void launch_assemble(cudaStream_t st, const Lvl &L, const Geo *geo, const double
                      float *K32, double *BI64, float *BI32)
 {
 	k_assemble<<<nblocks(L.nno, 128), 128, 0, st>>>(L, geo, evi, aug, lambda, K64, K32, BI64, BI32);
+	++g_kernel_launches;
 }
 
 void launch_bpi(cudaStream_t st, const Lvl &L, const Geo *geo, const double *BI64, double *BPI, int precond)
 {
 	k_bpi<<<nblocks(L.nel), TPB, 0, st>>>(L, geo, BI64, BPI, precond);
+	++g_kernel_launches;
 }
 
 static int max_colour(const Lvl &L)
@@ -1221,25 +1225,31 @@ template <typename T> void launch_kmul(cudaStream_t st, const Lvl &L, const T *K
 {
 	dim3 grid(nblocks(max_colour(L)), 8);
 	k_kmul<T, 0><<<grid, TPB, 0, st>>>(L, K, u, (const T *)nullptr, Au);
+	++g_kernel_launches;
 }
 
 template <typename T> void launch_residual(cudaStream_t st, const Lvl &L, const T *K, const T *f, const T *u, T *r)
 {
 	dim3 grid(nblocks(max_colour(L)), 8);
 	k_kmul<T, 1><<<grid, TPB, 0, st>>>(L, K, u, f, r);
+	++g_kernel_launches;
 }
 
 template <typename T>
 void launch_kmul_linesearch(cudaStream_t st, const Lvl &L, const T *K, const T *u, const T *res, T *Au, Red red, double *out2)
 {
 	k_kmul_ls<T><<<red_grid(L.nno), RED_THREADS, 0, st>>>(L, K, u, res, Au, red, out2);
+	++g_kernel_launches;
 }
 
 template <typename T> void launch_gs_colour(cudaStream_t st, const Lvl &L, const T *K, const T *BI, const T *F, T *d, int c)
 {
 	const int n = L.coff[c + 1] - L.coff[c];
 	if(n > 0)
+	{
 		k_gs_colour<T><<<nblocks(n), TPB, 0, st>>>(L, K, BI, F, d, c);
+		++g_kernel_launches;
+	}
 }
 
 bool gs_small_fits(const Lvl &L) { return L.nno <= 4 * GS_SMALL_THREADS; }
@@ -1248,22 +1258,26 @@ template <typename T>
 void launch_gs_small(cudaStream_t st, const Lvl &L, const T *K, const T *BI, const T *F, T *d, int cycles, int zero_start)
 {
 	k_gs_small<T><<<1, GS_SMALL_THREADS, 0, st>>>(L, K, BI, F, d, cycles, zero_start);
+	++g_kernel_launches;
 }
 
 template <typename T> void launch_project(cudaStream_t st, const Lvl &Lf, const Lvl &Lc, const T *AU, T *AD)
 {
 	k_project<T><<<nblocks(Lc.nno), TPB, 0, st>>>(Lf, Lc, AU, AD);
+	++g_kernel_launches;
 }
 
 template <typename T> void launch_interp(cudaStream_t st, const Lvl &Lc, const Lvl &Lf, const T *AD, T *AU)
 {
 	k_interp<T><<<nblocks(Lf.nno), TPB, 0, st>>>(Lc, Lf, AD, AU);
+	++g_kernel_launches;
 }
 
 template <typename T>
 void launch_vel_update(cudaStream_t st, int n, T *vel, const T *del, T *res, const T *AU, const double *nd, int update_res)
 {
 	k_vel_update<T><<<nblocks(n), TPB, 0, st>>>(n, vel, del, res, AU, nd, update_res);
+	++g_kernel_launches;
 }
 
 #define INST(T)                                                                                                              \
@@ -1282,11 +1296,13 @@ INST(float)
 void launch_div(cudaStream_t st, const Lvl &L, const Geo *geo, const double *U, double *divU)
 {
 	k_div<<<nblocks(L.nel), TPB, 0, st>>>(L, geo, U, divU);
+	++g_kernel_launches;
 }
 
 void launch_grad(cudaStream_t st, const Lvl &L, const Geo *geo, const double *P, double *gradP)
 {
 	k_grad<<<nblocks(L.nno), TPB, 0, st>>>(L, geo, P, gradP);
+	++g_kernel_launches;
 }
 
 void launch_strip(cudaStream_t st, const Lvl &L, double *r) { k_strip<<<nblocks(L.nno), TPB, 0, st>>>(L, r); }
@@ -1294,17 +1310,20 @@ void launch_strip(cudaStream_t st, const Lvl &L, double *r) { k_strip<<<nblocks(
 void launch_dot(cudaStream_t st, int n, const double *a, const double *b, Red red, double *out)
 {
 	k_dot<<<red_grid(n), RED_THREADS, 0, st>>>(n, a, b, red, out);
+	++g_kernel_launches;
 }
 
 void launch_dots4(cudaStream_t st, int n, const double *a0, const double *b0, const double *a1, const double *b1, const double *a2,
                   const double *b2, const double *a3, const double *b3, Red red, double *out)
 {
 	k_dots4<<<red_grid(n), RED_THREADS, 0, st>>>(n, a0, b0, a1, b1, a2, b2, a3, b3, red, out);
+	++g_kernel_launches;
 }
 
 void launch_axpby(cudaStream_t st, int n, double *y, double a, const double *x, double b)
 {
 	k_axpby<<<nblocks(n), TPB, 0, st>>>(n, y, a, x, b);
+	++g_kernel_launches;
 }
 
 void launch_mul(cudaStream_t st, int n, double *z, const double *a, const double *b) { k_mul<<<nblocks(n), TPB, 0, st>>>(n, z, a, b); }
@@ -1312,11 +1331,13 @@ void launch_mul(cudaStream_t st, int n, double *z, const double *a, const double
 void launch_lin2(cudaStream_t st, int n, double *z, double a, const double *x, double b, const double *y)
 {
 	k_lin2<<<nblocks(n), TPB, 0, st>>>(n, z, a, x, b, y);
+	++g_kernel_launches;
 }
 
 void launch_sub3(cudaStream_t st, int n, double *z, const double *f, const double *a, const double *b)
 {
 	k_sub3<<<nblocks(n), TPB, 0, st>>>(n, z, f, a, b);
+	++g_kernel_launches;
 }
 
 void launch_copy_d2f(cudaStream_t st, int n, float *dst, const double *src) { k_d2f<<<nblocks(n), TPB, 0, st>>>(n, dst, src); }
@@ -1326,19 +1347,24 @@ void launch_add_f2d(cudaStream_t st, int n, double *dst, const float *src) { k_a
 void launch_residual64(cudaStream_t st, const Lvl &L, const double *K, const double *f, const double *u, double *r, Red red, double *out)
 {
 	k_residual64<<<red_grid(L.nno), RED_THREADS, 0, st>>>(L, K, f, u, r, red, out);
+	++g_kernel_launches;
 }
 
 void launch_visc_from_T(cudaStream_t st, const Lvl &L, const Geo *geo, const Rheo &r, const double *T, double *evi)
 {
 	k_visc_from_T<<<nblocks(L.nel), TPB, 0, st>>>(L, geo, r, T, evi);
+	++g_kernel_launches;
 }
 
 void launch_project_viscosity(cudaStream_t st, const Lvl &Lf, const Lvl &Lc, const Geo *geoc, const double *evi_f, double *evi_c,
                               double *work_f, double *work_c)
 {
 	k_visc_to_nodes<<<nblocks(Lf.nno), TPB, 0, st>>>(Lf, evi_f, work_f);
+	++g_kernel_launches;
 	k_project_scalar<<<nblocks(Lc.nno), TPB, 0, st>>>(Lf, Lc, work_f, work_c);
+	++g_kernel_launches;
 	k_visc_to_gint<<<nblocks(Lc.nel), TPB, 0, st>>>(Lc, geoc, work_c, evi_c);
+	++g_kernel_launches;
 }
 
 void launch_buoyancy(cudaStream_t st, const Lvl &L, double Ra, const double *T, double *buoy)
@@ -1346,48 +1372,58 @@ void launch_buoyancy(cudaStream_t st, const Lvl &L, double Ra, const double *T, 
 	// the layer means go into the tail of `buoy`'s companion buffer: buoy + nno (caller sizes it nno + noz)
 	double *H = buoy + L.nno;
 	k_horiz_ave<<<L.noz, TPB, 0, st>>>(L, Ra, T, H);
+	++g_kernel_launches;
 	k_buoyancy<<<nblocks(L.nno), TPB, 0, st>>>(L, Ra, T, H, buoy);
+	++g_kernel_launches;
 }
 
 void launch_forces(cudaStream_t st, const Lvl &L, const Geo *geo, const double *buoy, double *F)
 {
 	k_forces<<<nblocks(L.nno), TPB, 0, st>>>(L, geo, buoy, F);
+	++g_kernel_launches;
 }
 
 void launch_v_from_vector(cudaStream_t st, const Lvl &L, const double *U, double *V)
 {
 	k_v_from_vector<<<nblocks(L.nno), TPB, 0, st>>>(L, U, V);
+	++g_kernel_launches;
 }
 
 void launch_pg_residual(cudaStream_t st, const Lvl &L, const Geo *geo, const double *T, const double *Tdot, const double *V, double Q0,
                         double *Eres)
 {
 	k_pg_residual<<<nblocks(L.nel, 128), 128, 0, st>>>(L, geo, T, Tdot, V, Q0, Eres);
+	++g_kernel_launches;
 }
 
 void launch_pg_gather(cudaStream_t st, const Lvl &L, const double *Eres, double *DTdot)
 {
 	k_pg_gather<<<nblocks(L.nno), TPB, 0, st>>>(L, Eres, DTdot);
+	++g_kernel_launches;
 }
 
 void launch_predictor(cudaStream_t st, const Lvl &L, double *T, double *Tdot, double dt, double gamma)
 {
 	k_predictor<<<nblocks(L.nno), TPB, 0, st>>>(L, T, Tdot, dt, gamma);
+	++g_kernel_launches;
 }
 
 void launch_corrector(cudaStream_t st, const Lvl &L, double *T, double *Tdot, const double *DTdot, double dt, double gamma)
 {
 	k_corrector<<<nblocks(L.nno), TPB, 0, st>>>(L, T, Tdot, DTdot, dt, gamma);
+	++g_kernel_launches;
 }
 
 void launch_tmax(cudaStream_t st, int n, const double *T, Red red, double *out)
 {
 	k_max<<<red_grid(n), RED_THREADS, 0, st>>>(n, T, red, out);
+	++g_kernel_launches;
 }
 
 void launch_adv_timestep(cudaStream_t st, const Lvl &L, const double *V, Red red, double *out)
 {
 	k_adv_step<<<red_grid(L.nel), RED_THREADS, 0, st>>>(L, V, red, out);
+	++g_kernel_launches;
 }
 
 void launch_conform_T(cudaStream_t st, const Lvl &L, double *T) { k_conform_T<<<nblocks(L.nno), TPB, 0, st>>>(L, T); }
@@ -1396,11 +1432,15 @@ void launch_heat_flux(cudaStream_t st, const Lvl &L, const Geo *geo, const doubl
 {
 	// work holds nel element means then nno nodal fluxes
 	k_hf_elem<<<nblocks(L.nel), TPB, 0, st>>>(L, geo, T, V, work);
+	++g_kernel_launches;
 	k_hf_node<<<nblocks(L.nno), TPB, 0, st>>>(L, work, work + L.nel);
+	++g_kernel_launches;
 	k_hf_surface<<<red_grid((long)L.elx * L.ely), RED_THREADS, 0, st>>>(L, work + L.nel, red, out);
+	++g_kernel_launches;
 }
 
 void launch_vrms(cudaStream_t st, const Lvl &L, const Geo *geo, const double *V, Red red, double *out)
 {
 	k_vrms<<<red_grid(L.nel), RED_THREADS, 0, st>>>(L, geo, V, red, out);
+	++g_kernel_launches;
 }

@@ -27,6 +27,10 @@ struct Red
 
 void geo_fill_host(const Lvl &L, Geo *g);
 
+// kernels issued by the launchers below since load (host-side count; a graph
+// capture counts its kernels once, each replay is added by the driver)
+extern unsigned long long g_kernel_launches;
+
 // set-up
 void launch_assemble(cudaStream_t st, const Lvl &L, const Geo *geo, const double *evi, int aug, double lambda,
                      double *K64, float *K32, double *BI64, float *BI32);

@@ -16,7 +16,9 @@
  * *_device variants take device pointers and do no host traffic.
  *
  * Every function returns CITCOM_GPU_OK (0) or a negative error code; the
- * message is available from citcom_gpu_error_string().  There is no CPU
+ * message is available from citcom_gpu_error_string().  Setting the
+ * environment variable CITCOM_GPU_VERBOSE=1 prints one line per Uzawa
+ * iteration in the spirit of the reference's generate_log_message.  There is no CPU
  * fallback: without a usable CUDA device citcom_gpu_create fails.
  *
  * Scope: Cartesian box, uniform spacing per axis on every multigrid level,
@@ -85,6 +87,10 @@ typedef struct citcom_gpu_stats
 	int mg_passes;              /* multi_grid calls */
 	double initial_residual;    /* return value of solve_Ahat_p_fhat */
 	double stokes_ms;           /* device time of the last solve (CUDA events) */
+	double energy_ms;           /* device time of the last PG_timestep of step_resident */
+	double smoother_ms;         /* device time of the finest-level Gauss-Seidel calls */
+	int smoother_sweeps;        /* finest-level sweeps (8 colour launches each) in smoother_ms */
+	unsigned long long kernel_launches;  /* kernels launched by the library since it was loaded */
 } citcom_gpu_stats;
 
 /* Allocates every device buffer the solver will use (on the current
@@ -144,6 +150,11 @@ int citcom_gpu_store_state(citcom_gpu *h, double *T, double *Tdot, double *U, do
 int citcom_gpu_stokes_resident(citcom_gpu *h);
 int citcom_gpu_step_resident(citcom_gpu *h, citcom_gpu_advection *adv);
 int citcom_gpu_last_stats(const citcom_gpu *h, citcom_gpu_stats *s);
+/* Residuals of the resident solution, in FP64: out[0] = |F - K U - G P| / |F|
+ * (momentum), out[1] = |div U| / (|U| sqrt(npno/neq)) (continuity).  No
+ * counterpart in the reference, which stops on the relative increments
+ * dv/v and dp/p (Stokes_flow_Incomp.c:393, 442-443). */
+int citcom_gpu_stokes_residuals(citcom_gpu *h, double out[2]);
 
 /* Single operators of level lev, host buffers (the kernels the solver uses;
  * exposed for parity checks against the reference's routines). */

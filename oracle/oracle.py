@@ -332,6 +332,14 @@ class Oracle:
         v = lib().oracle_solve_del2_u(self.h, _dp(d0), _dp(f), acc, ctypes.byref(calls))
         return d0[:neq], v, calls.value
 
+    def solve_Ahat_p_fhat(self, imp, steps):
+        """solve_Ahat_p_fhat on the oracle's own U, P, F (after setup_operators)."""
+        st, c, m = ctypes.c_int(steps), ctypes.c_int(0), ctypes.c_int(0)
+        r = lib().oracle_solve_Ahat_p_fhat(self.h, lib().oracle_U(self.h), lib().oracle_P(self.h),
+                                           lib().oracle_F(self.h), imp, ctypes.byref(st), ctypes.byref(c),
+                                           ctypes.byref(m))
+        return dict(residual=r, uzawa=st.value, del2_calls=c.value, mg_calls=m.value)
+
     def stokes(self):
         s, c, m = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
         r = lib().oracle_stokes(self.h, ctypes.byref(s), ctypes.byref(c), ctypes.byref(m))
