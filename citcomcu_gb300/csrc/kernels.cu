@@ -24,6 +24,17 @@ namespace {
 
 constexpr int TPB = 256;
 
+// Programmatic dependent launch: every kernel first waits for its
+// predecessor in the stream to finish (griddepcontrol.wait), then lets its own
+// successor start launching (griddepcontrol.launch_dependents), so the launch
+// latency of the next kernel overlaps this kernel's execution.  Both are
+// no-ops when a kernel was launched without the attribute.
+__device__ __forceinline__ void pdl_begin()
+{
+	asm volatile("griddepcontrol.wait;" ::: "memory");
+	asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 inline int nblocks(long n, int tpb = TPB) { return (int)((n + tpb - 1) / tpb); }
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
@@ -38,6 +49,8 @@ __device__ __forceinline__ int colour_of_pos(const Lvl &L, int p)
 }
 
 template <typename T> __device__ __forceinline__ T ldcs(const T *p) { return __ldcs(p); }
+
+
 
 // ---------------------------------------------------------------- reduce
 
@@ -116,6 +129,7 @@ inline int red_grid(long n)
 __global__ void k_assemble(Lvl L, const Geo *__restrict__ geo, const double *__restrict__ evi, int aug, double lambda,
                            double *__restrict__ K64, float *__restrict__ K32, double *__restrict__ BI64, float *__restrict__ BI32)
 {
+	pdl_begin();
 	const int p = blockIdx.x * blockDim.x + threadIdx.x;
 	if(p >= L.nno)
 		return;
@@ -198,29 +212,32 @@ __global__ void k_assemble(Lvl L, const Geo *__restrict__ geo, const double *__r
 						blk[3 * i + j] = 0.0;
 		}
 #pragma unroll
-		for(int q = 0; q < 9; ++q)
-		{
-			const size_t off = (size_t)(9 * s + q) * L.npad + p;
-			if(K64)
-				K64[off] = blk[q];
-			if(K32)
-				K32[off] = (float)blk[q];
-		}
+		for(int i = 0; i < 3; ++i)
+#pragma unroll
+			for(int j = 0; j < 3; ++j)
+			{
+				const size_t off = cg_kidx(L, s, i, j, p);
+				if(K64)
+					K64[off] = blk[3 * i + j];
+				if(K32)
+					K32[off] = (float)blk[3 * i + j];
+			}
 	}
 #pragma unroll
 	for(int i = 0; i < 3; ++i)
 	{
 		const double bi = 1.0 / diag[i];
 		if(BI64)
-			BI64[(size_t)i * L.npad + p] = bi;
+			BI64[3 * (size_t)p + i] = bi;
 		if(BI32)
-			BI32[(size_t)i * L.npad + p] = (float)bi;
+			BI32[3 * (size_t)p + i] = (float)bi;
 	}
 }
 
 // build_diagonal_of_Ahat / assemble_dAhatp_entry (Element_calculations.c:654-689, 771-829)
 __global__ void k_bpi(Lvl L, const Geo *__restrict__ geo, const double *__restrict__ BI, double *__restrict__ BPI, int precond)
 {
+	pdl_begin();
 	const int e = blockIdx.x * blockDim.x + threadIdx.x;
 	if(e >= L.nel)
 		return;
@@ -238,7 +255,7 @@ __global__ void k_bpi(Lvl L, const Geo *__restrict__ geo, const double *__restri
 		for(int i = 0; i < 3; ++i)
 		{
 			const double g = geo->g[3 * a + i];
-			bu += g * g * BI[(size_t)i * L.npad + p];
+			bu += g * g * BI[3 * (size_t)p + i];
 		}
 	}
 	BPI[e] = (bu != 0.0) ? 1.0 / bu : 1.0;
@@ -246,18 +263,18 @@ __global__ void k_bpi(Lvl L, const Geo *__restrict__ geo, const double *__restri
 
 // ---------------------------------------------------------------- stencil
 
-// row product of node (x,y,z) at colour-major position p: out = sum_m K_{n,m} u_m.
-// Neighbours outside the mesh are clamped onto the mesh; their coefficients
-// are zero, so they contribute nothing.
-// `u` is deliberately not __restrict__: the single-CTA smoother reads values
-// that other threads of the block wrote in the previous colour.
-template <typename T>
-__device__ __forceinline__ void row_product(const Lvl &L, const T *__restrict__ K, const T *u, int p, int x, int y,
-                                            int z, T &o0, T &o1, T &o2)
+// Row i of node (x,y,z) at colour-major position p: sum over the 27
+// neighbours m of K_{n,m}[i][:] . u_m.  Three threads share a node (one per
+// row), which triples the memory-level parallelism of the gather.
+// Neighbours outside the mesh are clamped onto it; their coefficients are
+// zero.  `u` is deliberately not __restrict__: the single-CTA smoothers read
+// values that other threads of the block wrote in the previous colour.
+template <typename T, bool STREAM>
+__device__ __forceinline__ T row_dot(const Lvl &L, const T *K, const T *u, int p, int i, int x, int y, int z)
 {
-	T a0 = 0, a1 = 0, a2 = 0;
-	const size_t np = (size_t)L.npad;
-	const T *kp = K + p;
+	T a = 0;
+	const size_t s3 = 3 * (size_t)L.npad;
+	const T *kp = K + 3 * (size_t)p + i;
 #pragma unroll
 	for(int dy = -1; dy <= 1; ++dy)
 	{
@@ -265,50 +282,41 @@ __device__ __forceinline__ void row_product(const Lvl &L, const T *__restrict__ 
 #pragma unroll
 		for(int dx = -1; dx <= 1; ++dx)
 		{
-			const int xx = clampi(x + dx, 0, L.nox - 1);
-			const int base = L.noz * (xx + L.nox * yy);
+			const int base = L.noz * (clampi(x + dx, 0, L.nox - 1) + L.nox * yy);
 #pragma unroll
 			for(int dz = -1; dz <= 1; ++dz)
 			{
-				const int zz = clampi(z + dz, 0, L.noz - 1);
-				const int m = base + zz;
-				const int s = (dz + 1) + 3 * (dx + 1) + 9 * (dy + 1);
-				const T *kc = kp + (size_t)(9 * s) * np;
-				const T u0 = u[3 * m], u1 = u[3 * m + 1], u2 = u[3 * m + 2];
-				a0 += ldcs(kc + 0 * np) * u0 + ldcs(kc + 1 * np) * u1 + ldcs(kc + 2 * np) * u2;
-				a1 += ldcs(kc + 3 * np) * u0 + ldcs(kc + 4 * np) * u1 + ldcs(kc + 5 * np) * u2;
-				a2 += ldcs(kc + 6 * np) * u0 + ldcs(kc + 7 * np) * u1 + ldcs(kc + 8 * np) * u2;
+				const int m = base + clampi(z + dz, 0, L.noz - 1);
+				const T *kc = kp + (size_t)(3 * ((dz + 1) + 3 * (dx + 1) + 9 * (dy + 1))) * s3;
+				const T k0 = STREAM ? ldcs(kc) : kc[0];
+				const T k1 = STREAM ? ldcs(kc + s3) : kc[s3];
+				const T k2 = STREAM ? ldcs(kc + 2 * s3) : kc[2 * s3];
+				a += k0 * u[3 * m] + k1 * u[3 * m + 1] + k2 * u[3 * m + 2];
 			}
 		}
 	}
-	o0 = a0;
-	o1 = a1;
-	o2 = a2;
+	return a;
 }
 
-// MODE 0: out = K u;  MODE 1: out = f - K u
+constexpr int TPB3 = 192;  // multiple of 3 and of 32: a node's three rows share a block
+
+// MODE 0: out = K u;  MODE 1: out = f - K u.  Grid: x over 3 * colour size, y over colours.
 template <typename T, int MODE>
 __global__ void k_kmul(Lvl L, const T *__restrict__ K, const T *__restrict__ u, const T *__restrict__ f, T *__restrict__ out)
 {
+	pdl_begin();
 	const int c = blockIdx.y;
-	const int q = blockIdx.x * blockDim.x + threadIdx.x;
+	const int t = blockIdx.x * blockDim.x + threadIdx.x;
+	const int q = t / 3, i = t - 3 * q;
 	if(q >= L.coff[c + 1] - L.coff[c])
 		return;
 	int x, y, z;
 	cg_decode(L, c, q, x, y, z);
-	const int p = L.coff[c] + q;
 	const int n = cg_node(L, x, y, z);
-	T r0, r1, r2;
-	row_product(L, K, u, p, x, y, z, r0, r1, r2);
+	T r = row_dot<T, true>(L, K, u, L.coff[c] + q, i, x, y, z);
 	if(MODE == 1)
-	{
-		r0 = f[3 * n] - r0;
-		r1 = f[3 * n + 1] - r1;
-		r2 = f[3 * n + 2] - r2;
-	}
-	out[3 * n] = r0;
-	out[3 * n + 1] = r1;
-	out[3 * n + 2] = r2;
+		r = f[3 * n + i] - r;
+	out[3 * n + i] = r;
 }
 
 // AU = K u together with AU.AU and AU.res (the line search of multi_grid,
@@ -317,20 +325,19 @@ template <typename T>
 __global__ void k_kmul_ls(Lvl L, const T *__restrict__ K, const T *__restrict__ u, const T *__restrict__ res, T *__restrict__ Au,
                           Red red, double *out2)
 {
+	pdl_begin();
 	double v[2] = {0.0, 0.0};
-	for(int p = blockIdx.x * blockDim.x + threadIdx.x; p < L.nno; p += gridDim.x * blockDim.x)
+	for(int t = blockIdx.x * blockDim.x + threadIdx.x; t < 3 * L.nno; t += gridDim.x * blockDim.x)
 	{
+		const int p = t / 3, i = t - 3 * p;
 		const int c = colour_of_pos(L, p);
 		int x, y, z;
 		cg_decode(L, c, p - L.coff[c], x, y, z);
 		const int n = cg_node(L, x, y, z);
-		T r0, r1, r2;
-		row_product(L, K, u, p, x, y, z, r0, r1, r2);
-		Au[3 * n] = r0;
-		Au[3 * n + 1] = r1;
-		Au[3 * n + 2] = r2;
-		v[0] += (double)r0 * (double)res[3 * n] + (double)r1 * (double)res[3 * n + 1] + (double)r2 * (double)res[3 * n + 2];
-		v[1] += (double)r0 * (double)r0 + (double)r1 * (double)r1 + (double)r2 * (double)r2;
+		const T r = row_dot<T, true>(L, K, u, p, i, x, y, z);
+		Au[3 * n + i] = r;
+		v[0] += (double)r * (double)res[3 * n + i];
+		v[1] += (double)r * (double)r;
 	}
 	block_reduce_store<2>(v, red, out2);
 }
@@ -340,6 +347,7 @@ template <typename T>
 __global__ void k_vel_update(int n, T *__restrict__ vel, const T *__restrict__ del, T *__restrict__ res, const T *__restrict__ AU,
                              const double *__restrict__ nd, int update_res)
 {
+	pdl_begin();
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i >= n)
 		return;
@@ -349,54 +357,120 @@ __global__ void k_vel_update(int n, T *__restrict__ vel, const T *__restrict__ d
 		res[i] -= (T)(alpha * (double)AU[i]);
 }
 
-// one Gauss-Seidel colour: d_n += (F_n - sum_m K_{n,m} d_m) o BI_n
+// One Gauss-Seidel colour: d_n += (F_n - sum_m K_{n,m} d_m) o BI_n.  The three
+// rows of a node are relaxed together from the same d (the reference's
+// "Jacobi at a node"), so all rows are read before any is written.
 template <typename T>
-__global__ void k_gs_colour(Lvl L, const T *__restrict__ K, const T *__restrict__ BI, const T *__restrict__ F, T *d, int c)
+__global__ void __launch_bounds__(TPB3) k_gs_colour(Lvl L, const T *__restrict__ K, const T *__restrict__ BI,
+                                                    const T *__restrict__ F, T *d, int c)
 {
-	const int q = blockIdx.x * blockDim.x + threadIdx.x;
-	if(q >= L.coff[c + 1] - L.coff[c])
-		return;
-	int x, y, z;
-	cg_decode(L, c, q, x, y, z);
-	const int p = L.coff[c] + q;
-	const int n = cg_node(L, x, y, z);
-	T r0, r1, r2;
-	row_product(L, K, d, p, x, y, z, r0, r1, r2);
-	const size_t np = (size_t)L.npad;
-	d[3 * n] += (F[3 * n] - r0) * BI[p];
-	d[3 * n + 1] += (F[3 * n + 1] - r1) * BI[np + p];
-	d[3 * n + 2] += (F[3 * n + 2] - r2) * BI[2 * np + p];
+	pdl_begin();
+	const int t = blockIdx.x * blockDim.x + threadIdx.x;
+	const int q = t / 3, i = t - 3 * q;
+	const bool active = q < L.coff[c + 1] - L.coff[c];
+	T upd = 0;
+	int n = 0;
+	if(active)
+	{
+		int x, y, z;
+		cg_decode(L, c, q, x, y, z);
+		n = cg_node(L, x, y, z);
+		const int p = L.coff[c] + q;
+		upd = (F[3 * n + i] - row_dot<T, true>(L, K, d, p, i, x, y, z)) * BI[3 * (size_t)p + i];
+	}
+	__syncthreads();
+	if(active)
+		d[3 * n + i] += upd;
 }
 
-// all sweeps and colours of one gauss_seidel call on a small level in one CTA
-constexpr int GS_SMALL_THREADS = 1024;
+// All sweeps and colours of one gauss_seidel call on a small level in one CTA
+// (coefficients read through L2).
+constexpr int GS_SMALL_THREADS = 1023;  // multiple of 3
 template <typename T>
-__global__ void __launch_bounds__(GS_SMALL_THREADS) k_gs_small(Lvl L, const T *__restrict__ K, const T *__restrict__ BI,
-                                                               const T *__restrict__ F, T *d, int cycles, int zero_start)
+__global__ void __launch_bounds__(1024) k_gs_small(Lvl L, const T *__restrict__ K, const T *__restrict__ BI,
+                                                   const T *__restrict__ F, T *d, int cycles, int zero_start)
 {
+	pdl_begin();
 	if(zero_start)
 		for(int i = threadIdx.x; i < L.neq; i += blockDim.x)
 			d[i] = 0;
 	__syncthreads();
-	const size_t np = (size_t)L.npad;
 	for(int cyc = 0; cyc < cycles; ++cyc)
 		for(int c = 0; c < 8; ++c)
 		{
-			const int nc = L.coff[c + 1] - L.coff[c];
-			for(int q = threadIdx.x; q < nc; q += blockDim.x)
+			const int nr = 3 * (L.coff[c + 1] - L.coff[c]);
+			for(int t0 = 0; t0 < nr; t0 += blockDim.x)
 			{
-				int x, y, z;
-				cg_decode(L, c, q, x, y, z);
-				const int p = L.coff[c] + q;
-				const int n = cg_node(L, x, y, z);
-				T r0, r1, r2;
-				row_product(L, K, d, p, x, y, z, r0, r1, r2);
-				d[3 * n] += (F[3 * n] - r0) * BI[p];
-				d[3 * n + 1] += (F[3 * n + 1] - r1) * BI[np + p];
-				d[3 * n + 2] += (F[3 * n + 2] - r2) * BI[2 * np + p];
+				const int t = t0 + threadIdx.x;
+				const int q = t / 3, i = t - 3 * q;
+				T upd = 0;
+				int n = 0;
+				if(t < nr)
+				{
+					int x, y, z;
+					cg_decode(L, c, q, x, y, z);
+					n = cg_node(L, x, y, z);
+					const int p = L.coff[c] + q;
+					upd = (F[3 * n + i] - row_dot<T, false>(L, K, d, p, i, x, y, z)) * BI[3 * (size_t)p + i];
+				}
+				__syncthreads();
+				if(t < nr)
+					d[3 * n + i] += upd;
 			}
 			__syncthreads();
 		}
+}
+
+// The same smoother with the level's stencil, 1/diag, F and d staged in
+// shared memory (coarsest levels): every colour phase then reads shared
+// memory only, which takes the L2 latency out of the 20-sweep coarse solve of
+// every V-cycle.
+template <typename T>
+__global__ void __launch_bounds__(1024) k_gs_small_smem(Lvl L, const T *__restrict__ K, const T *__restrict__ BI,
+                                                        const T *__restrict__ F, T *d, int cycles, int zero_start)
+{
+	pdl_begin();
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	T *sK = reinterpret_cast<T *>(smem_raw);  // 243 * npad
+	T *sB = sK + (size_t)243 * L.npad;         // 3 * npad
+	T *sF = sB + (size_t)3 * L.npad;           // neq
+	T *sd = sF + L.neq;                        // neq
+	for(int i = threadIdx.x; i < 243 * L.npad; i += blockDim.x)
+		sK[i] = K[i];
+	for(int i = threadIdx.x; i < 3 * L.npad; i += blockDim.x)
+		sB[i] = BI[i];
+	for(int i = threadIdx.x; i < L.neq; i += blockDim.x)
+	{
+		sF[i] = F[i];
+		sd[i] = zero_start ? (T)0 : d[i];
+	}
+	__syncthreads();
+	for(int cyc = 0; cyc < cycles; ++cyc)
+		for(int c = 0; c < 8; ++c)
+		{
+			const int nr = 3 * (L.coff[c + 1] - L.coff[c]);
+			for(int t0 = 0; t0 < nr; t0 += blockDim.x)
+			{
+				const int t = t0 + threadIdx.x;
+				const int q = t / 3, i = t - 3 * q;
+				T upd = 0;
+				int n = 0;
+				if(t < nr)
+				{
+					int x, y, z;
+					cg_decode(L, c, q, x, y, z);
+					n = cg_node(L, x, y, z);
+					const int p = L.coff[c] + q;
+					upd = (sF[3 * n + i] - row_dot<T, false>(L, sK, sd, p, i, x, y, z)) * sB[3 * p + i];
+				}
+				__syncthreads();
+				if(t < nr)
+					sd[3 * n + i] += upd;
+			}
+			__syncthreads();
+		}
+	for(int i = threadIdx.x; i < L.neq; i += blockDim.x)
+		d[i] = sd[i];
 }
 
 // ---------------------------------------------------------------- transfers
@@ -406,6 +480,7 @@ __global__ void __launch_bounds__(GS_SMALL_THREADS) k_gs_small(Lvl L, const T *_
 template <typename T>
 __global__ void k_project(Lvl Lf, Lvl Lc, const T *__restrict__ AU, T *__restrict__ AD)
 {
+	pdl_begin();
 	const int N = blockIdx.x * blockDim.x + threadIdx.x;
 	if(N >= Lc.nno)
 		return;
@@ -462,6 +537,7 @@ template <typename T> __device__ __forceinline__ T fill_z(const Lvl &Lc, const T
 template <typename T>
 __global__ void k_interp(Lvl Lc, Lvl Lf, const T *__restrict__ AD, T *__restrict__ AU)
 {
+	pdl_begin();
 	const int n = blockIdx.x * blockDim.x + threadIdx.x;
 	if(n >= Lf.nno)
 		return;
@@ -484,6 +560,7 @@ __global__ void k_interp(Lvl Lc, Lvl Lf, const T *__restrict__ AD, T *__restrict
 // assemble_div_u (Element_calculations.c:691-722)
 __global__ void k_div(Lvl L, const Geo *__restrict__ geo, const double *__restrict__ U, double *__restrict__ divU)
 {
+	pdl_begin();
 	const int e = blockIdx.x * blockDim.x + threadIdx.x;
 	if(e >= L.nel)
 		return;
@@ -501,6 +578,7 @@ __global__ void k_div(Lvl L, const Geo *__restrict__ geo, const double *__restri
 // assemble_grad_p (Element_calculations.c:727-769) as a node-centred gather
 __global__ void k_grad(Lvl L, const Geo *__restrict__ geo, const double *__restrict__ P, double *__restrict__ gradP)
 {
+	pdl_begin();
 	const int n = blockIdx.x * blockDim.x + threadIdx.x;
 	if(n >= L.nno)
 		return;
@@ -524,6 +602,7 @@ __global__ void k_grad(Lvl L, const Geo *__restrict__ geo, const double *__restr
 
 __global__ void k_strip(Lvl L, double *r)
 {
+	pdl_begin();
 	const int n = blockIdx.x * blockDim.x + threadIdx.x;
 	if(n >= L.nno)
 		return;
@@ -538,6 +617,7 @@ __global__ void k_strip(Lvl L, double *r)
 
 __global__ void k_dot(int n, const double *__restrict__ a, const double *__restrict__ b, Red red, double *out)
 {
+	pdl_begin();
 	double v[1] = {0.0};
 	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
 		v[0] += a[i] * b[i];
@@ -547,6 +627,7 @@ __global__ void k_dot(int n, const double *__restrict__ a, const double *__restr
 __global__ void k_dots4(int n, const double *a0, const double *b0, const double *a1, const double *b1, const double *a2,
                         const double *b2, const double *a3, const double *b3, Red red, double *out)
 {
+	pdl_begin();
 	double v[4] = {0.0, 0.0, 0.0, 0.0};
 	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
 	{
@@ -564,6 +645,7 @@ __global__ void k_dots4(int n, const double *a0, const double *b0, const double 
 
 __global__ void k_axpby(int n, double *y, double a, const double *x, double b)
 {
+	pdl_begin();
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i < n)
 		y[i] = a * y[i] + b * x[i];
@@ -571,6 +653,7 @@ __global__ void k_axpby(int n, double *y, double a, const double *x, double b)
 
 __global__ void k_mul(int n, double *z, const double *a, const double *b)
 {
+	pdl_begin();
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i < n)
 		z[i] = a[i] * b[i];
@@ -578,6 +661,7 @@ __global__ void k_mul(int n, double *z, const double *a, const double *b)
 
 __global__ void k_lin2(int n, double *z, double a, const double *x, double b, const double *y)
 {
+	pdl_begin();
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i < n)
 		z[i] = a * x[i] + b * y[i];
@@ -585,6 +669,7 @@ __global__ void k_lin2(int n, double *z, double a, const double *x, double b, co
 
 __global__ void k_sub3(int n, double *z, const double *f, const double *a, const double *b)
 {
+	pdl_begin();
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i < n)
 		z[i] = f[i] - a[i] - b[i];
@@ -592,6 +677,7 @@ __global__ void k_sub3(int n, double *z, const double *f, const double *a, const
 
 __global__ void k_d2f(int n, float *dst, const double *src)
 {
+	pdl_begin();
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i < n)
 		dst[i] = (float)src[i];
@@ -599,6 +685,7 @@ __global__ void k_d2f(int n, float *dst, const double *src)
 
 __global__ void k_add_f2d(int n, double *dst, const float *src)
 {
+	pdl_begin();
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i < n)
 		dst[i] += (double)src[i];
@@ -608,22 +695,18 @@ __global__ void k_add_f2d(int n, double *dst, const float *src)
 __global__ void k_residual64(Lvl L, const double *__restrict__ K, const double *__restrict__ f, const double *__restrict__ u,
                              double *__restrict__ r, Red red, double *out)
 {
+	pdl_begin();
 	double v[1] = {0.0};
-	for(int p = blockIdx.x * blockDim.x + threadIdx.x; p < L.nno; p += gridDim.x * blockDim.x)
+	for(int t = blockIdx.x * blockDim.x + threadIdx.x; t < 3 * L.nno; t += gridDim.x * blockDim.x)
 	{
+		const int p = t / 3, i = t - 3 * p;
 		const int c = colour_of_pos(L, p);
 		int x, y, z;
 		cg_decode(L, c, p - L.coff[c], x, y, z);
 		const int n = cg_node(L, x, y, z);
-		double r0, r1, r2;
-		row_product(L, K, u, p, x, y, z, r0, r1, r2);
-		r0 = f[3 * n] - r0;
-		r1 = f[3 * n + 1] - r1;
-		r2 = f[3 * n + 2] - r2;
-		r[3 * n] = r0;
-		r[3 * n + 1] = r1;
-		r[3 * n + 2] = r2;
-		v[0] += r0 * r0 + r1 * r1 + r2 * r2;
+		const double ri = f[3 * n + i] - row_dot<double, true>(L, K, u, p, i, x, y, z);
+		r[3 * n + i] = ri;
+		v[0] += ri * ri;
 	}
 	block_reduce_store<1>(v, red, out);
 }
@@ -635,6 +718,7 @@ __global__ void k_residual64(Lvl L, const double *__restrict__ K, const double *
 // centroid (construct_mat_group, Construct_arrays.c:742-800)
 __global__ void k_visc_from_T(Lvl L, const Geo *__restrict__ geo, Rheo r, const double *__restrict__ T, double *__restrict__ evi)
 {
+	pdl_begin();
 	const int e = blockIdx.x * blockDim.x + threadIdx.x;
 	if(e >= L.nel)
 		return;
@@ -682,6 +766,7 @@ __global__ void k_visc_from_T(Lvl L, const Geo *__restrict__ geo, Rheo r, const 
 // visc_from_gint_to_nodes (Nodal_mesh.c:583-615)
 __global__ void k_visc_to_nodes(Lvl L, const double *__restrict__ evi, double *__restrict__ VN)
 {
+	pdl_begin();
 	const int n = blockIdx.x * blockDim.x + threadIdx.x;
 	if(n >= L.nno)
 		return;
@@ -706,6 +791,7 @@ __global__ void k_visc_to_nodes(Lvl L, const double *__restrict__ evi, double *_
 // project_scalar (Solver_multigrid.c:338-394)
 __global__ void k_project_scalar(Lvl Lf, Lvl Lc, const double *__restrict__ VN, double *__restrict__ VD)
 {
+	pdl_begin();
 	const int N = blockIdx.x * blockDim.x + threadIdx.x;
 	if(N >= Lc.nno)
 		return;
@@ -730,6 +816,7 @@ __global__ void k_project_scalar(Lvl Lf, Lvl Lc, const double *__restrict__ VN, 
 // visc_from_nodes_to_gint (Nodal_mesh.c:617-640)
 __global__ void k_visc_to_gint(Lvl L, const Geo *__restrict__ geo, const double *__restrict__ VN, double *__restrict__ evi)
 {
+	pdl_begin();
 	const int e = blockIdx.x * blockDim.x + threadIdx.x;
 	if(e >= L.nel)
 		return;
@@ -754,6 +841,7 @@ __global__ void k_visc_to_gint(Lvl L, const Geo *__restrict__ geo, const double 
 // return_horiz_ave (Global_operations.c:133-251) of Ra*T, one block per z layer
 __global__ void k_horiz_ave(Lvl L, double Ra, const double *__restrict__ T, double *__restrict__ H)
 {
+	pdl_begin();
 	const int z = blockIdx.x;
 	__shared__ double sh[2][TPB / 32];
 	double s = 0.0, w = 0.0;
@@ -791,6 +879,7 @@ __global__ void k_horiz_ave(Lvl L, double Ra, const double *__restrict__ T, doub
 // thermal_buoyancy (Pan_problem_misc_functions.c:83-156): Ra*T minus the layer mean
 __global__ void k_buoyancy(Lvl L, double Ra, const double *__restrict__ T, const double *__restrict__ H, double *__restrict__ b)
 {
+	pdl_begin();
 	const int n = blockIdx.x * blockDim.x + threadIdx.x;
 	if(n < L.nno)
 		b[n] = Ra * T[n] - H[n % L.noz];
@@ -799,6 +888,7 @@ __global__ void k_buoyancy(Lvl L, double Ra, const double *__restrict__ T, const
 // assemble_forces + get_elt_f (Element_calculations.c:74-125, 989-1075), node-centred, stripped
 __global__ void k_forces(Lvl L, const Geo *__restrict__ geo, const double *__restrict__ buoy, double *__restrict__ F)
 {
+	pdl_begin();
 	const int n = blockIdx.x * blockDim.x + threadIdx.x;
 	if(n >= L.nno)
 		return;
@@ -831,6 +921,7 @@ __global__ void k_forces(Lvl L, const Geo *__restrict__ geo, const double *__res
 // v_from_vector (Stokes_flow_Incomp.c:530-553): V[d*nno + n]; constrained dofs take VB = 0
 __global__ void k_v_from_vector(Lvl L, const double *__restrict__ U, double *__restrict__ V)
 {
+	pdl_begin();
 	const int n = blockIdx.x * blockDim.x + threadIdx.x;
 	if(n >= L.nno)
 		return;
@@ -849,6 +940,7 @@ __device__ __forceinline__ bool t_dirichlet(const Lvl &L, int n) { int z = n % L
 __global__ void k_pg_residual(Lvl L, const Geo *__restrict__ geo, const double *__restrict__ T, const double *__restrict__ Tdot,
                               const double *__restrict__ V, double Q0, double *__restrict__ Eres)
 {
+	pdl_begin();
 	const int e = blockIdx.x * blockDim.x + threadIdx.x;
 	if(e >= L.nel)
 		return;
@@ -917,6 +1009,7 @@ __global__ void k_pg_residual(Lvl L, const Geo *__restrict__ geo, const double *
 // DTdot = (sum of element residuals at the node) / lumped mass
 __global__ void k_pg_gather(Lvl L, const double *__restrict__ Eres, double *__restrict__ DTdot)
 {
+	pdl_begin();
 	const int n = blockIdx.x * blockDim.x + threadIdx.x;
 	if(n >= L.nno)
 		return;
@@ -937,6 +1030,7 @@ __global__ void k_pg_gather(Lvl L, const double *__restrict__ Eres, double *__re
 // predictor (Advection_diffusion.c:352-367)
 __global__ void k_predictor(Lvl L, double *T, double *Tdot, double dt, double gamma)
 {
+	pdl_begin();
 	const int n = blockIdx.x * blockDim.x + threadIdx.x;
 	if(n >= L.nno)
 		return;
@@ -948,6 +1042,7 @@ __global__ void k_predictor(Lvl L, double *T, double *Tdot, double dt, double ga
 // corrector (Advection_diffusion.c:369-386)
 __global__ void k_corrector(Lvl L, double *T, double *Tdot, const double *DTdot, double dt, double gamma)
 {
+	pdl_begin();
 	const int n = blockIdx.x * blockDim.x + threadIdx.x;
 	if(n >= L.nno)
 		return;
@@ -959,6 +1054,7 @@ __global__ void k_corrector(Lvl L, double *T, double *Tdot, const double *DTdot,
 // temperatures_conform_bcs (Boundary_conditions.c:949-991): T = 1 at the bottom, 0 at the top
 __global__ void k_conform_T(Lvl L, double *T)
 {
+	pdl_begin();
 	const int n = blockIdx.x * blockDim.x + threadIdx.x;
 	if(n >= L.nno)
 		return;
@@ -972,6 +1068,7 @@ __global__ void k_conform_T(Lvl L, double *T)
 // max (Tmax, Global_operations.c:394-407) reported through the sum machinery as -min(-x)
 __global__ void k_max(int n, const double *__restrict__ T, Red red, double *out)
 {
+	pdl_begin();
 	__shared__ double sh[RED_THREADS / 32];
 	__shared__ bool last;
 	double m = -10.0;
@@ -1006,6 +1103,7 @@ __global__ void k_max(int n, const double *__restrict__ T, Red red, double *out)
 // advective part of std_timestep (Advection_diffusion.c:737-810): min over elements of 0.5/uc
 __global__ void k_adv_step(Lvl L, const double *__restrict__ V, Red red, double *out)
 {
+	pdl_begin();
 	__shared__ double sh[RED_THREADS / 32];
 	__shared__ bool last;
 	double m = 1.0e8;
@@ -1054,6 +1152,7 @@ __global__ void k_adv_step(Lvl L, const double *__restrict__ V, Red red, double 
 __global__ void k_hf_elem(Lvl L, const Geo *__restrict__ geo, const double *__restrict__ T, const double *__restrict__ V,
                           double *__restrict__ uTe)
 {
+	pdl_begin();
 	const int e = blockIdx.x * blockDim.x + threadIdx.x;
 	if(e >= L.nel)
 		return;
@@ -1083,6 +1182,7 @@ __global__ void k_hf_elem(Lvl L, const Geo *__restrict__ geo, const double *__re
 // step 2: nodal flux = TWW-weighted element means / lumped mass
 __global__ void k_hf_node(Lvl L, const double *__restrict__ uTe, double *__restrict__ hf)
 {
+	pdl_begin();
 	const int n = blockIdx.x * blockDim.x + threadIdx.x;
 	if(n >= L.nno)
 		return;
@@ -1103,6 +1203,7 @@ __global__ void k_hf_node(Lvl L, const double *__restrict__ uTe, double *__restr
 // step 3: surface extrapolation 2 hf[s] - hf[s-1] and the element-area means; out = (Nut, Nub)
 __global__ void k_hf_surface(Lvl L, const double *__restrict__ hf, Red red, double *out)
 {
+	pdl_begin();
 	double v[2] = {0.0, 0.0};
 	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < L.elx * L.ely; i += gridDim.x * blockDim.x)
 	{
@@ -1123,6 +1224,7 @@ __global__ void k_hf_surface(Lvl L, const double *__restrict__ hf, Red red, doub
 
 __global__ void k_vrms(Lvl L, const Geo *__restrict__ geo, const double *__restrict__ V, Red red, double *out)
 {
+	pdl_begin();
 	double v[1] = {0.0};
 	for(int e = blockIdx.x * blockDim.x + threadIdx.x; e < L.nel; e += gridDim.x * blockDim.x)
 	{
@@ -1154,6 +1256,40 @@ __global__ void k_vrms(Lvl L, const Geo *__restrict__ geo, const double *__restr
 // ====================================================================== host
 
 unsigned long long g_kernel_launches = 0;
+
+template <typename... KArgs, typename... Args>
+static void launch_k_smem(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args... args)
+{
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim = grid;
+	cfg.blockDim = block;
+	cfg.dynamicSmemBytes = smem;
+	cfg.stream = st;
+	cudaLaunchAttribute attr[1];
+	attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+	attr[0].val.programmaticStreamSerializationAllowed = 1;
+	cfg.attrs = attr;
+	cfg.numAttrs = 1;
+	cudaLaunchKernelEx(&cfg, kern, ((KArgs)args)...);
+	++g_kernel_launches;
+}
+
+template <typename... KArgs, typename... Args>
+static void launch_k(void (*kern)(KArgs...), dim3 grid, dim3 block, cudaStream_t st, Args... args)
+{
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim = grid;
+	cfg.blockDim = block;
+	cfg.dynamicSmemBytes = 0;
+	cfg.stream = st;
+	cudaLaunchAttribute attr[1];
+	attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+	attr[0].val.programmaticStreamSerializationAllowed = 1;
+	cfg.attrs = attr;
+	cfg.numAttrs = 1;
+	cudaLaunchKernelEx(&cfg, kern, ((KArgs)args)...);
+	++g_kernel_launches;
+}
 
 void geo_fill_host(const Lvl &L, Geo *g)
 {
@@ -1203,14 +1339,12 @@ void geo_fill_host(const Lvl &L, Geo *g)
 void launch_assemble(cudaStream_t st, const Lvl &L, const Geo *geo, const double *evi, int aug, double lambda, double *K64,
                      float *K32, double *BI64, float *BI32)
 {
-	k_assemble<<<nblocks(L.nno, 128), 128, 0, st>>>(L, geo, evi, aug, lambda, K64, K32, BI64, BI32);
-	++g_kernel_launches;
+	launch_k(k_assemble, nblocks(L.nno, 128), 128, st, L, geo, evi, aug, lambda, K64, K32, BI64, BI32);
 }
 
 void launch_bpi(cudaStream_t st, const Lvl &L, const Geo *geo, const double *BI64, double *BPI, int precond)
 {
-	k_bpi<<<nblocks(L.nel), TPB, 0, st>>>(L, geo, BI64, BPI, precond);
-	++g_kernel_launches;
+	launch_k(k_bpi, nblocks(L.nel), TPB, st, L, geo, BI64, BPI, precond);
 }
 
 static int max_colour(const Lvl &L)
@@ -1223,23 +1357,20 @@ static int max_colour(const Lvl &L)
 
 template <typename T> void launch_kmul(cudaStream_t st, const Lvl &L, const T *K, const T *u, T *Au)
 {
-	dim3 grid(nblocks(max_colour(L)), 8);
-	k_kmul<T, 0><<<grid, TPB, 0, st>>>(L, K, u, (const T *)nullptr, Au);
-	++g_kernel_launches;
+	dim3 grid(nblocks(3 * (long)max_colour(L), TPB3), 8);
+	launch_k(k_kmul<T, 0>, grid, TPB3, st, L, K, u, (const T *)nullptr, Au);
 }
 
 template <typename T> void launch_residual(cudaStream_t st, const Lvl &L, const T *K, const T *f, const T *u, T *r)
 {
-	dim3 grid(nblocks(max_colour(L)), 8);
-	k_kmul<T, 1><<<grid, TPB, 0, st>>>(L, K, u, f, r);
-	++g_kernel_launches;
+	dim3 grid(nblocks(3 * (long)max_colour(L), TPB3), 8);
+	launch_k(k_kmul<T, 1>, grid, TPB3, st, L, K, u, f, r);
 }
 
 template <typename T>
 void launch_kmul_linesearch(cudaStream_t st, const Lvl &L, const T *K, const T *u, const T *res, T *Au, Red red, double *out2)
 {
-	k_kmul_ls<T><<<red_grid(L.nno), RED_THREADS, 0, st>>>(L, K, u, res, Au, red, out2);
-	++g_kernel_launches;
+	launch_k(k_kmul_ls<T>, red_grid(3 * (long)L.nno), RED_THREADS, st, L, K, u, res, Au, red, out2);
 }
 
 template <typename T> void launch_gs_colour(cudaStream_t st, const Lvl &L, const T *K, const T *BI, const T *F, T *d, int c)
@@ -1247,37 +1378,50 @@ template <typename T> void launch_gs_colour(cudaStream_t st, const Lvl &L, const
 	const int n = L.coff[c + 1] - L.coff[c];
 	if(n > 0)
 	{
-		k_gs_colour<T><<<nblocks(n), TPB, 0, st>>>(L, K, BI, F, d, c);
-		++g_kernel_launches;
+		launch_k(k_gs_colour<T>, nblocks(3 * (long)n, TPB3), TPB3, st, L, K, BI, F, d, c);
 	}
 }
 
-bool gs_small_fits(const Lvl &L) { return L.nno <= 4 * GS_SMALL_THREADS; }
+bool gs_small_fits(const Lvl &L) { return 3 * L.nno <= 4 * GS_SMALL_THREADS; }
+
+int kernels_init()
+{
+	// opt in to large dynamic shared memory once, outside any stream capture
+	cudaError_t a = cudaFuncSetAttribute(k_gs_small_smem<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+	cudaError_t b = cudaFuncSetAttribute(k_gs_small_smem<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+	return (a == cudaSuccess && b == cudaSuccess) ? 0 : -1;
+}
+
+static size_t gs_smem_bytes(const Lvl &L, size_t word) { return word * ((size_t)246 * L.npad + 2 * (size_t)L.neq); }
+
+constexpr size_t GS_SMEM_LIMIT = 200 * 1024;
 
 template <typename T>
 void launch_gs_small(cudaStream_t st, const Lvl &L, const T *K, const T *BI, const T *F, T *d, int cycles, int zero_start)
 {
-	k_gs_small<T><<<1, GS_SMALL_THREADS, 0, st>>>(L, K, BI, F, d, cycles, zero_start);
-	++g_kernel_launches;
+	const size_t bytes = gs_smem_bytes(L, sizeof(T));
+	if(bytes <= GS_SMEM_LIMIT)
+	{
+		launch_k_smem(k_gs_small_smem<T>, dim3(1), dim3(GS_SMALL_THREADS), bytes, st, L, K, BI, F, d, cycles, zero_start);
+		return;
+	}
+	launch_k(k_gs_small<T>, 1, GS_SMALL_THREADS, st, L, K, BI, F, d, cycles, zero_start);
 }
 
 template <typename T> void launch_project(cudaStream_t st, const Lvl &Lf, const Lvl &Lc, const T *AU, T *AD)
 {
-	k_project<T><<<nblocks(Lc.nno), TPB, 0, st>>>(Lf, Lc, AU, AD);
-	++g_kernel_launches;
+	launch_k(k_project<T>, nblocks(Lc.nno), TPB, st, Lf, Lc, AU, AD);
 }
 
 template <typename T> void launch_interp(cudaStream_t st, const Lvl &Lc, const Lvl &Lf, const T *AD, T *AU)
 {
-	k_interp<T><<<nblocks(Lf.nno), TPB, 0, st>>>(Lc, Lf, AD, AU);
-	++g_kernel_launches;
+	launch_k(k_interp<T>, nblocks(Lf.nno), TPB, st, Lc, Lf, AD, AU);
 }
 
 template <typename T>
 void launch_vel_update(cudaStream_t st, int n, T *vel, const T *del, T *res, const T *AU, const double *nd, int update_res)
 {
-	k_vel_update<T><<<nblocks(n), TPB, 0, st>>>(n, vel, del, res, AU, nd, update_res);
-	++g_kernel_launches;
+	launch_k(k_vel_update<T>, nblocks(n), TPB, st, n, vel, del, res, AU, nd, update_res);
 }
 
 #define INST(T)                                                                                                              \
@@ -1295,152 +1439,126 @@ INST(float)
 
 void launch_div(cudaStream_t st, const Lvl &L, const Geo *geo, const double *U, double *divU)
 {
-	k_div<<<nblocks(L.nel), TPB, 0, st>>>(L, geo, U, divU);
-	++g_kernel_launches;
+	launch_k(k_div, nblocks(L.nel), TPB, st, L, geo, U, divU);
 }
 
 void launch_grad(cudaStream_t st, const Lvl &L, const Geo *geo, const double *P, double *gradP)
 {
-	k_grad<<<nblocks(L.nno), TPB, 0, st>>>(L, geo, P, gradP);
-	++g_kernel_launches;
+	launch_k(k_grad, nblocks(L.nno), TPB, st, L, geo, P, gradP);
 }
 
-void launch_strip(cudaStream_t st, const Lvl &L, double *r) { k_strip<<<nblocks(L.nno), TPB, 0, st>>>(L, r); }
+void launch_strip(cudaStream_t st, const Lvl &L, double *r) { launch_k(k_strip, nblocks(L.nno), TPB, st, L, r); }
 
 void launch_dot(cudaStream_t st, int n, const double *a, const double *b, Red red, double *out)
 {
-	k_dot<<<red_grid(n), RED_THREADS, 0, st>>>(n, a, b, red, out);
-	++g_kernel_launches;
+	launch_k(k_dot, red_grid(n), RED_THREADS, st, n, a, b, red, out);
 }
 
 void launch_dots4(cudaStream_t st, int n, const double *a0, const double *b0, const double *a1, const double *b1, const double *a2,
                   const double *b2, const double *a3, const double *b3, Red red, double *out)
 {
-	k_dots4<<<red_grid(n), RED_THREADS, 0, st>>>(n, a0, b0, a1, b1, a2, b2, a3, b3, red, out);
-	++g_kernel_launches;
+	launch_k(k_dots4, red_grid(n), RED_THREADS, st, n, a0, b0, a1, b1, a2, b2, a3, b3, red, out);
 }
 
 void launch_axpby(cudaStream_t st, int n, double *y, double a, const double *x, double b)
 {
-	k_axpby<<<nblocks(n), TPB, 0, st>>>(n, y, a, x, b);
-	++g_kernel_launches;
+	launch_k(k_axpby, nblocks(n), TPB, st, n, y, a, x, b);
 }
 
-void launch_mul(cudaStream_t st, int n, double *z, const double *a, const double *b) { k_mul<<<nblocks(n), TPB, 0, st>>>(n, z, a, b); }
+void launch_mul(cudaStream_t st, int n, double *z, const double *a, const double *b) { launch_k(k_mul, nblocks(n), TPB, st, n, z, a, b); }
 
 void launch_lin2(cudaStream_t st, int n, double *z, double a, const double *x, double b, const double *y)
 {
-	k_lin2<<<nblocks(n), TPB, 0, st>>>(n, z, a, x, b, y);
-	++g_kernel_launches;
+	launch_k(k_lin2, nblocks(n), TPB, st, n, z, a, x, b, y);
 }
 
 void launch_sub3(cudaStream_t st, int n, double *z, const double *f, const double *a, const double *b)
 {
-	k_sub3<<<nblocks(n), TPB, 0, st>>>(n, z, f, a, b);
-	++g_kernel_launches;
+	launch_k(k_sub3, nblocks(n), TPB, st, n, z, f, a, b);
 }
 
-void launch_copy_d2f(cudaStream_t st, int n, float *dst, const double *src) { k_d2f<<<nblocks(n), TPB, 0, st>>>(n, dst, src); }
+void launch_copy_d2f(cudaStream_t st, int n, float *dst, const double *src) { launch_k(k_d2f, nblocks(n), TPB, st, n, dst, src); }
 
-void launch_add_f2d(cudaStream_t st, int n, double *dst, const float *src) { k_add_f2d<<<nblocks(n), TPB, 0, st>>>(n, dst, src); }
+void launch_add_f2d(cudaStream_t st, int n, double *dst, const float *src) { launch_k(k_add_f2d, nblocks(n), TPB, st, n, dst, src); }
 
 void launch_residual64(cudaStream_t st, const Lvl &L, const double *K, const double *f, const double *u, double *r, Red red, double *out)
 {
-	k_residual64<<<red_grid(L.nno), RED_THREADS, 0, st>>>(L, K, f, u, r, red, out);
-	++g_kernel_launches;
+	launch_k(k_residual64, red_grid(3 * (long)L.nno), RED_THREADS, st, L, K, f, u, r, red, out);
 }
 
 void launch_visc_from_T(cudaStream_t st, const Lvl &L, const Geo *geo, const Rheo &r, const double *T, double *evi)
 {
-	k_visc_from_T<<<nblocks(L.nel), TPB, 0, st>>>(L, geo, r, T, evi);
-	++g_kernel_launches;
+	launch_k(k_visc_from_T, nblocks(L.nel), TPB, st, L, geo, r, T, evi);
 }
 
 void launch_project_viscosity(cudaStream_t st, const Lvl &Lf, const Lvl &Lc, const Geo *geoc, const double *evi_f, double *evi_c,
                               double *work_f, double *work_c)
 {
-	k_visc_to_nodes<<<nblocks(Lf.nno), TPB, 0, st>>>(Lf, evi_f, work_f);
-	++g_kernel_launches;
-	k_project_scalar<<<nblocks(Lc.nno), TPB, 0, st>>>(Lf, Lc, work_f, work_c);
-	++g_kernel_launches;
-	k_visc_to_gint<<<nblocks(Lc.nel), TPB, 0, st>>>(Lc, geoc, work_c, evi_c);
-	++g_kernel_launches;
+	launch_k(k_visc_to_nodes, nblocks(Lf.nno), TPB, st, Lf, evi_f, work_f);
+	launch_k(k_project_scalar, nblocks(Lc.nno), TPB, st, Lf, Lc, work_f, work_c);
+	launch_k(k_visc_to_gint, nblocks(Lc.nel), TPB, st, Lc, geoc, work_c, evi_c);
 }
 
 void launch_buoyancy(cudaStream_t st, const Lvl &L, double Ra, const double *T, double *buoy)
 {
 	// the layer means go into the tail of `buoy`'s companion buffer: buoy + nno (caller sizes it nno + noz)
 	double *H = buoy + L.nno;
-	k_horiz_ave<<<L.noz, TPB, 0, st>>>(L, Ra, T, H);
-	++g_kernel_launches;
-	k_buoyancy<<<nblocks(L.nno), TPB, 0, st>>>(L, Ra, T, H, buoy);
-	++g_kernel_launches;
+	launch_k(k_horiz_ave, L.noz, TPB, st, L, Ra, T, H);
+	launch_k(k_buoyancy, nblocks(L.nno), TPB, st, L, Ra, T, H, buoy);
 }
 
 void launch_forces(cudaStream_t st, const Lvl &L, const Geo *geo, const double *buoy, double *F)
 {
-	k_forces<<<nblocks(L.nno), TPB, 0, st>>>(L, geo, buoy, F);
-	++g_kernel_launches;
+	launch_k(k_forces, nblocks(L.nno), TPB, st, L, geo, buoy, F);
 }
 
 void launch_v_from_vector(cudaStream_t st, const Lvl &L, const double *U, double *V)
 {
-	k_v_from_vector<<<nblocks(L.nno), TPB, 0, st>>>(L, U, V);
-	++g_kernel_launches;
+	launch_k(k_v_from_vector, nblocks(L.nno), TPB, st, L, U, V);
 }
 
 void launch_pg_residual(cudaStream_t st, const Lvl &L, const Geo *geo, const double *T, const double *Tdot, const double *V, double Q0,
                         double *Eres)
 {
-	k_pg_residual<<<nblocks(L.nel, 128), 128, 0, st>>>(L, geo, T, Tdot, V, Q0, Eres);
-	++g_kernel_launches;
+	launch_k(k_pg_residual, nblocks(L.nel, 128), 128, st, L, geo, T, Tdot, V, Q0, Eres);
 }
 
 void launch_pg_gather(cudaStream_t st, const Lvl &L, const double *Eres, double *DTdot)
 {
-	k_pg_gather<<<nblocks(L.nno), TPB, 0, st>>>(L, Eres, DTdot);
-	++g_kernel_launches;
+	launch_k(k_pg_gather, nblocks(L.nno), TPB, st, L, Eres, DTdot);
 }
 
 void launch_predictor(cudaStream_t st, const Lvl &L, double *T, double *Tdot, double dt, double gamma)
 {
-	k_predictor<<<nblocks(L.nno), TPB, 0, st>>>(L, T, Tdot, dt, gamma);
-	++g_kernel_launches;
+	launch_k(k_predictor, nblocks(L.nno), TPB, st, L, T, Tdot, dt, gamma);
 }
 
 void launch_corrector(cudaStream_t st, const Lvl &L, double *T, double *Tdot, const double *DTdot, double dt, double gamma)
 {
-	k_corrector<<<nblocks(L.nno), TPB, 0, st>>>(L, T, Tdot, DTdot, dt, gamma);
-	++g_kernel_launches;
+	launch_k(k_corrector, nblocks(L.nno), TPB, st, L, T, Tdot, DTdot, dt, gamma);
 }
 
 void launch_tmax(cudaStream_t st, int n, const double *T, Red red, double *out)
 {
-	k_max<<<red_grid(n), RED_THREADS, 0, st>>>(n, T, red, out);
-	++g_kernel_launches;
+	launch_k(k_max, red_grid(n), RED_THREADS, st, n, T, red, out);
 }
 
 void launch_adv_timestep(cudaStream_t st, const Lvl &L, const double *V, Red red, double *out)
 {
-	k_adv_step<<<red_grid(L.nel), RED_THREADS, 0, st>>>(L, V, red, out);
-	++g_kernel_launches;
+	launch_k(k_adv_step, red_grid(L.nel), RED_THREADS, st, L, V, red, out);
 }
 
-void launch_conform_T(cudaStream_t st, const Lvl &L, double *T) { k_conform_T<<<nblocks(L.nno), TPB, 0, st>>>(L, T); }
+void launch_conform_T(cudaStream_t st, const Lvl &L, double *T) { launch_k(k_conform_T, nblocks(L.nno), TPB, st, L, T); }
 
 void launch_heat_flux(cudaStream_t st, const Lvl &L, const Geo *geo, const double *T, const double *V, double *work, Red red, double *out)
 {
 	// work holds nel element means then nno nodal fluxes
-	k_hf_elem<<<nblocks(L.nel), TPB, 0, st>>>(L, geo, T, V, work);
-	++g_kernel_launches;
-	k_hf_node<<<nblocks(L.nno), TPB, 0, st>>>(L, work, work + L.nel);
-	++g_kernel_launches;
-	k_hf_surface<<<red_grid((long)L.elx * L.ely), RED_THREADS, 0, st>>>(L, work + L.nel, red, out);
-	++g_kernel_launches;
+	launch_k(k_hf_elem, nblocks(L.nel), TPB, st, L, geo, T, V, work);
+	launch_k(k_hf_node, nblocks(L.nno), TPB, st, L, work, work + L.nel);
+	launch_k(k_hf_surface, red_grid((long)L.elx * L.ely), RED_THREADS, st, L, work + L.nel, red, out);
 }
 
 void launch_vrms(cudaStream_t st, const Lvl &L, const Geo *geo, const double *V, Red red, double *out)
 {
-	k_vrms<<<red_grid(L.nel), RED_THREADS, 0, st>>>(L, geo, V, red, out);
-	++g_kernel_launches;
+	launch_k(k_vrms, red_grid(L.nel), RED_THREADS, st, L, geo, V, red, out);
 }

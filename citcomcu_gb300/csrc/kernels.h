@@ -31,6 +31,9 @@ void geo_fill_host(const Lvl &L, Geo *g);
 // capture counts its kernels once, each replay is added by the driver)
 extern unsigned long long g_kernel_launches;
 
+// one-time function attributes (large dynamic shared memory); 0 on success
+int kernels_init();
+
 // set-up
 void launch_assemble(cudaStream_t st, const Lvl &L, const Geo *geo, const double *evi, int aug, double lambda,
                      double *K64, float *K32, double *BI64, float *BI32);

@@ -9,6 +9,8 @@
 // of every coefficient array.
 #pragma once
 
+#include <stddef.h>
+
 #define CITCOM_MAX_LEVELS 12
 
 struct Lvl
@@ -63,6 +65,15 @@ CG_HD int cg_loc(int a, int d)
 {
 	// a: 0 (0,0,0) 1 (1,0,0) 2 (1,1,0) 3 (0,1,0) 4 (0,0,1) 5 (1,0,1) 6 (1,1,1) 7 (0,1,1)
 	return d == 0 ? (((a & 3) == 1) || ((a & 3) == 2)) : d == 1 ? ((a & 3) >= 2) : (a >= 4);
+}
+
+// stencil coefficient (neighbour slot s = (dz+1) + 3(dx+1) + 9(dy+1), row i,
+// column j) of the node at colour-major position p: 81 arrays of 3*npad
+// words; the three rows of a node are adjacent, so the three threads that own
+// a node's rows read consecutive words
+CG_HD size_t cg_kidx(const Lvl &L, int s, int i, int j, int p)
+{
+	return (size_t)(3 * s + j) * 3 * (size_t)L.npad + 3 * (size_t)p + i;
 }
 
 CG_HD int cg_local_index(int ox, int oy, int oz)

@@ -18,7 +18,9 @@
  * Every function returns CITCOM_GPU_OK (0) or a negative error code; the
  * message is available from citcom_gpu_error_string().  Setting the
  * environment variable CITCOM_GPU_VERBOSE=1 prints one line per Uzawa
- * iteration in the spirit of the reference's generate_log_message.  There is no CPU
+ * iteration in the spirit of the reference's generate_log_message;
+ * CITCOM_GPU_NO_GRAPH=1 launches the multigrid pass kernel by kernel instead
+ * of replaying it as a CUDA graph (for kernel profilers).  There is no CPU
  * fallback: without a usable CUDA device citcom_gpu_create fails.
  *
  * Scope: Cartesian box, uniform spacing per axis on every multigrid level,
