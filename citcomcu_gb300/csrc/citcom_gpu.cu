@@ -30,6 +30,7 @@ enum Slot
 	S_VRMS = 18,
 	S_MIN = 20,
 	S_MAX = 21,
+	S_UZ = 22,    // Uzawa scalars: r1.z1, r0.z0, s2.Ahat, alpha, error flag
 	S_COUNT = 32
 };
 
@@ -188,13 +189,20 @@ template <typename T> void gs_inner(citcom_gpu *h, MG<T> &B, int lev, T *d, cons
 template <typename T> void gs(citcom_gpu *h, MG<T> &B, int lev, T *d, const T *F, int cycles, int zero_start)
 {
 	const bool timed = (lev == h->L - 1) && h->n_gs_pairs < 4 && !gs_small_fits(h->lv[lev]);
-	// external records become event-record nodes of the captured graph
+	// during stream capture, external records become event-record nodes of
+	// the graph; outside capture they are ordinary records
+	unsigned flags = 0;
 	if(timed)
-		cudaEventRecordWithFlags(h->ev_gs[2 * h->n_gs_pairs], h->st, cudaEventRecordExternal);
+	{
+		cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+		cudaStreamIsCapturing(h->st, &cs);
+		flags = (cs == cudaStreamCaptureStatusActive) ? cudaEventRecordExternal : 0u;
+		cudaEventRecordWithFlags(h->ev_gs[2 * h->n_gs_pairs], h->st, flags);
+	}
 	gs_inner<T>(h, B, lev, d, F, cycles, zero_start);
 	if(timed)
 	{
-		cudaEventRecordWithFlags(h->ev_gs[2 * h->n_gs_pairs + 1], h->st, cudaEventRecordExternal);
+		cudaEventRecordWithFlags(h->ev_gs[2 * h->n_gs_pairs + 1], h->st, flags);
 		h->n_gs_pairs++;
 	}
 }
@@ -386,35 +394,27 @@ int uzawa(citcom_gpu *h, double *V, double *P, const double *F, double imp, int 
 	const double residual = std::sqrt(h->hscal[S_R0] / npno);
 
 	int count = 0;
-	double dpressure = 1.0, dvelocity = 1.0, r1dotz1, r0dotz0 = 0.0;
+	double dpressure = 1.0, dvelocity = 1.0;
+	double *sc = h->dscal + S_UZ;
+	CK(cudaMemsetAsync(sc, 0, 5 * sizeof(double), st));
 	while(count < *steps_max && (dpressure >= imp || dvelocity >= imp))
 	{
-		launch_mul(st, npno, z1, h->BPI, r1);
-		launch_dots4(st, npno, r1, z1, count ? r0 : nullptr, z0, nullptr, nullptr, nullptr, nullptr, red_of(h), h->dscal + S_DOT);
-		TRY(readback(h, S_DOT, 2));
-		r1dotz1 = h->hscal[S_DOT];
-		if(count == 0)
-			CK(cudaMemcpyAsync(s2, z1, sizeof(double) * npno, cudaMemcpyDeviceToDevice, st));
-		else
-		{
-			r0dotz0 = h->hscal[S_DOT + 1];
-			if(r0dotz0 == 0.0)
-				return fail(h, CITCOM_GPU_ERR_NOCONV, "solve_Ahat_p_fhat: division by zero in head of incompressibility iteration");
-			launch_lin2(st, npno, s2, 1.0, z1, r1dotz1 / r0dotz0, s1);
-		}
+		// z1 = BPI r1, r1.z1, search direction s2 (scalars stay on the device)
+		launch_uzawa_precond(st, npno, h->BPI, r1, z1, red_of(h), sc);
+		launch_uzawa_search(st, npno, s2, z1, s1, sc, count == 0);
 		launch_grad(st, Lf, geo, s2, Ah);
 		TRY(solve_del2_u(h, imp * v_res, &valid));
 		launch_strip(st, Lf, u1);
 		launch_div(st, Lf, geo, u1, Ah);
-		launch_dot(st, npno, s2, Ah, red_of(h), h->dscal + S_R0);
-		TRY(readback(h, S_R0, 1));
-		const double alpha = valid ? r1dotz1 / h->hscal[S_R0] : 0.0;
-		launch_lin2(st, npno, r2, 1.0, r1, -alpha, Ah);
-		launch_axpby(st, npno, P, 1.0, s2, alpha);
-		launch_axpby(st, neq, V, 1.0, u1, -alpha);
+		launch_dot(st, npno, s2, Ah, red_of(h), sc + 2);
+		launch_uzawa_update(st, npno, neq, r2, r1, Ah, P, s2, V, u1, sc, valid);
 		launch_dots4(st, neq, V, V, u1, u1, nullptr, nullptr, nullptr, nullptr, red_of(h), h->dscal + S_DOT);
 		launch_dots4(st, npno, P, P, s2, s2, nullptr, nullptr, nullptr, nullptr, red_of(h), h->dscal + S_DOT + 4);
-		TRY(readback(h, S_DOT, 8));
+		CK(cudaMemcpyAsync(h->hscal + S_DOT, h->dscal + S_DOT, 8 * sizeof(double), cudaMemcpyDeviceToHost, st));
+		TRY(readback(h, S_UZ, 5));
+		if(h->hscal[S_UZ + 4] != 0.0)
+			return fail(h, CITCOM_GPU_ERR_NOCONV, "solve_Ahat_p_fhat: division by zero in head of incompressibility iteration");
+		const double alpha = h->hscal[S_UZ + 3];
 		const double vdotv = h->hscal[S_DOT], u1u1 = h->hscal[S_DOT + 1];
 		const double pdotp = h->hscal[S_DOT + 4], s2s2 = h->hscal[S_DOT + 5];
 		dpressure = alpha * std::sqrt(s2s2 / (1.0e-32 + pdotp));

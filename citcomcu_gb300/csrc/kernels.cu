@@ -263,81 +263,120 @@ __global__ void k_bpi(Lvl L, const Geo *__restrict__ geo, const double *__restri
 
 // ---------------------------------------------------------------- stencil
 
-// Row i of node (x,y,z) at colour-major position p: sum over the 27
-// neighbours m of K_{n,m}[i][:] . u_m.  Three threads share a node (one per
-// row), which triples the memory-level parallelism of the gather.
-// Neighbours outside the mesh are clamped onto it; their coefficients are
-// zero.  `u` is deliberately not __restrict__: the single-CTA smoothers read
-// values that other threads of the block wrote in the previous colour.
-template <typename T, bool STREAM>
-__device__ __forceinline__ T row_dot(const Lvl &L, const T *K, const T *u, int p, int i, int x, int y, int z)
+// Stencil products are computed by one thread per (node, neighbour slot): a
+// block holds NB = 32 nodes x 27 slots; warp w of the block is slot w for 32
+// consecutive nodes of one colour.  Each thread issues its 9 coefficient loads
+// and 3 neighbour loads at once (memory-level parallelism instead of a long
+// per-node gather), writes the 3 partial row sums to shared memory, and 96
+// threads then add the 27 partials of each (node, row).  Neighbours outside
+// the mesh are clamped onto it; their coefficients are zero.
+constexpr int NB = 32;
+constexpr int SLOT_THREADS = 27 * NB;  // 864
+
+// coordinates of the node at colour-major position p
+__device__ __forceinline__ void pos_xyz(const Lvl &L, int p, int &c, int &x, int &y, int &z)
 {
-	T a = 0;
-	const size_t s3 = 3 * (size_t)L.npad;
-	const T *kp = K + 3 * (size_t)p + i;
-#pragma unroll
-	for(int dy = -1; dy <= 1; ++dy)
-	{
-		const int yy = clampi(y + dy, 0, L.noy - 1);
-#pragma unroll
-		for(int dx = -1; dx <= 1; ++dx)
-		{
-			const int base = L.noz * (clampi(x + dx, 0, L.nox - 1) + L.nox * yy);
-#pragma unroll
-			for(int dz = -1; dz <= 1; ++dz)
-			{
-				const int m = base + clampi(z + dz, 0, L.noz - 1);
-				const T *kc = kp + (size_t)(3 * ((dz + 1) + 3 * (dx + 1) + 9 * (dy + 1))) * s3;
-				const T k0 = STREAM ? ldcs(kc) : kc[0];
-				const T k1 = STREAM ? ldcs(kc + s3) : kc[s3];
-				const T k2 = STREAM ? ldcs(kc + 2 * s3) : kc[2 * s3];
-				a += k0 * u[3 * m] + k1 * u[3 * m + 1] + k2 * u[3 * m + 2];
-			}
-		}
-	}
-	return a;
+	c = colour_of_pos(L, p);
+	cg_decode(L, c, p - L.coff[c], x, y, z);
 }
 
-constexpr int TPB3 = 192;  // multiple of 3 and of 32: a node's three rows share a block
+// partial row sums of slot s of the node at (x,y,z), position p
+template <typename T, bool STREAM>
+__device__ __forceinline__ void slot_partial(const Lvl &L, const T *K, const T *u, int p, int x, int y, int z, int s, T &a0,
+                                             T &a1, T &a2)
+{
+	const int dz = s % 3 - 1, dx = (s / 3) % 3 - 1, dy = s / 9 - 1;
+	const int m = cg_node(L, clampi(x + dx, 0, L.nox - 1), clampi(y + dy, 0, L.noy - 1), clampi(z + dz, 0, L.noz - 1));
+	const size_t s3 = 3 * (size_t)L.npad;
+	const T *kc = K + (size_t)(3 * s) * s3 + 3 * (size_t)p;  // group (3s + j), row i at +i
+	T k[9];
+#pragma unroll
+	for(int j = 0; j < 3; ++j)
+#pragma unroll
+		for(int i = 0; i < 3; ++i)
+			k[3 * j + i] = STREAM ? ldcs(kc + j * s3 + i) : kc[j * s3 + i];
+	const T u0 = u[3 * m], u1 = u[3 * m + 1], u2 = u[3 * m + 2];
+	a0 = k[0] * u0 + k[3] * u1 + k[6] * u2;
+	a1 = k[1] * u0 + k[4] * u1 + k[7] * u2;
+	a2 = k[2] * u0 + k[5] * u1 + k[8] * u2;
+}
 
-// MODE 0: out = K u;  MODE 1: out = f - K u.  Grid: x over 3 * colour size, y over colours.
+// Shared-memory layout of the partial sums: part[(s * 3 + i) * NB + ln]
+template <typename T> struct SlotSmem
+{
+	T part[27 * 3 * NB];
+};
+
+// Computes r_i = sum_m K_{n,m}[i][:] u_m for the NB nodes at colour-major
+// positions p0 .. p0+cnt-1 (all of one colour); on return the threads
+// t < 3*cnt hold (node t/3, row t%3) in `row` and its node index in `n`.
+// Every thread of the block must call it (it synchronises).
+template <typename T, bool STREAM>
+__device__ __forceinline__ void block_rows(const Lvl &L, const T *K, const T *u, int p0, int cnt, T *part, T &row, int &n)
+{
+	const int ln = threadIdx.x % NB, s = threadIdx.x / NB;
+	if(ln < cnt)
+	{
+		int c, x, y, z;
+		pos_xyz(L, p0 + ln, c, x, y, z);
+		T a0, a1, a2;
+		slot_partial<T, STREAM>(L, K, u, p0 + ln, x, y, z, s, a0, a1, a2);
+		part[(s * 3 + 0) * NB + ln] = a0;
+		part[(s * 3 + 1) * NB + ln] = a1;
+		part[(s * 3 + 2) * NB + ln] = a2;
+	}
+	__syncthreads();
+	row = 0;
+	n = 0;
+	if((int)threadIdx.x < 3 * cnt)
+	{
+		const int q = threadIdx.x / 3, i = threadIdx.x % 3;
+		T acc = 0;
+#pragma unroll
+		for(int ss = 0; ss < 27; ++ss)
+			acc += part[(ss * 3 + i) * NB + q];
+		row = acc;
+		int c, x, y, z;
+		pos_xyz(L, p0 + q, c, x, y, z);
+		n = cg_node(L, x, y, z);
+	}
+}
+
+// MODE 0: out = K u;  MODE 1: out = f - K u.  One block per NB nodes of a colour; grid (blocks, colours).
 template <typename T, int MODE>
-__global__ void k_kmul(Lvl L, const T *__restrict__ K, const T *__restrict__ u, const T *__restrict__ f, T *__restrict__ out)
+__global__ void __launch_bounds__(SLOT_THREADS) k_kmul(Lvl L, const T *__restrict__ K, const T *__restrict__ u, const T *__restrict__ f,
+                                                       T *__restrict__ out)
 {
 	pdl_begin();
+	__shared__ SlotSmem<T> sm;
 	const int c = blockIdx.y;
-	const int t = blockIdx.x * blockDim.x + threadIdx.x;
-	const int q = t / 3, i = t - 3 * q;
-	if(q >= L.coff[c + 1] - L.coff[c])
+	const int nc = L.coff[c + 1] - L.coff[c];
+	const int q0 = blockIdx.x * NB;
+	if(q0 >= nc)
 		return;
-	int x, y, z;
-	cg_decode(L, c, q, x, y, z);
-	const int n = cg_node(L, x, y, z);
-	T r = row_dot<T, true>(L, K, u, L.coff[c] + q, i, x, y, z);
-	if(MODE == 1)
-		r = f[3 * n + i] - r;
-	out[3 * n + i] = r;
+	const int cnt = min(NB, nc - q0);
+	T r;
+	int n;
+	block_rows<T, true>(L, K, u, L.coff[c] + q0, cnt, sm.part, r, n);
+	if((int)threadIdx.x < 3 * cnt)
+	{
+		const int i = threadIdx.x % 3;
+		out[3 * n + i] = (MODE == 1) ? f[3 * n + i] - r : r;
+	}
 }
 
-// AU = K u together with AU.AU and AU.res (the line search of multi_grid,
-// General_matrix_functions.c:626-630); out2[0] = AU.res, out2[1] = AU.AU
+// a.b and a.a in FP64 (a = AU, b = res for the line search of multi_grid,
+// General_matrix_functions.c:626-630): out2[0] = a.b, out2[1] = a.a
 template <typename T>
-__global__ void k_kmul_ls(Lvl L, const T *__restrict__ K, const T *__restrict__ u, const T *__restrict__ res, T *__restrict__ Au,
-                          Red red, double *out2)
+__global__ void k_dot2(int n, const T *__restrict__ a, const T *__restrict__ b, Red red, double *out2)
 {
 	pdl_begin();
 	double v[2] = {0.0, 0.0};
-	for(int t = blockIdx.x * blockDim.x + threadIdx.x; t < 3 * L.nno; t += gridDim.x * blockDim.x)
+	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
 	{
-		const int p = t / 3, i = t - 3 * p;
-		const int c = colour_of_pos(L, p);
-		int x, y, z;
-		cg_decode(L, c, p - L.coff[c], x, y, z);
-		const int n = cg_node(L, x, y, z);
-		const T r = row_dot<T, true>(L, K, u, p, i, x, y, z);
-		Au[3 * n + i] = r;
-		v[0] += (double)r * (double)res[3 * n + i];
-		v[1] += (double)r * (double)r;
+		const double x = a[i];
+		v[0] += x * (double)b[i];
+		v[1] += x * x;
 	}
 	block_reduce_store<2>(v, red, out2);
 }
@@ -359,118 +398,87 @@ __global__ void k_vel_update(int n, T *__restrict__ vel, const T *__restrict__ d
 
 // One Gauss-Seidel colour: d_n += (F_n - sum_m K_{n,m} d_m) o BI_n.  The three
 // rows of a node are relaxed together from the same d (the reference's
-// "Jacobi at a node"), so all rows are read before any is written.
+// "Jacobi at a node"): all reads happen before the block's barrier.
 template <typename T>
-__global__ void __launch_bounds__(TPB3) k_gs_colour(Lvl L, const T *__restrict__ K, const T *__restrict__ BI,
-                                                    const T *__restrict__ F, T *d, int c)
+__global__ void __launch_bounds__(SLOT_THREADS) k_gs_colour(Lvl L, const T *__restrict__ K, const T *__restrict__ BI,
+                                                            const T *__restrict__ F, T *d, int c)
 {
 	pdl_begin();
-	const int t = blockIdx.x * blockDim.x + threadIdx.x;
-	const int q = t / 3, i = t - 3 * q;
-	const bool active = q < L.coff[c + 1] - L.coff[c];
-	T upd = 0;
-	int n = 0;
-	if(active)
+	__shared__ SlotSmem<T> sm;
+	const int nc = L.coff[c + 1] - L.coff[c];
+	const int q0 = blockIdx.x * NB;
+	if(q0 >= nc)
+		return;
+	const int cnt = min(NB, nc - q0);
+	const int p0 = L.coff[c] + q0;
+	T r;
+	int n;
+	block_rows<T, true>(L, K, d, p0, cnt, sm.part, r, n);
+	if((int)threadIdx.x < 3 * cnt)
 	{
-		int x, y, z;
-		cg_decode(L, c, q, x, y, z);
-		n = cg_node(L, x, y, z);
-		const int p = L.coff[c] + q;
-		upd = (F[3 * n + i] - row_dot<T, true>(L, K, d, p, i, x, y, z)) * BI[3 * (size_t)p + i];
+		const int q = threadIdx.x / 3, i = threadIdx.x % 3;
+		d[3 * n + i] += (F[3 * n + i] - r) * BI[3 * (size_t)(p0 + q) + i];
 	}
-	__syncthreads();
-	if(active)
-		d[3 * n + i] += upd;
 }
 
-// All sweeps and colours of one gauss_seidel call on a small level in one CTA
-// (coefficients read through L2).
-constexpr int GS_SMALL_THREADS = 1023;  // multiple of 3
-template <typename T>
-__global__ void __launch_bounds__(1024) k_gs_small(Lvl L, const T *__restrict__ K, const T *__restrict__ BI,
-                                                   const T *__restrict__ F, T *d, int cycles, int zero_start)
+// All sweeps and colours of one gauss_seidel call on a small level in one
+// CTA.  SMEM: the level's stencil, 1/diag, F and d staged in shared memory
+// (coarsest levels); otherwise coefficients are read through L2.
+template <typename T, bool SMEM>
+__global__ void __launch_bounds__(SLOT_THREADS) k_gs_small(Lvl L, const T *__restrict__ K, const T *__restrict__ BI,
+                                                           const T *__restrict__ F, T *d, int cycles, int zero_start)
 {
 	pdl_begin();
-	if(zero_start)
+	__shared__ SlotSmem<T> sm;
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	const T *Kp = K, *Bp = BI, *Fp = F;
+	T *dp = d;
+	if(SMEM)
+	{
+		T *sK = reinterpret_cast<T *>(smem_raw);  // 243 * npad
+		T *sB = sK + (size_t)243 * L.npad;         // 3 * npad
+		T *sF = sB + (size_t)3 * L.npad;           // neq
+		T *sd = sF + L.neq;                        // neq
+		for(int i = threadIdx.x; i < 243 * L.npad; i += blockDim.x)
+			sK[i] = K[i];
+		for(int i = threadIdx.x; i < 3 * L.npad; i += blockDim.x)
+			sB[i] = BI[i];
+		for(int i = threadIdx.x; i < L.neq; i += blockDim.x)
+		{
+			sF[i] = F[i];
+			sd[i] = zero_start ? (T)0 : d[i];
+		}
+		Kp = sK;
+		Bp = sB;
+		Fp = sF;
+		dp = sd;
+	}
+	else if(zero_start)
 		for(int i = threadIdx.x; i < L.neq; i += blockDim.x)
 			d[i] = 0;
 	__syncthreads();
 	for(int cyc = 0; cyc < cycles; ++cyc)
 		for(int c = 0; c < 8; ++c)
 		{
-			const int nr = 3 * (L.coff[c + 1] - L.coff[c]);
-			for(int t0 = 0; t0 < nr; t0 += blockDim.x)
+			const int nc = L.coff[c + 1] - L.coff[c];
+			for(int q0 = 0; q0 < nc; q0 += NB)
 			{
-				const int t = t0 + threadIdx.x;
-				const int q = t / 3, i = t - 3 * q;
-				T upd = 0;
-				int n = 0;
-				if(t < nr)
+				const int cnt = min(NB, nc - q0);
+				const int p0 = L.coff[c] + q0;
+				T r;
+				int n;
+				block_rows<T, false>(L, Kp, dp, p0, cnt, sm.part, r, n);
+				if((int)threadIdx.x < 3 * cnt)
 				{
-					int x, y, z;
-					cg_decode(L, c, q, x, y, z);
-					n = cg_node(L, x, y, z);
-					const int p = L.coff[c] + q;
-					upd = (F[3 * n + i] - row_dot<T, false>(L, K, d, p, i, x, y, z)) * BI[3 * (size_t)p + i];
+					const int q = threadIdx.x / 3, i = threadIdx.x % 3;
+					dp[3 * n + i] += (Fp[3 * n + i] - r) * Bp[3 * (size_t)(p0 + q) + i];
 				}
 				__syncthreads();
-				if(t < nr)
-					d[3 * n + i] += upd;
 			}
-			__syncthreads();
 		}
-}
-
-// The same smoother with the level's stencil, 1/diag, F and d staged in
-// shared memory (coarsest levels): every colour phase then reads shared
-// memory only, which takes the L2 latency out of the 20-sweep coarse solve of
-// every V-cycle.
-template <typename T>
-__global__ void __launch_bounds__(1024) k_gs_small_smem(Lvl L, const T *__restrict__ K, const T *__restrict__ BI,
-                                                        const T *__restrict__ F, T *d, int cycles, int zero_start)
-{
-	pdl_begin();
-	extern __shared__ __align__(16) unsigned char smem_raw[];
-	T *sK = reinterpret_cast<T *>(smem_raw);  // 243 * npad
-	T *sB = sK + (size_t)243 * L.npad;         // 3 * npad
-	T *sF = sB + (size_t)3 * L.npad;           // neq
-	T *sd = sF + L.neq;                        // neq
-	for(int i = threadIdx.x; i < 243 * L.npad; i += blockDim.x)
-		sK[i] = K[i];
-	for(int i = threadIdx.x; i < 3 * L.npad; i += blockDim.x)
-		sB[i] = BI[i];
-	for(int i = threadIdx.x; i < L.neq; i += blockDim.x)
-	{
-		sF[i] = F[i];
-		sd[i] = zero_start ? (T)0 : d[i];
-	}
-	__syncthreads();
-	for(int cyc = 0; cyc < cycles; ++cyc)
-		for(int c = 0; c < 8; ++c)
-		{
-			const int nr = 3 * (L.coff[c + 1] - L.coff[c]);
-			for(int t0 = 0; t0 < nr; t0 += blockDim.x)
-			{
-				const int t = t0 + threadIdx.x;
-				const int q = t / 3, i = t - 3 * q;
-				T upd = 0;
-				int n = 0;
-				if(t < nr)
-				{
-					int x, y, z;
-					cg_decode(L, c, q, x, y, z);
-					n = cg_node(L, x, y, z);
-					const int p = L.coff[c] + q;
-					upd = (sF[3 * n + i] - row_dot<T, false>(L, sK, sd, p, i, x, y, z)) * sB[3 * p + i];
-				}
-				__syncthreads();
-				if(t < nr)
-					sd[3 * n + i] += upd;
-			}
-			__syncthreads();
-		}
-	for(int i = threadIdx.x; i < L.neq; i += blockDim.x)
-		d[i] = sd[i];
+	if(SMEM)
+		for(int i = threadIdx.x; i < L.neq; i += blockDim.x)
+			d[i] = dp[i];
 }
 
 // ---------------------------------------------------------------- transfers
@@ -659,6 +667,82 @@ __global__ void k_mul(int n, double *z, const double *a, const double *b)
 		z[i] = a[i] * b[i];
 }
 
+// ------------------------------------------------ Uzawa iteration (device scalars)
+// The scalars of one iteration of solve_Ahat_p_fhat (Stokes_flow_Incomp.c:393-446)
+// stay on the device: sc[0] = r1.z1, sc[1] = previous r1.z1 (= r0.z0),
+// sc[2] = s2.Ahat, sc[3] = alpha, sc[4] = error flag.
+
+// z1 = BPI o r1 and r1.z1 -> sc[0]
+__global__ void k_uz_precond(int n, const double *__restrict__ BPI, const double *__restrict__ r1, double *__restrict__ z1,
+                             Red red, double *sc)
+{
+	pdl_begin();
+	double v[1] = {0.0};
+	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+	{
+		const double z = BPI[i] * r1[i];
+		z1[i] = z;
+		v[0] += r1[i] * z;
+	}
+	block_reduce_store<1>(v, red, sc);
+}
+
+// s2 = z1 (first iteration) or z1 + (r1.z1 / r0.z0) s1; a zero r0.z0 sets the error flag
+__global__ void k_uz_search(int n, double *__restrict__ s2, const double *__restrict__ z1, const double *__restrict__ s1,
+                            double *sc, int first)
+{
+	pdl_begin();
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	double delta = 0.0;
+	if(!first)
+	{
+		if(sc[1] == 0.0)
+		{
+			if(i == 0)
+				sc[4] = 1.0;
+		}
+		else
+			delta = sc[0] / sc[1];
+	}
+	if(i < n)
+		s2[i] = first ? z1[i] : z1[i] + delta * s1[i];
+}
+
+// alpha = valid ? r1.z1 / s2.Ahat : 0;  r2 = r1 - alpha Ahat;  P += alpha s2
+__global__ void k_uz_update_p(int n, double *__restrict__ r2, const double *__restrict__ r1, const double *__restrict__ Ah,
+                              double *__restrict__ P, const double *__restrict__ s2, double *sc, int valid)
+{
+	pdl_begin();
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	const double alpha = valid ? sc[0] / sc[2] : 0.0;
+	if(i < n)
+	{
+		r2[i] = r1[i] - alpha * Ah[i];
+		P[i] += alpha * s2[i];
+	}
+}
+
+// V -= alpha u1; the last kernel of the iteration also records alpha and
+// moves r1.z1 into the r0.z0 slot for the next iteration
+__global__ void k_uz_update_v(int n, double *__restrict__ V, const double *__restrict__ u1, double *sc, int valid)
+{
+	pdl_begin();
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	const double alpha = valid ? sc[0] / sc[2] : 0.0;
+	if(i < n)
+		V[i] -= alpha * u1[i];
+}
+
+__global__ void k_uz_finish(double *sc, int valid)
+{
+	pdl_begin();
+	if(threadIdx.x == 0 && blockIdx.x == 0)
+	{
+		sc[3] = valid ? sc[0] / sc[2] : 0.0;
+		sc[1] = sc[0];
+	}
+}
+
 __global__ void k_lin2(int n, double *z, double a, const double *x, double b, const double *y)
 {
 	pdl_begin();
@@ -689,26 +773,6 @@ __global__ void k_add_f2d(int n, double *dst, const float *src)
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i < n)
 		dst[i] += (double)src[i];
-}
-
-// r = f - K u in FP64 with r.r
-__global__ void k_residual64(Lvl L, const double *__restrict__ K, const double *__restrict__ f, const double *__restrict__ u,
-                             double *__restrict__ r, Red red, double *out)
-{
-	pdl_begin();
-	double v[1] = {0.0};
-	for(int t = blockIdx.x * blockDim.x + threadIdx.x; t < 3 * L.nno; t += gridDim.x * blockDim.x)
-	{
-		const int p = t / 3, i = t - 3 * p;
-		const int c = colour_of_pos(L, p);
-		int x, y, z;
-		cg_decode(L, c, p - L.coff[c], x, y, z);
-		const int n = cg_node(L, x, y, z);
-		const double ri = f[3 * n + i] - row_dot<double, true>(L, K, u, p, i, x, y, z);
-		r[3 * n + i] = ri;
-		v[0] += ri * ri;
-	}
-	block_reduce_store<1>(v, red, out);
 }
 
 // ---------------------------------------------------------------- viscosity
@@ -1357,20 +1421,21 @@ static int max_colour(const Lvl &L)
 
 template <typename T> void launch_kmul(cudaStream_t st, const Lvl &L, const T *K, const T *u, T *Au)
 {
-	dim3 grid(nblocks(3 * (long)max_colour(L), TPB3), 8);
-	launch_k(k_kmul<T, 0>, grid, TPB3, st, L, K, u, (const T *)nullptr, Au);
+	dim3 grid((max_colour(L) + NB - 1) / NB, 8);
+	launch_k(k_kmul<T, 0>, grid, SLOT_THREADS, st, L, K, u, (const T *)nullptr, Au);
 }
 
 template <typename T> void launch_residual(cudaStream_t st, const Lvl &L, const T *K, const T *f, const T *u, T *r)
 {
-	dim3 grid(nblocks(3 * (long)max_colour(L), TPB3), 8);
-	launch_k(k_kmul<T, 1>, grid, TPB3, st, L, K, u, f, r);
+	dim3 grid((max_colour(L) + NB - 1) / NB, 8);
+	launch_k(k_kmul<T, 1>, grid, SLOT_THREADS, st, L, K, u, f, r);
 }
 
 template <typename T>
 void launch_kmul_linesearch(cudaStream_t st, const Lvl &L, const T *K, const T *u, const T *res, T *Au, Red red, double *out2)
 {
-	launch_k(k_kmul_ls<T>, red_grid(3 * (long)L.nno), RED_THREADS, st, L, K, u, res, Au, red, out2);
+	launch_kmul<T>(st, L, K, u, Au);
+	launch_k(k_dot2<T>, red_grid(L.neq), RED_THREADS, st, L.neq, (const T *)Au, res, red, out2);
 }
 
 template <typename T> void launch_gs_colour(cudaStream_t st, const Lvl &L, const T *K, const T *BI, const T *F, T *d, int c)
@@ -1378,34 +1443,31 @@ template <typename T> void launch_gs_colour(cudaStream_t st, const Lvl &L, const
 	const int n = L.coff[c + 1] - L.coff[c];
 	if(n > 0)
 	{
-		launch_k(k_gs_colour<T>, nblocks(3 * (long)n, TPB3), TPB3, st, L, K, BI, F, d, c);
+		launch_k(k_gs_colour<T>, (n + NB - 1) / NB, SLOT_THREADS, st, L, K, BI, F, d, c);
 	}
 }
 
-bool gs_small_fits(const Lvl &L) { return 3 * L.nno <= 4 * GS_SMALL_THREADS; }
+bool gs_small_fits(const Lvl &L) { return L.nno <= 1400; }
 
 int kernels_init()
 {
 	// opt in to large dynamic shared memory once, outside any stream capture
-	cudaError_t a = cudaFuncSetAttribute(k_gs_small_smem<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-	cudaError_t b = cudaFuncSetAttribute(k_gs_small_smem<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+	cudaError_t a = cudaFuncSetAttribute(k_gs_small<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 180 * 1024);
+	cudaError_t b = cudaFuncSetAttribute(k_gs_small<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 180 * 1024);
 	return (a == cudaSuccess && b == cudaSuccess) ? 0 : -1;
 }
 
 static size_t gs_smem_bytes(const Lvl &L, size_t word) { return word * ((size_t)246 * L.npad + 2 * (size_t)L.neq); }
 
-constexpr size_t GS_SMEM_LIMIT = 200 * 1024;
-
 template <typename T>
 void launch_gs_small(cudaStream_t st, const Lvl &L, const T *K, const T *BI, const T *F, T *d, int cycles, int zero_start)
 {
+	// dynamic part + the static partial-sum buffer must fit the 227 KB of a CTA
 	const size_t bytes = gs_smem_bytes(L, sizeof(T));
-	if(bytes <= GS_SMEM_LIMIT)
-	{
-		launch_k_smem(k_gs_small_smem<T>, dim3(1), dim3(GS_SMALL_THREADS), bytes, st, L, K, BI, F, d, cycles, zero_start);
-		return;
-	}
-	launch_k(k_gs_small<T>, 1, GS_SMALL_THREADS, st, L, K, BI, F, d, cycles, zero_start);
+	if(bytes <= 180 * 1024)
+		launch_k_smem(k_gs_small<T, true>, dim3(1), dim3(SLOT_THREADS), bytes, st, L, K, BI, F, d, cycles, zero_start);
+	else
+		launch_k(k_gs_small<T, false>, 1, SLOT_THREADS, st, L, K, BI, F, d, cycles, zero_start);
 }
 
 template <typename T> void launch_project(cudaStream_t st, const Lvl &Lf, const Lvl &Lc, const T *AU, T *AD)
@@ -1467,6 +1529,24 @@ void launch_axpby(cudaStream_t st, int n, double *y, double a, const double *x, 
 
 void launch_mul(cudaStream_t st, int n, double *z, const double *a, const double *b) { launch_k(k_mul, nblocks(n), TPB, st, n, z, a, b); }
 
+void launch_uzawa_precond(cudaStream_t st, int n, const double *BPI, const double *r1, double *z1, Red red, double *sc)
+{
+	launch_k(k_uz_precond, red_grid(n), RED_THREADS, st, n, BPI, r1, z1, red, sc);
+}
+
+void launch_uzawa_search(cudaStream_t st, int n, double *s2, const double *z1, const double *s1, double *sc, int first)
+{
+	launch_k(k_uz_search, nblocks(n), TPB, st, n, s2, z1, s1, sc, first);
+}
+
+void launch_uzawa_update(cudaStream_t st, int npno, int neq, double *r2, const double *r1, const double *Ah, double *P,
+                         const double *s2, double *V, const double *u1, double *sc, int valid)
+{
+	launch_k(k_uz_update_p, nblocks(npno), TPB, st, npno, r2, r1, Ah, P, s2, sc, valid);
+	launch_k(k_uz_update_v, nblocks(neq), TPB, st, neq, V, u1, sc, valid);
+	launch_k(k_uz_finish, 1, 32, st, sc, valid);
+}
+
 void launch_lin2(cudaStream_t st, int n, double *z, double a, const double *x, double b, const double *y)
 {
 	launch_k(k_lin2, nblocks(n), TPB, st, n, z, a, x, b, y);
@@ -1483,7 +1563,8 @@ void launch_add_f2d(cudaStream_t st, int n, double *dst, const float *src) { lau
 
 void launch_residual64(cudaStream_t st, const Lvl &L, const double *K, const double *f, const double *u, double *r, Red red, double *out)
 {
-	launch_k(k_residual64, red_grid(3 * (long)L.nno), RED_THREADS, st, L, K, f, u, r, red, out);
+	launch_residual<double>(st, L, K, f, u, r);
+	launch_k(k_dot, red_grid(L.neq), RED_THREADS, st, L.neq, (const double *)r, (const double *)r, red, out);
 }
 
 void launch_visc_from_T(cudaStream_t st, const Lvl &L, const Geo *geo, const Rheo &r, const double *T, double *evi)

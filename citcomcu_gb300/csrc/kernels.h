@@ -63,6 +63,11 @@ void launch_dots4(cudaStream_t st, int n, const double *a0, const double *b0, co
                   const double *a2, const double *b2, const double *a3, const double *b3, Red red, double *out);
 void launch_axpby(cudaStream_t st, int n, double *y, double a, const double *x, double b);  // y = a*y + b*x
 void launch_mul(cudaStream_t st, int n, double *z, const double *a, const double *b);       // z = a*b
+// one Uzawa iteration's vector work with device-resident scalars sc[0..4]
+void launch_uzawa_precond(cudaStream_t st, int n, const double *BPI, const double *r1, double *z1, Red red, double *sc);
+void launch_uzawa_search(cudaStream_t st, int n, double *s2, const double *z1, const double *s1, double *sc, int first);
+void launch_uzawa_update(cudaStream_t st, int npno, int neq, double *r2, const double *r1, const double *Ah, double *P,
+                         const double *s2, double *V, const double *u1, double *sc, int valid);
 void launch_lin2(cudaStream_t st, int n, double *z, double a, const double *x, double b, const double *y);  // z = a*x + b*y
 void launch_sub3(cudaStream_t st, int n, double *z, const double *f, const double *a, const double *b);     // z = f - a - b
 void launch_copy_d2f(cudaStream_t st, int n, float *dst, const double *src);
