@@ -137,6 +137,7 @@ void make_level(const citcom_gpu_config &c, int l, Lvl &L)
 	L.nel = L.elx * L.ely * L.elz;
 	L.neq = 3 * L.nno;
 	L.npad = (L.nno + 31) / 32 * 32;
+	L.aos = L.nno <= CG_SMALL_LEVEL_NODES;
 	const int N[3] = {L.nox, L.noy, L.noz};
 	for(int a = 0; a < 3; ++a)
 		for(int p = 0; p < 2; ++p)

@@ -264,14 +264,14 @@ __global__ void k_bpi(Lvl L, const Geo *__restrict__ geo, const double *__restri
 // ---------------------------------------------------------------- stencil
 
 // Stencil products are computed by one thread per (node, neighbour slot): a
-// block holds NB = 32 nodes x 27 slots; warp w of the block is slot w for 32
+// block holds NB = 16 nodes x 27 slots; each warp covers two slots of 16
 // consecutive nodes of one colour.  Each thread issues its 9 coefficient loads
 // and 3 neighbour loads at once (memory-level parallelism instead of a long
 // per-node gather), writes the 3 partial row sums to shared memory, and 96
 // threads then add the 27 partials of each (node, row).  Neighbours outside
 // the mesh are clamped onto it; their coefficients are zero.
-constexpr int NB = 32;
-constexpr int SLOT_THREADS = 27 * NB;  // 864
+constexpr int NB = 16;
+constexpr int SLOT_THREADS = 27 * NB;  // 432
 
 // coordinates of the node at colour-major position p
 __device__ __forceinline__ void pos_xyz(const Lvl &L, int p, int &c, int &x, int &y, int &z)
@@ -287,14 +287,26 @@ __device__ __forceinline__ void slot_partial(const Lvl &L, const T *K, const T *
 {
 	const int dz = s % 3 - 1, dx = (s / 3) % 3 - 1, dy = s / 9 - 1;
 	const int m = cg_node(L, clampi(x + dx, 0, L.nox - 1), clampi(y + dy, 0, L.noy - 1), clampi(z + dz, 0, L.noz - 1));
-	const size_t s3 = 3 * (size_t)L.npad;
-	const T *kc = K + (size_t)(3 * s) * s3 + 3 * (size_t)p;  // group (3s + j), row i at +i
-	T k[9];
-#pragma unroll
-	for(int j = 0; j < 3; ++j)
+	T k[9];  // k[3j + i] = K_{n,m}[i][j]
+	if(L.aos)
+	{
+		const T *kc = K + (size_t)243 * p + 9 * s;
 #pragma unroll
 		for(int i = 0; i < 3; ++i)
-			k[3 * j + i] = STREAM ? ldcs(kc + j * s3 + i) : kc[j * s3 + i];
+#pragma unroll
+			for(int j = 0; j < 3; ++j)
+				k[3 * j + i] = kc[3 * i + j];
+	}
+	else
+	{
+		const size_t s3 = 3 * (size_t)L.npad;
+		const T *kc = K + (size_t)(3 * s) * s3 + 3 * (size_t)p;  // group (3s + j), row i at +i
+#pragma unroll
+		for(int j = 0; j < 3; ++j)
+#pragma unroll
+			for(int i = 0; i < 3; ++i)
+				k[3 * j + i] = STREAM ? ldcs(kc + j * s3 + i) : kc[j * s3 + i];
+	}
 	const T u0 = u[3 * m], u1 = u[3 * m + 1], u2 = u[3 * m + 2];
 	a0 = k[0] * u0 + k[3] * u1 + k[6] * u2;
 	a1 = k[1] * u0 + k[4] * u1 + k[7] * u2;
@@ -421,27 +433,32 @@ __global__ void __launch_bounds__(SLOT_THREADS) k_gs_colour(Lvl L, const T *__re
 	}
 }
 
-// All sweeps and colours of one gauss_seidel call on a small level in one
-// CTA.  SMEM: the level's stencil, 1/diag, F and d staged in shared memory
-// (coarsest levels); otherwise coefficients are read through L2.
+// All sweeps and colours of one gauss_seidel call on a small level (stored
+// node by node) in one CTA of 32 warps: a warp relaxes one node at a time,
+// lane s < 27 handling neighbour slot s (9 coefficients and 3 neighbour
+// values), the 27 partial rows added by warp shuffles; lanes 0..2 then apply
+// the node update.  SMEM: stencil, 1/diag, F and d staged in shared memory
+// (coarsest levels); otherwise coefficients come through L2 and each warp
+// processes up to GSW nodes at once to overlap their loads.
+constexpr int GS_WARPS = 32;
+constexpr int GSW = 3;
 template <typename T, bool SMEM>
-__global__ void __launch_bounds__(SLOT_THREADS) k_gs_small(Lvl L, const T *__restrict__ K, const T *__restrict__ BI,
-                                                           const T *__restrict__ F, T *d, int cycles, int zero_start)
+__global__ void __launch_bounds__(GS_WARPS * 32) k_gs_small(Lvl L, const T *__restrict__ K, const T *__restrict__ BI,
+                                                            const T *__restrict__ F, T *d, int cycles, int zero_start)
 {
 	pdl_begin();
-	__shared__ SlotSmem<T> sm;
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	const T *Kp = K, *Bp = BI, *Fp = F;
 	T *dp = d;
 	if(SMEM)
 	{
-		T *sK = reinterpret_cast<T *>(smem_raw);  // 243 * npad
-		T *sB = sK + (size_t)243 * L.npad;         // 3 * npad
-		T *sF = sB + (size_t)3 * L.npad;           // neq
+		T *sK = reinterpret_cast<T *>(smem_raw);  // 243 * nno
+		T *sB = sK + (size_t)243 * L.nno;          // 3 * nno
+		T *sF = sB + (size_t)3 * L.nno;            // neq
 		T *sd = sF + L.neq;                        // neq
-		for(int i = threadIdx.x; i < 243 * L.npad; i += blockDim.x)
+		for(int i = threadIdx.x; i < 243 * L.nno; i += blockDim.x)
 			sK[i] = K[i];
-		for(int i = threadIdx.x; i < 3 * L.npad; i += blockDim.x)
+		for(int i = threadIdx.x; i < 3 * L.nno; i += blockDim.x)
 			sB[i] = BI[i];
 		for(int i = threadIdx.x; i < L.neq; i += blockDim.x)
 		{
@@ -457,24 +474,56 @@ __global__ void __launch_bounds__(SLOT_THREADS) k_gs_small(Lvl L, const T *__res
 		for(int i = threadIdx.x; i < L.neq; i += blockDim.x)
 			d[i] = 0;
 	__syncthreads();
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	const int s = lane < 27 ? lane : 13;  // idle lanes shadow the centre slot with zero weight
+	const int dz = s % 3 - 1, dx = (s / 3) % 3 - 1, dy = s / 9 - 1;
 	for(int cyc = 0; cyc < cycles; ++cyc)
 		for(int c = 0; c < 8; ++c)
 		{
 			const int nc = L.coff[c + 1] - L.coff[c];
-			for(int q0 = 0; q0 < nc; q0 += NB)
+			for(int q0 = warp; q0 < nc; q0 += GS_WARPS * GSW)
 			{
-				const int cnt = min(NB, nc - q0);
-				const int p0 = L.coff[c] + q0;
-				T r;
-				int n;
-				block_rows<T, false>(L, Kp, dp, p0, cnt, sm.part, r, n);
-				if((int)threadIdx.x < 3 * cnt)
+				T r[GSW][3];
+				int nn[GSW], pp[GSW];
+#pragma unroll
+				for(int w = 0; w < GSW; ++w)
 				{
-					const int q = threadIdx.x / 3, i = threadIdx.x % 3;
-					dp[3 * n + i] += (Fp[3 * n + i] - r) * Bp[3 * (size_t)(p0 + q) + i];
+					const int q = q0 + w * GS_WARPS;
+					r[w][0] = r[w][1] = r[w][2] = 0;
+					nn[w] = -1;
+					pp[w] = 0;
+					if(q < nc)
+					{
+						int x, y, z;
+						cg_decode(L, c, q, x, y, z);
+						const int p = L.coff[c] + q;
+						const int m = cg_node(L, clampi(x + dx, 0, L.nox - 1), clampi(y + dy, 0, L.noy - 1),
+						                      clampi(z + dz, 0, L.noz - 1));
+						const T *kc = Kp + (size_t)243 * p + 9 * s;
+						const T u0 = dp[3 * m], u1 = dp[3 * m + 1], u2 = dp[3 * m + 2];
+						const T wgt = lane < 27 ? (T)1 : (T)0;
+						r[w][0] = wgt * (kc[0] * u0 + kc[1] * u1 + kc[2] * u2);
+						r[w][1] = wgt * (kc[3] * u0 + kc[4] * u1 + kc[5] * u2);
+						r[w][2] = wgt * (kc[6] * u0 + kc[7] * u1 + kc[8] * u2);
+						nn[w] = cg_node(L, x, y, z);
+						pp[w] = p;
+					}
 				}
-				__syncthreads();
+#pragma unroll
+				for(int w = 0; w < GSW; ++w)
+#pragma unroll
+					for(int i = 0; i < 3; ++i)
+						for(int o = 16; o > 0; o >>= 1)
+							r[w][i] += __shfl_xor_sync(0xffffffffu, r[w][i], o);
+#pragma unroll
+				for(int w = 0; w < GSW; ++w)
+					if(nn[w] >= 0 && lane < 3)
+					{
+						const T ri = lane == 0 ? r[w][0] : (lane == 1 ? r[w][1] : r[w][2]);
+						dp[3 * nn[w] + lane] += (Fp[3 * nn[w] + lane] - ri) * Bp[3 * (size_t)pp[w] + lane];
+					}
 			}
+			__syncthreads();
 		}
 	if(SMEM)
 		for(int i = threadIdx.x; i < L.neq; i += blockDim.x)
@@ -483,44 +532,60 @@ __global__ void __launch_bounds__(SLOT_THREADS) k_gs_small(Lvl L, const T *__res
 
 // ---------------------------------------------------------------- transfers
 
-// project_vector (Solver_multigrid.c:72-159) at one coarse node, followed by
-// strip_bcs_from_residual on the coarse level
+// project_vector (Solver_multigrid.c:72-159), node-centred: 8 consecutive
+// lanes serve one coarse node, lane a its coarse element at corner a (the
+// fine sub-element of that corner); the lanes' sums are added by shuffles.
+// Followed by strip_bcs_from_residual on the coarse level.
 template <typename T>
 __global__ void k_project(Lvl Lf, Lvl Lc, const T *__restrict__ AU, T *__restrict__ AD)
 {
 	pdl_begin();
-	const int N = blockIdx.x * blockDim.x + threadIdx.x;
-	if(N >= Lc.nno)
-		return;
-	const int Z = N % Lc.noz, X = (N / Lc.noz) % Lc.nox, Y = N / (Lc.noz * Lc.nox);
+	const int t = blockIdx.x * blockDim.x + threadIdx.x;
+	const int N = t >> 3, a = t & 7;
 	double s0 = 0.0, s1 = 0.0, s2 = 0.0;
 	int cnt = 0;
-	for(int a = 0; a < 8; ++a)
+	int X = 0, Y = 0, Z = 0;
+	if(N < Lc.nno)
 	{
+		Z = N % Lc.noz;
+		X = (N / Lc.noz) % Lc.nox;
+		Y = N / (Lc.noz * Lc.nox);
 		const int ox = cg_loc(a, 0), oy = cg_loc(a, 1), oz = cg_loc(a, 2);
 		const int ex = X - ox, ey = Y - oy, ez = Z - oz;
-		if(ex < 0 || ex >= Lc.elx || ey < 0 || ey >= Lc.ely || ez < 0 || ez >= Lc.elz)
-			continue;
-		++cnt;
-		// fine sub-element at corner a of the coarse element
-		const int fx = 2 * ex + ox, fy = 2 * ey + oy, fz = 2 * ez + oz;
-		double t0 = 0.0, t1 = 0.0, t2 = 0.0;
-		for(int b = 0; b < 8; ++b)
+		if(ex >= 0 && ex < Lc.elx && ey >= 0 && ey < Lc.ely && ez >= 0 && ez < Lc.elz)
 		{
-			const int m = cg_node(Lf, fx + cg_loc(b, 0), fy + cg_loc(b, 1), fz + cg_loc(b, 2));
-			t0 += (double)AU[3 * m];
-			t1 += (double)AU[3 * m + 1];
-			t2 += (double)AU[3 * m + 2];
+			cnt = 1;
+			const int fx = 2 * ex + ox, fy = 2 * ey + oy, fz = 2 * ez + oz;
+			double t0 = 0.0, t1 = 0.0, t2 = 0.0;
+#pragma unroll
+			for(int b = 0; b < 8; ++b)
+			{
+				const int m = cg_node(Lf, fx + cg_loc(b, 0), fy + cg_loc(b, 1), fz + cg_loc(b, 2));
+				t0 += (double)AU[3 * m];
+				t1 += (double)AU[3 * m + 1];
+				t2 += (double)AU[3 * m + 2];
+			}
+			s0 = Lc.J * t0;
+			s1 = Lc.J * t1;
+			s2 = Lc.J * t2;
 		}
-		s0 += Lc.J * t0;
-		s1 += Lc.J * t1;
-		s2 += Lc.J * t2;
 	}
-	const double mass = 1.0 / ((double)cnt * Lc.J);
-	const unsigned f = cg_vflag(Lc, X, Y, Z);
-	AD[3 * N] = (f & 1u) ? (T)0 : (T)(s0 * mass);
-	AD[3 * N + 1] = (f & 2u) ? (T)0 : (T)(s1 * mass);
-	AD[3 * N + 2] = (f & 4u) ? (T)0 : (T)(s2 * mass);
+	// fixed-order sum over the 8 corners (lane a of the group holds corner a)
+	for(int o = 1; o < 8; o <<= 1)
+	{
+		s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+		s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+		s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+		cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+	}
+	if(N < Lc.nno && a == 0)
+	{
+		const double mass = 1.0 / ((double)cnt * Lc.J);
+		const unsigned f = cg_vflag(Lc, X, Y, Z);
+		AD[3 * N] = (f & 1u) ? (T)0 : (T)(s0 * mass);
+		AD[3 * N + 1] = (f & 2u) ? (T)0 : (T)(s1 * mass);
+		AD[3 * N + 2] = (f & 4u) ? (T)0 : (T)(s2 * mass);
+	}
 }
 
 // interp_vector (Solver_multigrid.c:173-298): injection, then linear fill
@@ -1447,32 +1512,31 @@ template <typename T> void launch_gs_colour(cudaStream_t st, const Lvl &L, const
 	}
 }
 
-bool gs_small_fits(const Lvl &L) { return L.nno <= 1400; }
+bool gs_small_fits(const Lvl &L) { return L.aos != 0; }
 
 int kernels_init()
 {
 	// opt in to large dynamic shared memory once, outside any stream capture
-	cudaError_t a = cudaFuncSetAttribute(k_gs_small<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 180 * 1024);
-	cudaError_t b = cudaFuncSetAttribute(k_gs_small<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 180 * 1024);
+	cudaError_t a = cudaFuncSetAttribute(k_gs_small<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+	cudaError_t b = cudaFuncSetAttribute(k_gs_small<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
 	return (a == cudaSuccess && b == cudaSuccess) ? 0 : -1;
 }
 
-static size_t gs_smem_bytes(const Lvl &L, size_t word) { return word * ((size_t)246 * L.npad + 2 * (size_t)L.neq); }
+static size_t gs_smem_bytes(const Lvl &L, size_t word) { return word * ((size_t)246 * L.nno + 2 * (size_t)L.neq); }
 
 template <typename T>
 void launch_gs_small(cudaStream_t st, const Lvl &L, const T *K, const T *BI, const T *F, T *d, int cycles, int zero_start)
 {
-	// dynamic part + the static partial-sum buffer must fit the 227 KB of a CTA
 	const size_t bytes = gs_smem_bytes(L, sizeof(T));
-	if(bytes <= 180 * 1024)
-		launch_k_smem(k_gs_small<T, true>, dim3(1), dim3(SLOT_THREADS), bytes, st, L, K, BI, F, d, cycles, zero_start);
+	if(bytes <= 200 * 1024)
+		launch_k_smem(k_gs_small<T, true>, dim3(1), dim3(GS_WARPS * 32), bytes, st, L, K, BI, F, d, cycles, zero_start);
 	else
-		launch_k(k_gs_small<T, false>, 1, SLOT_THREADS, st, L, K, BI, F, d, cycles, zero_start);
+		launch_k(k_gs_small<T, false>, 1, GS_WARPS * 32, st, L, K, BI, F, d, cycles, zero_start);
 }
 
 template <typename T> void launch_project(cudaStream_t st, const Lvl &Lf, const Lvl &Lc, const T *AU, T *AD)
 {
-	launch_k(k_project<T>, nblocks(Lc.nno), TPB, st, Lf, Lc, AU, AD);
+	launch_k(k_project<T>, nblocks(8 * (long)Lc.nno), TPB, st, Lf, Lc, AU, AD);
 }
 
 template <typename T> void launch_interp(cudaStream_t st, const Lvl &Lc, const Lvl &Lf, const T *AD, T *AU)

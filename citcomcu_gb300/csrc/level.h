@@ -19,6 +19,7 @@ struct Lvl
 	int nno, nel, neq;
 	int elx, ely, elz;
 	int npad;        // stride of the structure-of-arrays coefficient storage
+	int aos;         // 1: small level, stencil stored node by node (243 contiguous words per node)
 	int cnt[3][2];   // number of indices of parity p along axis (0 x, 1 y, 2 z)
 	int coff[9];     // colour offsets in colour-major order
 	double h[3];     // element edge lengths (uniform per axis)
@@ -73,8 +74,14 @@ CG_HD int cg_loc(int a, int d)
 // a node's rows read consecutive words
 CG_HD size_t cg_kidx(const Lvl &L, int s, int i, int j, int p)
 {
+	if(L.aos)
+		return (size_t)243 * p + 9 * s + 3 * i + j;
 	return (size_t)(3 * s + j) * 3 * (size_t)L.npad + 3 * (size_t)p + i;
 }
+
+// levels up to this many nodes keep the node-by-node layout and are smoothed
+// by one CTA (warp per node)
+#define CG_SMALL_LEVEL_NODES 1400
 
 CG_HD int cg_local_index(int ox, int oy, int oz)
 {

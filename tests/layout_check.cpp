@@ -35,9 +35,11 @@ static int fail(const char *m, int a, int b)
 int main()
 {
 	const int sizes[][3] = {{4, 4, 4}, {8, 12, 8}, {16, 16, 16}, {2, 3, 2}, {4, 4, 2}, {8, 8, 4}, {1, 1, 1}, {32, 32, 32}};
+	for(int aos = 0; aos < 2; ++aos)
 	for(auto &sz : sizes)
 	{
 		Lvl L = make(sz[0], sz[1], sz[2]);
+		L.aos = aos;
 		if(L.coff[8] != L.nno)
 			return fail("colour counts", L.coff[8], L.nno);
 		std::vector<int> seen(L.nno, 0);
@@ -66,10 +68,13 @@ int main()
 							return fail("kidx range", p, s);
 						if(used[k]++)
 							return fail("kidx unique", p, s);
-						// row_dot: kp = K + 3p + i, kc = kp + 3*slot*s3, loads kc + j*s3
+						// slot_partial: structure-of-arrays kc = K + 3s*s3 + 3p, loads kc + j*s3 + i;
+						// node-by-node kc = K + 243p + 9s, loads kc + 3i + j
 						const size_t s3 = 3 * (size_t)L.npad;
-						if(3 * (size_t)p + i + (size_t)(3 * s) * s3 + j * s3 != k)
-							return fail("row_dot pattern", p, s);
+						const size_t expect = aos ? (size_t)243 * p + 9 * s + 3 * i + j
+						                          : 3 * (size_t)p + i + (size_t)(3 * s) * s3 + j * s3;
+						if(expect != k)
+							return fail("gather pattern", p, s);
 					}
 		// BI[3p + i] inside 3*npad; vectors 3n + i inside neq
 		if(3 * (size_t)(L.nno - 1) + 2 >= 3 * (size_t)L.npad)
