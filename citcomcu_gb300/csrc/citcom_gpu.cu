@@ -77,6 +77,10 @@ struct citcom_gpu
 	bool visc_ready;
 	bool verbose;
 	bool no_graph;
+	bool level_timing;            // CITCOM_GPU_LEVEL_TIMING: time every smoother call (no graph)
+	double lt_ms[CITCOM_MAX_LEVELS];
+	long lt_calls[CITCOM_MAX_LEVELS];
+	long lt_sweeps[CITCOM_MAX_LEVELS];
 	citcom_gpu_stats stats;
 	std::vector<void *> allocs;
 	char err[512];
@@ -200,7 +204,20 @@ template <typename T> void gs(citcom_gpu *h, MG<T> &B, int lev, T *d, const T *F
 		flags = (cs == cudaStreamCaptureStatusActive) ? cudaEventRecordExternal : 0u;
 		cudaEventRecordWithFlags(h->ev_gs[2 * h->n_gs_pairs], h->st, flags);
 	}
-	gs_inner<T>(h, B, lev, d, F, cycles, zero_start);
+	if(h->level_timing)
+	{
+		cudaEventRecord(h->ev_gs[4], h->st);
+		gs_inner<T>(h, B, lev, d, F, cycles, zero_start);
+		cudaEventRecord(h->ev_gs[5], h->st);
+		cudaEventSynchronize(h->ev_gs[5]);
+		float ms = 0.f;
+		cudaEventElapsedTime(&ms, h->ev_gs[4], h->ev_gs[5]);
+		h->lt_ms[lev] += ms;
+		h->lt_calls[lev] += 1;
+		h->lt_sweeps[lev] += cycles;
+	}
+	else
+		gs_inner<T>(h, B, lev, d, F, cycles, zero_start);
 	if(timed)
 	{
 		cudaEventRecordWithFlags(h->ev_gs[2 * h->n_gs_pairs + 1], h->st, flags);
@@ -650,6 +667,13 @@ int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 		h->verbose = v && v[0] && v[0] != '0';
 		const char *g = getenv("CITCOM_GPU_NO_GRAPH");
 		h->no_graph = g && g[0] && g[0] != '0';
+		const char *t = getenv("CITCOM_GPU_LEVEL_TIMING");
+		h->level_timing = t && t[0] && t[0] != '0';
+		if(h->level_timing)
+			h->no_graph = true;
+		const char *q = getenv("CITCOM_GPU_NO_PDL");
+		if(q && q[0] && q[0] != '0')
+			g_use_pdl = 0;
 	}
 	memset(&h->stats, 0, sizeof(h->stats));
 	int r = CITCOM_GPU_OK;
@@ -767,6 +791,12 @@ void citcom_gpu_destroy(citcom_gpu *h)
 {
 	if(!h)
 		return;
+	if(h->level_timing)
+		for(int l = 0; l < h->L; ++l)
+			fprintf(stderr, "level %d (%d nodes, %s): %ld smoother calls, %ld sweeps, %.3f ms total, %.2f us/call, %.2f us/sweep\n",
+			        l, h->lv[l].nno, h->cfg.precision == CITCOM_GPU_FP64 ? "fp64" : "fp32", h->lt_calls[l], h->lt_sweeps[l],
+			        h->lt_ms[l], h->lt_calls[l] ? 1e3 * h->lt_ms[l] / h->lt_calls[l] : 0.0,
+			        h->lt_sweeps[l] ? 1e3 * h->lt_ms[l] / h->lt_sweeps[l] : 0.0);
 	if(h->st)
 		cudaStreamSynchronize(h->st);
 	if(h->mg_exec)

@@ -1385,6 +1385,7 @@ __global__ void k_vrms(Lvl L, const Geo *__restrict__ geo, const double *__restr
 // ====================================================================== host
 
 unsigned long long g_kernel_launches = 0;
+int g_use_pdl = 1;
 
 template <typename... KArgs, typename... Args>
 static void launch_k_smem(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args... args)
@@ -1398,7 +1399,7 @@ static void launch_k_smem(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t 
 	attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
 	attr[0].val.programmaticStreamSerializationAllowed = 1;
 	cfg.attrs = attr;
-	cfg.numAttrs = 1;
+	cfg.numAttrs = g_use_pdl ? 1 : 0;
 	cudaLaunchKernelEx(&cfg, kern, ((KArgs)args)...);
 	++g_kernel_launches;
 }
@@ -1415,7 +1416,7 @@ static void launch_k(void (*kern)(KArgs...), dim3 grid, dim3 block, cudaStream_t
 	attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
 	attr[0].val.programmaticStreamSerializationAllowed = 1;
 	cfg.attrs = attr;
-	cfg.numAttrs = 1;
+	cfg.numAttrs = g_use_pdl ? 1 : 0;
 	cudaLaunchKernelEx(&cfg, kern, ((KArgs)args)...);
 	++g_kernel_launches;
 }

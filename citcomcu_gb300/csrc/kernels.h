@@ -30,6 +30,8 @@ void geo_fill_host(const Lvl &L, Geo *g);
 // kernels issued by the launchers below since load (host-side count; a graph
 // capture counts its kernels once, each replay is added by the driver)
 extern unsigned long long g_kernel_launches;
+// launches carry the programmatic-dependent-launch attribute unless 0
+extern int g_use_pdl;
 
 // one-time function attributes (large dynamic shared memory); 0 on success
 int kernels_init();

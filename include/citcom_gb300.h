@@ -20,7 +20,10 @@
  * environment variable CITCOM_GPU_VERBOSE=1 prints one line per Uzawa
  * iteration in the spirit of the reference's generate_log_message;
  * CITCOM_GPU_NO_GRAPH=1 launches the multigrid pass kernel by kernel instead
- * of replaying it as a CUDA graph (for kernel profilers).  There is no CPU
+ * of replaying it as a CUDA graph (for kernel profilers); CITCOM_GPU_NO_PDL=1
+ * launches without programmatic dependent launch; CITCOM_GPU_LEVEL_TIMING=1
+ * times every smoother call per level (no graph) and prints the totals when
+ * the handle is destroyed.  There is no CPU
  * fallback: without a usable CUDA device citcom_gpu_create fails.
  *
  * Scope: Cartesian box, uniform spacing per axis on every multigrid level,
