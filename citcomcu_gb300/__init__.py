@@ -19,7 +19,7 @@ import numpy as np
 from .build import LIB as LIB_PATH
 from .build import build as _build_lib
 
-__all__ = ["Config", "Solver", "CitcomGPUError", "load_library", "build", "FP64", "MIXED"]
+__all__ = ["Config", "Solver", "CitcomGPUError", "load_library", "build", "heat_flux_noalloc", "FP64", "MIXED"]
 
 FP64 = 0
 MIXED = 1
@@ -169,6 +169,8 @@ _SIGNATURES = {
     "citcom_gpu_op_multi_grid": (ctypes.c_int, [_H, _D, _D, _D]),
     "citcom_gpu_op_solve_del2_u": (ctypes.c_int, [_H, _D, _D, ctypes.c_double, _I]),
     "citcom_gpu_op_diagonals": (ctypes.c_int, [_H, ctypes.c_int, _D, _D]),
+    "citcom_gpu_heat_flux_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _D, ctypes.c_void_p,
+                                                    ctypes.c_void_p, _D, _D]),
 }
 
 _lib = None
@@ -191,6 +193,25 @@ def load_library(path: str = LIB_PATH):
             fn.argtypes = args
         _lib = lib
     return _lib
+
+
+NOALLOC_MAX_NODES = 274625
+NOALLOC_MAX_ELEMENTS = 262144
+
+
+def heat_flux_noalloc(nox: int, noy: int, noz: int, dimen, dT: int, dV: int):
+    """Nusselt numbers (top, bottom) from device-resident T (nno) and V
+    (3*nno) given as raw device addresses, without any device allocation:
+    for callers that cannot allocate (see include/citcom_gb300.h).  Raises
+    for meshes above NOALLOC_MAX_NODES / NOALLOC_MAX_ELEMENTS."""
+    lib = load_library()
+    dim = (ctypes.c_double * 3)(*[float(x) for x in dimen])
+    a, b = ctypes.c_double(), ctypes.c_double()
+    rc = lib.citcom_gpu_heat_flux_noalloc(nox, noy, noz, dim, ctypes.c_void_p(dT), ctypes.c_void_p(dV),
+                                          ctypes.byref(a), ctypes.byref(b))
+    if rc != 0:
+        raise CitcomGPUError(f"citcom_gpu_heat_flux_noalloc failed ({_ERRORS.get(rc, rc)})")
+    return a.value, b.value
 
 
 def _dp(a: np.ndarray):

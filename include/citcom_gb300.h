@@ -182,6 +182,26 @@ int citcom_gpu_op_solve_del2_u(citcom_gpu *h, double *d0, const double *F, doubl
 /* BI (neq, 1/diag K) and BPI (nel) of level lev as the solver holds them */
 int citcom_gpu_op_diagonals(citcom_gpu *h, int lev, double *BI, double *BPI);
 
+/* Surface Nusselt numbers of heat_flux (Process_buoyancy.c:63) for callers
+ * that cannot allocate device memory.  No counterpart in the reference.
+ * Everything it needs beyond its inputs and outputs lives in one fixed device
+ * array inside the library (about 4.4 MB, held by every GPU that loads the
+ * library until the process exits); it calls no cudaMalloc/cudaFree and needs
+ * no handle.  dT (nno) and dV (3*nno, layout of V above) are DEVICE pointers
+ * of a nox*noy*noz box of size dimen; nut/nub receive the results on the
+ * host.  Meshes above CITCOM_GPU_NOALLOC_MAX_NODES nodes or
+ * CITCOM_GPU_NOALLOC_MAX_ELEMENTS elements are rejected with
+ * CITCOM_GPU_ERR_ARG and a message on stderr.  Runs on the legacy default
+ * stream and returns after the result is on the host.  The first call on a
+ * device looks up the array's device address (once per device, with that
+ * device current), so make the first call before any stream capture.  All
+ * calls share the one array: calls that overlap on the GPU race and must be
+ * serialised by the caller. */
+#define CITCOM_GPU_NOALLOC_MAX_NODES 274625
+#define CITCOM_GPU_NOALLOC_MAX_ELEMENTS 262144
+int citcom_gpu_heat_flux_noalloc(int nox, int noy, int noz, const double dimen[3], const double *dT, const double *dV,
+                                 double *nut, double *nub);
+
 #ifdef __cplusplus
 }
 #endif
