@@ -193,7 +193,7 @@ template <typename T> void gs_inner(citcom_gpu *h, MG<T> &B, int lev, T *d, cons
 // device time is measured live during every solve.
 template <typename T> void gs(citcom_gpu *h, MG<T> &B, int lev, T *d, const T *F, int cycles, int zero_start)
 {
-	const bool timed = (lev == h->L - 1) && h->n_gs_pairs < 4 && !gs_small_fits(h->lv[lev]);
+	const bool timed = (lev == h->L - 1) && h->n_gs_pairs < 4 && !gs_small_fits(h->lv[lev], sizeof(T));
 	// during stream capture, external records become event-record nodes of
 	// the graph; outside capture they are ordinary records
 	unsigned flags = 0;
@@ -228,7 +228,7 @@ template <typename T> void gs(citcom_gpu *h, MG<T> &B, int lev, T *d, const T *F
 template <typename T> void gs_inner(citcom_gpu *h, MG<T> &B, int lev, T *d, const T *F, int cycles, int zero_start)
 {
 	const Lvl &L = h->lv[lev];
-	if(gs_small_fits(L))
+	if(gs_small_fits(L, sizeof(T)))
 	{
 		launch_gs_small<T>(h->st, L, B.K[lev], B.BI[lev], F, d, cycles, zero_start);
 		return;

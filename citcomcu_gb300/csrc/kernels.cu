@@ -437,25 +437,42 @@ __global__ void __launch_bounds__(SLOT_THREADS) k_gs_colour(Lvl L, const T *__re
 // node by node) in one CTA of 32 warps: a warp relaxes one node at a time,
 // lane s < 27 handling neighbour slot s (9 coefficients and 3 neighbour
 // values), the 27 partial rows added by warp shuffles; lanes 0..2 then apply
-// the node update.  SMEM: stencil, 1/diag, F and d staged in shared memory
-// (coarsest levels); otherwise coefficients come through L2 and each warp
-// processes up to GSW nodes at once to overlap their loads.
+// the node update.  The node and neighbour indices of every (position, slot)
+// are computed once into a shared-memory table, so a colour phase is loads,
+// 9 FMAs and the shuffles.  SMEM: stencil, 1/diag, F and d staged in shared
+// memory as well (coarsest levels); otherwise coefficients and vectors come
+// through L2 and each warp processes up to GSW nodes at once.
 constexpr int GS_WARPS = 32;
 constexpr int GSW = 3;
 template <typename T, bool SMEM>
 __global__ void __launch_bounds__(GS_WARPS * 32) k_gs_small(Lvl L, const T *__restrict__ K, const T *__restrict__ BI,
                                                             const T *__restrict__ F, T *d, int cycles, int zero_start)
 {
-	pdl_begin();
 	extern __shared__ __align__(16) unsigned char smem_raw[];
+	// neighbour table: nb[28 * p + s] = neighbour node of slot s (clamped), nb[28 * p + 27] = node of position p
+	int *nb = reinterpret_cast<int *>(smem_raw);
+	T *tail = reinterpret_cast<T *>(smem_raw + (((size_t)28 * L.nno * sizeof(int) + 15) / 16) * 16);
+	for(int t = threadIdx.x; t < 28 * L.nno; t += blockDim.x)
+	{
+		const int p = t / 28, s = t - 28 * p;
+		int c, x, y, z;
+		pos_xyz(L, p, c, x, y, z);
+		if(s == 27)
+			nb[t] = cg_node(L, x, y, z);
+		else
+		{
+			const int dz = s % 3 - 1, dx = (s / 3) % 3 - 1, dy = s / 9 - 1;
+			nb[t] = cg_node(L, clampi(x + dx, 0, L.nox - 1), clampi(y + dy, 0, L.noy - 1), clampi(z + dz, 0, L.noz - 1));
+		}
+	}
 	const T *Kp = K, *Bp = BI, *Fp = F;
 	T *dp = d;
 	if(SMEM)
 	{
-		T *sK = reinterpret_cast<T *>(smem_raw);  // 243 * nno
-		T *sB = sK + (size_t)243 * L.nno;          // 3 * nno
-		T *sF = sB + (size_t)3 * L.nno;            // neq
-		T *sd = sF + L.neq;                        // neq
+		T *sK = tail;                        // 243 * nno
+		T *sB = sK + (size_t)243 * L.nno;    // 3 * nno
+		T *sF = sB + (size_t)3 * L.nno;      // neq
+		T *sd = sF + L.neq;                  // neq
 		for(int i = threadIdx.x; i < 243 * L.nno; i += blockDim.x)
 			sK[i] = K[i];
 		for(int i = threadIdx.x; i < 3 * L.nno; i += blockDim.x)
@@ -476,7 +493,7 @@ __global__ void __launch_bounds__(GS_WARPS * 32) k_gs_small(Lvl L, const T *__re
 	__syncthreads();
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	const int s = lane < 27 ? lane : 13;  // idle lanes shadow the centre slot with zero weight
-	const int dz = s % 3 - 1, dx = (s / 3) % 3 - 1, dy = s / 9 - 1;
+	const T wgt = lane < 27 ? (T)1 : (T)0;
 	for(int cyc = 0; cyc < cycles; ++cyc)
 		for(int c = 0; c < 8; ++c)
 		{
@@ -494,27 +511,27 @@ __global__ void __launch_bounds__(GS_WARPS * 32) k_gs_small(Lvl L, const T *__re
 					pp[w] = 0;
 					if(q < nc)
 					{
-						int x, y, z;
-						cg_decode(L, c, q, x, y, z);
 						const int p = L.coff[c] + q;
-						const int m = cg_node(L, clampi(x + dx, 0, L.nox - 1), clampi(y + dy, 0, L.noy - 1),
-						                      clampi(z + dz, 0, L.noz - 1));
+						const int m = nb[28 * p + s];
 						const T *kc = Kp + (size_t)243 * p + 9 * s;
 						const T u0 = dp[3 * m], u1 = dp[3 * m + 1], u2 = dp[3 * m + 2];
-						const T wgt = lane < 27 ? (T)1 : (T)0;
 						r[w][0] = wgt * (kc[0] * u0 + kc[1] * u1 + kc[2] * u2);
 						r[w][1] = wgt * (kc[3] * u0 + kc[4] * u1 + kc[5] * u2);
 						r[w][2] = wgt * (kc[6] * u0 + kc[7] * u1 + kc[8] * u2);
-						nn[w] = cg_node(L, x, y, z);
+						nn[w] = nb[28 * p + 27];
 						pp[w] = p;
 					}
 				}
 #pragma unroll
 				for(int w = 0; w < GSW; ++w)
+				{
+					if(q0 + w * GS_WARPS >= nc)
+						break;  // warp-uniform
 #pragma unroll
 					for(int i = 0; i < 3; ++i)
 						for(int o = 16; o > 0; o >>= 1)
 							r[w][i] += __shfl_xor_sync(0xffffffffu, r[w][i], o);
+				}
 #pragma unroll
 				for(int w = 0; w < GSW; ++w)
 					if(nn[w] >= 0 && lane < 3)
@@ -1513,26 +1530,32 @@ template <typename T> void launch_gs_colour(cudaStream_t st, const Lvl &L, const
 	}
 }
 
-bool gs_small_fits(const Lvl &L) { return L.aos != 0; }
+// The single-CTA smoother serves the small FP32 levels.  In FP64 the one SM
+// it runs on is limited by GB300's FP64 rate, so FP64 small levels use the
+// all-SM colour launches instead.
+bool gs_small_fits(const Lvl &L, size_t word) { return L.aos != 0 && word == sizeof(float); }
+
+static size_t gs_table_bytes(const Lvl &L) { return (((size_t)28 * L.nno * sizeof(int) + 15) / 16) * 16; }
+static size_t gs_smem_bytes(const Lvl &L, size_t word) { return gs_table_bytes(L) + word * ((size_t)246 * L.nno + 2 * (size_t)L.neq); }
+constexpr size_t GS_SMEM_MAX = 200 * 1024;
 
 int kernels_init()
 {
 	// opt in to large dynamic shared memory once, outside any stream capture
-	cudaError_t a = cudaFuncSetAttribute(k_gs_small<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-	cudaError_t b = cudaFuncSetAttribute(k_gs_small<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+	cudaError_t a = cudaFuncSetAttribute(k_gs_small<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GS_SMEM_MAX);
+	cudaError_t b = cudaFuncSetAttribute(k_gs_small<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GS_SMEM_MAX);
 	return (a == cudaSuccess && b == cudaSuccess) ? 0 : -1;
 }
-
-static size_t gs_smem_bytes(const Lvl &L, size_t word) { return word * ((size_t)246 * L.nno + 2 * (size_t)L.neq); }
 
 template <typename T>
 void launch_gs_small(cudaStream_t st, const Lvl &L, const T *K, const T *BI, const T *F, T *d, int cycles, int zero_start)
 {
 	const size_t bytes = gs_smem_bytes(L, sizeof(T));
-	if(bytes <= 200 * 1024)
+	if(bytes <= GS_SMEM_MAX)
 		launch_k_smem(k_gs_small<T, true>, dim3(1), dim3(GS_WARPS * 32), bytes, st, L, K, BI, F, d, cycles, zero_start);
 	else
-		launch_k(k_gs_small<T, false>, 1, GS_WARPS * 32, st, L, K, BI, F, d, cycles, zero_start);
+		launch_k_smem(k_gs_small<T, false>, dim3(1), dim3(GS_WARPS * 32), gs_table_bytes(L), st, L, K, BI, F, d, cycles,
+		              zero_start);
 }
 
 template <typename T> void launch_project(cudaStream_t st, const Lvl &Lf, const Lvl &Lc, const T *AU, T *AD)

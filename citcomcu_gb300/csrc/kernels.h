@@ -52,7 +52,7 @@ void launch_gs_small(cudaStream_t st, const Lvl &L, const T *K, const T *BI, con
 template <typename T> void launch_project(cudaStream_t st, const Lvl &Lf, const Lvl &Lc, const T *AU, T *AD);
 template <typename T> void launch_interp(cudaStream_t st, const Lvl &Lc, const Lvl &Lf, const T *AD, T *AU);
 template <typename T> void launch_vel_update(cudaStream_t st, int n, T *vel, const T *del, T *res, const T *AU, const double *alpha_num_den, int update_res);
-bool gs_small_fits(const Lvl &L);
+bool gs_small_fits(const Lvl &L, size_t word);
 
 // FP64 element operators
 void launch_div(cudaStream_t st, const Lvl &L, const Geo *geo, const double *U, double *divU);
