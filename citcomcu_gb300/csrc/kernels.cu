@@ -321,10 +321,10 @@ template <typename T> struct SlotSmem
 
 // Computes r_i = sum_m K_{n,m}[i][:] u_m for the NB nodes at colour-major
 // positions p0 .. p0+cnt-1 (all of one colour); on return the threads
-// t < 3*cnt hold (node t/3, row t%3) in `row` and its node index in `n`.
-// Every thread of the block must call it (it synchronises).
+// t < 3*cnt hold (node t/3, row t%3) in `row`.  Every thread of the block
+// must call it (it synchronises).
 template <typename T, bool STREAM>
-__device__ __forceinline__ void block_rows(const Lvl &L, const T *K, const T *u, int p0, int cnt, T *part, T &row, int &n)
+__device__ __forceinline__ void block_rows(const Lvl &L, const T *K, const T *u, int p0, int cnt, T *part, T &row)
 {
 	const int ln = threadIdx.x % NB, s = threadIdx.x / NB;
 	if(ln < cnt)
@@ -339,7 +339,6 @@ __device__ __forceinline__ void block_rows(const Lvl &L, const T *K, const T *u,
 	}
 	__syncthreads();
 	row = 0;
-	n = 0;
 	if((int)threadIdx.x < 3 * cnt)
 	{
 		const int q = threadIdx.x / 3, i = threadIdx.x % 3;
@@ -348,13 +347,19 @@ __device__ __forceinline__ void block_rows(const Lvl &L, const T *K, const T *u,
 		for(int ss = 0; ss < 27; ++ss)
 			acc += part[(ss * 3 + i) * NB + q];
 		row = acc;
-		int c, x, y, z;
-		pos_xyz(L, p0 + q, c, x, y, z);
-		n = cg_node(L, x, y, z);
 	}
 }
 
+// node index of the (node, row) owner thread t < 3*cnt of a slot block
+__device__ __forceinline__ int row_owner_node(const Lvl &L, int p0)
+{
+	int c, x, y, z;
+	pos_xyz(L, p0 + (int)threadIdx.x / 3, c, x, y, z);
+	return cg_node(L, x, y, z);
+}
+
 // MODE 0: out = K u;  MODE 1: out = f - K u.  One block per NB nodes of a colour; grid (blocks, colours).
+// The owner threads fetch their f before the gather so that its latency overlaps.
 template <typename T, int MODE>
 __global__ void __launch_bounds__(SLOT_THREADS) k_kmul(Lvl L, const T *__restrict__ K, const T *__restrict__ u, const T *__restrict__ f,
                                                        T *__restrict__ out)
@@ -367,14 +372,21 @@ __global__ void __launch_bounds__(SLOT_THREADS) k_kmul(Lvl L, const T *__restric
 	if(q0 >= nc)
 		return;
 	const int cnt = min(NB, nc - q0);
-	T r;
-	int n;
-	block_rows<T, true>(L, K, u, L.coff[c] + q0, cnt, sm.part, r, n);
-	if((int)threadIdx.x < 3 * cnt)
+	const int p0 = L.coff[c] + q0;
+	const bool owner = (int)threadIdx.x < 3 * cnt;
+	const int i = threadIdx.x % 3;
+	int n = 0;
+	T fi = 0;
+	if(owner)
 	{
-		const int i = threadIdx.x % 3;
-		out[3 * n + i] = (MODE == 1) ? f[3 * n + i] - r : r;
+		n = row_owner_node(L, p0);
+		if(MODE == 1)
+			fi = f[3 * n + i];
 	}
+	T r;
+	block_rows<T, true>(L, K, u, p0, cnt, sm.part, r);
+	if(owner)
+		out[3 * n + i] = (MODE == 1) ? fi - r : r;
 }
 
 // a.b and a.a in FP64 (a = AU, b = res for the line search of multi_grid,
@@ -410,7 +422,9 @@ __global__ void k_vel_update(int n, T *__restrict__ vel, const T *__restrict__ d
 
 // One Gauss-Seidel colour: d_n += (F_n - sum_m K_{n,m} d_m) o BI_n.  The three
 // rows of a node are relaxed together from the same d (the reference's
-// "Jacobi at a node"): all reads happen before the block's barrier.
+// "Jacobi at a node"): all reads happen before the block's barrier.  The
+// owner of (node, row) fetches F, 1/diag and its own d before the gather, so
+// the update needs no second memory round trip.
 template <typename T>
 __global__ void __launch_bounds__(SLOT_THREADS) k_gs_colour(Lvl L, const T *__restrict__ K, const T *__restrict__ BI,
                                                             const T *__restrict__ F, T *d, int c)
@@ -423,14 +437,21 @@ __global__ void __launch_bounds__(SLOT_THREADS) k_gs_colour(Lvl L, const T *__re
 		return;
 	const int cnt = min(NB, nc - q0);
 	const int p0 = L.coff[c] + q0;
-	T r;
-	int n;
-	block_rows<T, true>(L, K, d, p0, cnt, sm.part, r, n);
-	if((int)threadIdx.x < 3 * cnt)
+	const bool owner = (int)threadIdx.x < 3 * cnt;
+	const int i = threadIdx.x % 3;
+	int n = 0;
+	T fi = 0, bi = 0, di = 0;
+	if(owner)
 	{
-		const int q = threadIdx.x / 3, i = threadIdx.x % 3;
-		d[3 * n + i] += (F[3 * n + i] - r) * BI[3 * (size_t)(p0 + q) + i];
+		n = row_owner_node(L, p0);
+		fi = F[3 * n + i];
+		bi = BI[3 * (size_t)(p0 + (int)threadIdx.x / 3) + i];
+		di = d[3 * n + i];
 	}
+	T r;
+	block_rows<T, true>(L, K, d, p0, cnt, sm.part, r);
+	if(owner)
+		d[3 * n + i] = di + (fi - r) * bi;
 }
 
 // All sweeps and colours of one gauss_seidel call on a small level (stored
@@ -439,12 +460,13 @@ __global__ void __launch_bounds__(SLOT_THREADS) k_gs_colour(Lvl L, const T *__re
 // values), the 27 partial rows added by warp shuffles; lanes 0..2 then apply
 // the node update.  The node and neighbour indices of every (position, slot)
 // are computed once into a shared-memory table, so a colour phase is loads,
-// 9 FMAs and the shuffles.  SMEM: stencil, 1/diag, F and d staged in shared
-// memory as well (coarsest levels); otherwise coefficients and vectors come
-// through L2 and each warp processes up to GSW nodes at once.
+// 9 FMAs and the shuffles.  STAGE 2: stencil, 1/diag, F and d staged in
+// shared memory as well (coarsest levels); STAGE 1: 1/diag, F and d staged,
+// the stencil read through L2 (it does not depend on the colour phase, so a
+// phase costs one L2 round trip); each warp processes up to GSW nodes at once.
 constexpr int GS_WARPS = 32;
 constexpr int GSW = 3;
-template <typename T, bool SMEM>
+template <typename T, int STAGE>
 __global__ void __launch_bounds__(GS_WARPS * 32) k_gs_small(Lvl L, const T *__restrict__ K, const T *__restrict__ BI,
                                                             const T *__restrict__ F, T *d, int cycles, int zero_start)
 {
@@ -467,14 +489,18 @@ __global__ void __launch_bounds__(GS_WARPS * 32) k_gs_small(Lvl L, const T *__re
 	}
 	const T *Kp = K, *Bp = BI, *Fp = F;
 	T *dp = d;
-	if(SMEM)
+	if(STAGE > 0)
 	{
-		T *sK = tail;                        // 243 * nno
-		T *sB = sK + (size_t)243 * L.nno;    // 3 * nno
-		T *sF = sB + (size_t)3 * L.nno;      // neq
-		T *sd = sF + L.neq;                  // neq
-		for(int i = threadIdx.x; i < 243 * L.nno; i += blockDim.x)
-			sK[i] = K[i];
+		T *sK = tail;                                         // 243 * nno when STAGE == 2
+		T *sB = sK + (STAGE == 2 ? (size_t)243 * L.nno : 0);  // 3 * nno
+		T *sF = sB + (size_t)3 * L.nno;                       // neq
+		T *sd = sF + L.neq;                                   // neq
+		if(STAGE == 2)
+		{
+			for(int i = threadIdx.x; i < 243 * L.nno; i += blockDim.x)
+				sK[i] = K[i];
+			Kp = sK;
+		}
 		for(int i = threadIdx.x; i < 3 * L.nno; i += blockDim.x)
 			sB[i] = BI[i];
 		for(int i = threadIdx.x; i < L.neq; i += blockDim.x)
@@ -482,7 +508,6 @@ __global__ void __launch_bounds__(GS_WARPS * 32) k_gs_small(Lvl L, const T *__re
 			sF[i] = F[i];
 			sd[i] = zero_start ? (T)0 : d[i];
 		}
-		Kp = sK;
 		Bp = sB;
 		Fp = sF;
 		dp = sd;
@@ -542,7 +567,7 @@ __global__ void __launch_bounds__(GS_WARPS * 32) k_gs_small(Lvl L, const T *__re
 			}
 			__syncthreads();
 		}
-	if(SMEM)
+	if(STAGE > 0)
 		for(int i = threadIdx.x; i < L.neq; i += blockDim.x)
 			d[i] = dp[i];
 }
@@ -1533,29 +1558,38 @@ template <typename T> void launch_gs_colour(cudaStream_t st, const Lvl &L, const
 // The single-CTA smoother serves the small FP32 levels.  In FP64 the one SM
 // it runs on is limited by GB300's FP64 rate, so FP64 small levels use the
 // all-SM colour launches instead.
-bool gs_small_fits(const Lvl &L, size_t word) { return L.aos != 0 && word == sizeof(float); }
+bool gs_small_fits(const Lvl &L, size_t word)
+{
+	return L.aos != 0 && word == sizeof(float) && (((size_t)28 * L.nno * sizeof(int) + 15) / 16) * 16 <= 200 * 1024;
+}
 
 static size_t gs_table_bytes(const Lvl &L) { return (((size_t)28 * L.nno * sizeof(int) + 15) / 16) * 16; }
-static size_t gs_smem_bytes(const Lvl &L, size_t word) { return gs_table_bytes(L) + word * ((size_t)246 * L.nno + 2 * (size_t)L.neq); }
+static size_t gs_smem_bytes(const Lvl &L, size_t word, int stage)
+{
+	return gs_table_bytes(L) + word * ((stage == 2 ? (size_t)243 * L.nno : 0) + (stage > 0 ? 3 * (size_t)L.nno + 2 * (size_t)L.neq : 0));
+}
 constexpr size_t GS_SMEM_MAX = 200 * 1024;
 
 int kernels_init()
 {
 	// opt in to large dynamic shared memory once, outside any stream capture
-	cudaError_t a = cudaFuncSetAttribute(k_gs_small<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GS_SMEM_MAX);
-	cudaError_t b = cudaFuncSetAttribute(k_gs_small<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GS_SMEM_MAX);
-	return (a == cudaSuccess && b == cudaSuccess) ? 0 : -1;
+	cudaError_t e[3];
+	e[0] = cudaFuncSetAttribute(k_gs_small<float, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GS_SMEM_MAX);
+	e[1] = cudaFuncSetAttribute(k_gs_small<float, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GS_SMEM_MAX);
+	e[2] = cudaFuncSetAttribute(k_gs_small<float, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GS_SMEM_MAX);
+	return (e[0] == cudaSuccess && e[1] == cudaSuccess && e[2] == cudaSuccess) ? 0 : -1;
 }
 
 template <typename T>
 void launch_gs_small(cudaStream_t st, const Lvl &L, const T *K, const T *BI, const T *F, T *d, int cycles, int zero_start)
 {
-	const size_t bytes = gs_smem_bytes(L, sizeof(T));
-	if(bytes <= GS_SMEM_MAX)
-		launch_k_smem(k_gs_small<T, true>, dim3(1), dim3(GS_WARPS * 32), bytes, st, L, K, BI, F, d, cycles, zero_start);
+	const dim3 g(1), b(GS_WARPS * 32);
+	if(gs_smem_bytes(L, sizeof(T), 2) <= GS_SMEM_MAX)
+		launch_k_smem(k_gs_small<T, 2>, g, b, gs_smem_bytes(L, sizeof(T), 2), st, L, K, BI, F, d, cycles, zero_start);
+	else if(gs_smem_bytes(L, sizeof(T), 1) <= GS_SMEM_MAX)
+		launch_k_smem(k_gs_small<T, 1>, g, b, gs_smem_bytes(L, sizeof(T), 1), st, L, K, BI, F, d, cycles, zero_start);
 	else
-		launch_k_smem(k_gs_small<T, false>, dim3(1), dim3(GS_WARPS * 32), gs_table_bytes(L), st, L, K, BI, F, d, cycles,
-		              zero_start);
+		launch_k_smem(k_gs_small<T, 0>, g, b, gs_table_bytes(L), st, L, K, BI, F, d, cycles, zero_start);
 }
 
 template <typename T> void launch_project(cudaStream_t st, const Lvl &Lf, const Lvl &Lc, const T *AU, T *AD)
