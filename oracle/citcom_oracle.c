@@ -34,6 +34,10 @@ typedef struct level
 	double g[24];         /* divergence operator of one element (get_elt_g) */
 	double *evi;          /* viscosity at the 8 Gauss points of each element */
 	double *K;            /* assembled block stencil: node*243 + slot*9 + 3i + j */
+	double *H;            /* half stencil of the reference (construct_node_maps): per node the
+	                         self block and the 13 lower-numbered neighbours' blocks, 14*9 words,
+	                         with the neighbour index of each block in HI */
+	int *HI;
 	double *BI;           /* 1 / diag(K) (unmasked) */
 	double *BPI;          /* pressure preconditioner */
 	double *mass;         /* 1 / lumped mass */
@@ -234,6 +238,8 @@ oracle *oracle_create(const oracle_params *p)
 		lv->h[2] = p->dimen[2] / lv->elz;
 		lv->evi = (double *)xcalloc((size_t)lv->nel * 8, sizeof(double));
 		lv->K = (double *)xcalloc((size_t)lv->nno * 243, sizeof(double));
+		lv->H = (double *)xcalloc((size_t)lv->nno * 126, sizeof(double));
+		lv->HI = (int *)xcalloc((size_t)lv->nno * 14, sizeof(int));
 		lv->BI = (double *)xcalloc((size_t)lv->neq + 2, sizeof(double));
 		lv->BPI = (double *)xcalloc((size_t)lv->nel, sizeof(double));
 		lv->mass = (double *)xcalloc((size_t)lv->nno, sizeof(double));
@@ -297,6 +303,8 @@ void oracle_destroy(oracle *o)
 		level *lv = &o->lv[l];
 		free(lv->evi);
 		free(lv->K);
+		free(lv->H);
+		free(lv->HI);
 		free(lv->BI);
 		free(lv->BPI);
 		free(lv->mass);
@@ -611,6 +619,34 @@ void oracle_construct_stiffness(oracle *o)
 		}
 		for(i = 0; i < l->neq; i++)
 			l->BI[i] = 1.0 / l->BI[i];
+		/* half stencil in the order of construct_node_maps (Construct_arrays.c:280-356):
+		   self first, then the neighbours with smaller node number, y-1 plane, x-1 row, z-1 */
+		{
+			int n;
+			for(n = 0; n < l->nno; n++)
+			{
+				int z = n % l->noz, x = (n / l->noz) % l->nox, y = n / (l->noz * l->nox);
+				int dx, dy, dz, cnt = 0, q;
+				for(q = 0; q < 14; q++)
+					l->HI[14 * n + q] = -1;
+				memcpy(l->H + (size_t)126 * n, l->K + (size_t)243 * n + 9 * slot_of(0, 0, 0), 9 * sizeof(double));
+				l->HI[14 * n] = n;
+				cnt = 1;
+				for(dy = -1; dy <= 0; dy++)
+					for(dx = -1; dx <= 1; dx++)
+						for(dz = -1; dz <= 1; dz++)
+						{
+							if(dy == 0 && (dx > 0 || (dx == 0 && dz >= 0)))
+								continue;
+							if(y + dy < 0 || x + dx < 0 || x + dx >= l->nox || z + dz < 0 || z + dz >= l->noz)
+								continue;
+							memcpy(l->H + (size_t)126 * n + 9 * cnt, l->K + (size_t)243 * n + 9 * slot_of(dx, dy, dz),
+							       9 * sizeof(double));
+							l->HI[14 * n + cnt] = nidx(l, x + dx, y + dy, z + dz);
+							cnt++;
+						}
+			}
+		}
 		for(e = 0; e < l->nel; e++)
 		{
 			l->BPI[e] = 1.0;
@@ -662,11 +698,50 @@ static inline void row_mul(const level *l, int n, const double *u, double out[3]
 	}
 }
 
-/* n_assemble_del2_u (Element_calculations.c:552-621) */
+/* n_assemble_del2_u (Element_calculations.c:552-621): in the reference's
+ * order, each node gathers its lower neighbours' contributions and scatters
+ * its own value through the transposed blocks of its half stencil; in the
+ * colour mode (the GPU's arithmetic) every row is a full 27-block gather */
 void oracle_kmul(oracle *o, int lev, const double *u, double *Au, int strip)
 {
 	const level *l = &o->lv[lev];
 	int n;
+	if(!o->p.gs_colored)
+	{
+		int i, q;
+		for(i = 0; i < l->neq; i++)
+			Au[i] = 0.0;
+		for(n = 0; n < l->nno; n++)
+		{
+			const double *Hn = l->H + (size_t)126 * n;
+			const int *In = l->HI + 14 * n;
+			const double u0 = u[3 * n], u1 = u[3 * n + 1], u2 = u[3 * n + 2];
+			for(q = 1; q < 14; q++)
+			{
+				const int m = In[q];
+				const double *b = Hn + 9 * q;
+				if(m < 0)
+					break;
+				Au[3 * n] += b[0] * u[3 * m] + b[1] * u[3 * m + 1] + b[2] * u[3 * m + 2];
+				Au[3 * n + 1] += b[3] * u[3 * m] + b[4] * u[3 * m + 1] + b[5] * u[3 * m + 2];
+				Au[3 * n + 2] += b[6] * u[3 * m] + b[7] * u[3 * m + 1] + b[8] * u[3 * m + 2];
+			}
+			for(q = 0; q < 14; q++)
+			{
+				const int m = In[q];
+				const double *b = Hn + 9 * q;
+				if(m < 0)
+					break;
+				Au[3 * m] += b[0] * u0 + b[3] * u1 + b[6] * u2;
+				Au[3 * m + 1] += b[1] * u0 + b[4] * u1 + b[7] * u2;
+				Au[3 * m + 2] += b[2] * u0 + b[5] * u1 + b[8] * u2;
+			}
+		}
+		Au[l->neq] = Au[l->neq + 1] = 0.0;
+		if(strip)
+			oracle_strip_bcs(o, lev, Au);
+		return;
+	}
 	for(n = 0; n < l->nno; n++)
 		row_mul(l, n, u, Au + 3 * n);
 	Au[l->neq] = Au[l->neq + 1] = 0.0;
@@ -701,49 +776,36 @@ void oracle_gauss_seidel(oracle *o, int lev, double *d0, const double *F, double
 	{
 		if(!o->p.gs_colored)
 		{
-			int n;
+			int n, q, d;
 			for(i = 0; i <= neq + 1; i++)
 				temp[i] = 0.0;
 			for(n = 0; n < l->nno; n++)
 			{
-				int z = n % l->noz, x = (n / l->noz) % l->nox, y = n / (l->noz * l->nox);
-				int dx, dy, dz, d;
-				const double *Kn = l->K + (size_t)n * 243;
+				const double *Hn = l->H + (size_t)126 * n;
+				const int *In = l->HI + 14 * n;
 				double t[3];
 				/* gather lower neighbours' fresh increments: K_{n,m} temp_m */
-				for(dy = -1; dy <= 0; dy++)
-					for(dx = -1; dx <= 1; dx++)
-						for(dz = -1; dz <= 1; dz++)
-						{
-							int m;
-							const double *blk;
-							if(dy == 0 && (dx > 0 || (dx == 0 && dz >= 0)))
-								continue;
-							if(y + dy < 0 || x + dx < 0 || x + dx >= l->nox || z + dz < 0 || z + dz >= l->noz)
-								continue;
-							m = nidx(l, x + dx, y + dy, z + dz);
-							blk = Kn + 9 * slot_of(dx, dy, dz);
-							for(d = 0; d < 3; d++)
-								Ad[3 * n + d] += blk[3 * d] * temp[3 * m] + blk[3 * d + 1] * temp[3 * m + 1] + blk[3 * d + 2] * temp[3 * m + 2];
-						}
+				for(q = 1; q < 14; q++)
+				{
+					const int m = In[q];
+					const double *b = Hn + 9 * q;
+					if(m < 0)
+						break;
+					for(d = 0; d < 3; d++)
+						Ad[3 * n + d] += b[3 * d] * temp[3 * m] + b[3 * d + 1] * temp[3 * m + 1] + b[3 * d + 2] * temp[3 * m + 2];
+				}
 				for(d = 0; d < 3; d++)
 					t[d] = temp[3 * n + d] = (F[3 * n + d] - Ad[3 * n + d]) * l->BI[3 * n + d];
-				/* scatter to self and lower neighbours: Ad_m += K_{m,n} temp_n */
-				for(dy = -1; dy <= 0; dy++)
-					for(dx = -1; dx <= 1; dx++)
-						for(dz = -1; dz <= 1; dz++)
-						{
-							int m;
-							const double *blk;
-							if(dy == 0 && (dx > 0 || (dx == 0 && dz > 0)))
-								continue;
-							if(y + dy < 0 || x + dx < 0 || x + dx >= l->nox || z + dz < 0 || z + dz >= l->noz)
-								continue;
-							m = nidx(l, x + dx, y + dy, z + dz);
-							blk = l->K + (size_t)m * 243 + 9 * slot_of(-dx, -dy, -dz);
-							for(d = 0; d < 3; d++)
-								Ad[3 * m + d] += blk[3 * d] * t[0] + blk[3 * d + 1] * t[1] + blk[3 * d + 2] * t[2];
-						}
+				/* scatter to self and lower neighbours through the transposed blocks */
+				for(q = 0; q < 14; q++)
+				{
+					const int m = In[q];
+					const double *b = Hn + 9 * q;
+					if(m < 0)
+						break;
+					for(d = 0; d < 3; d++)
+						Ad[3 * m + d] += b[d] * t[0] + b[3 + d] * t[1] + b[6 + d] * t[2];
+				}
 				for(d = 0; d < 3; d++)
 					d0[3 * n + d] += t[d];
 			}
