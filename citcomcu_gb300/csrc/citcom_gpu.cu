@@ -13,6 +13,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/citcom_gb300.h"
@@ -54,6 +55,7 @@ struct citcom_gpu
 	double *BI64[CITCOM_MAX_LEVELS];
 	float *K32[CITCOM_MAX_LEVELS];
 	float *BI32[CITCOM_MAX_LEVELS];
+	float4 *Kt32[CITCOM_MAX_LEVELS];  // padded FP32 stencil of the levels k_gs_tiny smooths, else null
 	double *BPI;
 	MG<double> mg64;
 	MG<float> mg32;
@@ -78,6 +80,7 @@ struct citcom_gpu
 	bool verbose;
 	bool no_graph;
 	bool level_timing;            // CITCOM_GPU_LEVEL_TIMING: time every smoother call (no graph)
+	bool no_tiny;                 // CITCOM_GPU_NO_TINY: coarsest FP32 levels use k_gs_small instead of k_gs_tiny
 	double lt_ms[CITCOM_MAX_LEVELS];
 	long lt_calls[CITCOM_MAX_LEVELS];
 	long lt_sweeps[CITCOM_MAX_LEVELS];
@@ -228,6 +231,12 @@ template <typename T> void gs(citcom_gpu *h, MG<T> &B, int lev, T *d, const T *F
 template <typename T> void gs_inner(citcom_gpu *h, MG<T> &B, int lev, T *d, const T *F, int cycles, int zero_start)
 {
 	const Lvl &L = h->lv[lev];
+	if constexpr(std::is_same<T, float>::value)
+		if(h->Kt32[lev] && !h->no_tiny)
+		{
+			launch_gs_tiny(h->st, L, h->Kt32[lev], B.BI[lev], F, d, cycles, zero_start);
+			return;
+		}
 	if(gs_small_fits(L, sizeof(T)))
 	{
 		launch_gs_small<T>(h->st, L, B.K[lev], B.BI[lev], F, d, cycles, zero_start);
@@ -464,6 +473,8 @@ int construct_stiffness(citcom_gpu *h)
 		const bool need32 = (c.precision == CITCOM_GPU_MIXED);
 		launch_assemble(h->st, h->lv[l], h->geo[l], h->evi[l], c.aug_lagr, c.aug_number, need64 ? h->K64[l] : nullptr,
 		                need32 ? h->K32[l] : nullptr, need64 ? h->BI64[l] : nullptr, need32 ? h->BI32[l] : nullptr);
+		if(h->Kt32[l])
+			launch_tiny_stencil(h->st, h->lv[l], h->K32[l], h->Kt32[l]);
 	}
 	launch_bpi(h->st, h->lv[lmax], h->geo[lmax], h->BI64[lmax], h->BPI, c.precond);
 	CK(cudaGetLastError());
@@ -671,6 +682,8 @@ int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 		h->level_timing = t && t[0] && t[0] != '0';
 		if(h->level_timing)
 			h->no_graph = true;
+		const char *tn = getenv("CITCOM_GPU_NO_TINY");
+		h->no_tiny = tn && tn[0] && tn[0] != '0';
 		const char *q = getenv("CITCOM_GPU_NO_PDL");
 		if(q && q[0] && q[0] != '0')
 			g_use_pdl = 0;
@@ -726,10 +739,13 @@ int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 				TRYC(dalloc(h, &h->K64[l], (size_t)243 * L.npad));
 				TRYC(dalloc(h, &h->BI64[l], (size_t)3 * L.npad));
 			}
+			h->Kt32[l] = nullptr;
 			if(need32)
 			{
 				TRYC(dalloc(h, &h->K32[l], (size_t)243 * L.npad));
 				TRYC(dalloc(h, &h->BI32[l], (size_t)3 * L.npad));
+				if(gs_tiny_fits(L, sizeof(float)))
+					TRYC(dalloc(h, &h->Kt32[l], (size_t)63 * L.nno));
 			}
 			h->mg64.K[l] = h->K64[l];
 			h->mg64.BI[l] = h->BI64[l];
@@ -1106,11 +1122,35 @@ int citcom_gpu_op_gauss_seidel(citcom_gpu *h, int lev, double *d0, const double 
 {
 	TRY(check_handle(h));
 	TRY(check_level(h, lev));
-	if(h->cfg.precision != CITCOM_GPU_FP64)
-		return fail(h, CITCOM_GPU_ERR_STATE, "op_gauss_seidel is provided for the FP64 configuration");
 	if(!h->stiffness_ready)
 		return fail(h, CITCOM_GPU_ERR_STATE, "construct_stiffness_B_matrix has not been called");
 	const Lvl &L = h->lv[lev];
+	if(h->cfg.precision != CITCOM_GPU_FP64)
+	{
+		// mixed configuration: the FP32 smoother of a multigrid level
+		if(lev == h->L - 1)
+			return fail(h, CITCOM_GPU_ERR_ARG, "the finest level is smoothed in FP32 only inside multi_grid; use a coarser level");
+		MG<float> &B = h->mg32;
+		std::vector<float> f(L.neq), v(L.neq);
+		for(int i = 0; i < L.neq; ++i)
+		{
+			f[i] = (float)F[i];
+			v[i] = guess ? (float)d0[i] : 0.f;
+		}
+		TRY(h2d(h, B.rhs[lev], f.data(), sizeof(float) * L.neq));
+		TRY(h2d(h, B.vel[lev], v.data(), sizeof(float) * L.neq));
+		gs<float>(h, B, lev, B.vel[lev], B.rhs[lev], cycles, !guess);
+		launch_kmul<float>(h->st, L, B.K[lev], B.vel[lev], B.AU[lev]);
+		TRY(d2h(h, v.data(), B.vel[lev], sizeof(float) * L.neq));
+		TRY(d2h(h, f.data(), B.AU[lev], sizeof(float) * L.neq));
+		TRY(sync(h));
+		for(int i = 0; i < L.neq; ++i)
+		{
+			d0[i] = v[i];
+			Ad[i] = f[i];
+		}
+		return CITCOM_GPU_OK;
+	}
 	MG<double> &B = h->mg64;
 	TRY(h2d(h, B.rhs[lev], F, sizeof(double) * L.neq));
 	if(guess)

@@ -15,6 +15,7 @@
 //    block sums partials in block order.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 
@@ -290,12 +291,12 @@ __device__ __forceinline__ void slot_partial(const Lvl &L, const T *K, const T *
 	T k[9];  // k[3j + i] = K_{n,m}[i][j]
 	if(L.aos)
 	{
-		const T *kc = K + (size_t)243 * p + 9 * s;
+		const T *kc = K + (size_t)243 * p + s;
 #pragma unroll
 		for(int i = 0; i < 3; ++i)
 #pragma unroll
 			for(int j = 0; j < 3; ++j)
-				k[3 * j + i] = kc[3 * i + j];
+				k[3 * j + i] = kc[27 * (3 * i + j)];
 	}
 	else
 	{
@@ -470,6 +471,7 @@ template <typename T, int STAGE>
 __global__ void __launch_bounds__(GS_WARPS * 32) k_gs_small(Lvl L, const T *__restrict__ K, const T *__restrict__ BI,
                                                             const T *__restrict__ F, T *d, int cycles, int zero_start)
 {
+	pdl_begin();
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	// neighbour table: nb[28 * p + s] = neighbour node of slot s (clamped), nb[28 * p + 27] = node of position p
 	int *nb = reinterpret_cast<int *>(smem_raw);
@@ -497,7 +499,25 @@ __global__ void __launch_bounds__(GS_WARPS * 32) k_gs_small(Lvl L, const T *__re
 		T *sd = sF + L.neq;                                   // neq
 		if(STAGE == 2)
 		{
-			for(int i = threadIdx.x; i < 243 * L.nno; i += blockDim.x)
+			// 16-byte words, eight loads in flight per thread before the stores
+			// (K comes from cudaMalloc and sK is 16-byte aligned)
+			const int nk = 243 * L.nno;
+			const int n16 = (int)(((size_t)nk * sizeof(T)) / 16);
+			const uint4 *src = reinterpret_cast<const uint4 *>(K);
+			uint4 *dst = reinterpret_cast<uint4 *>(sK);
+			for(int b = threadIdx.x; b < n16; b += 8 * blockDim.x)
+			{
+				uint4 v[8];
+#pragma unroll
+				for(int k = 0; k < 8; ++k)
+					if(b + k * (int)blockDim.x < n16)
+						v[k] = __ldg(src + b + k * blockDim.x);
+#pragma unroll
+				for(int k = 0; k < 8; ++k)
+					if(b + k * (int)blockDim.x < n16)
+						dst[b + k * blockDim.x] = v[k];
+			}
+			for(int i = n16 * (int)(16 / sizeof(T)) + threadIdx.x; i < nk; i += blockDim.x)
 				sK[i] = K[i];
 			Kp = sK;
 		}
@@ -538,11 +558,11 @@ __global__ void __launch_bounds__(GS_WARPS * 32) k_gs_small(Lvl L, const T *__re
 					{
 						const int p = L.coff[c] + q;
 						const int m = nb[28 * p + s];
-						const T *kc = Kp + (size_t)243 * p + 9 * s;
+						const T *kc = Kp + (size_t)243 * p + s;
 						const T u0 = dp[3 * m], u1 = dp[3 * m + 1], u2 = dp[3 * m + 2];
-						r[w][0] = wgt * (kc[0] * u0 + kc[1] * u1 + kc[2] * u2);
-						r[w][1] = wgt * (kc[3] * u0 + kc[4] * u1 + kc[5] * u2);
-						r[w][2] = wgt * (kc[6] * u0 + kc[7] * u1 + kc[8] * u2);
+						r[w][0] = wgt * (kc[0] * u0 + kc[27] * u1 + kc[54] * u2);
+						r[w][1] = wgt * (kc[81] * u0 + kc[108] * u1 + kc[135] * u2);
+						r[w][2] = wgt * (kc[162] * u0 + kc[189] * u1 + kc[216] * u2);
 						nn[w] = nb[28 * p + 27];
 						pp[w] = p;
 					}
@@ -570,6 +590,175 @@ __global__ void __launch_bounds__(GS_WARPS * 32) k_gs_small(Lvl L, const T *__re
 	if(STAGE > 0)
 		for(int i = threadIdx.x; i < L.neq; i += blockDim.x)
 			d[i] = dp[i];
+}
+
+// Relaxation of small FP32 levels with the correction vector in shared
+// memory on a grid with a one-node zero halo (the neighbour of every slot is
+// then a fixed offset from the node and needs no clamping; stencil blocks of
+// missing neighbours are zero).  Nine lanes serve one node: lane r9 =
+// 3(dy+1) + (dx+1) takes the slots 3r9 .. 3r9+2 (dz = -1, 0, 1), whose
+// neighbours are three consecutive halo cells, and the 27 stencil words of
+// those slots (all three rows), padded to 28: "padded stencil" Kt, 252 words
+// per node, Kt[252p + 28r9 + 9k + 3i + j] = K_ij of slot 3r9 + k.  The nine
+// lanes of a node read 1008 consecutive bytes of stencil and 432 of vector.
+constexpr int KT_WORDS = 252;
+
+// rows r_i = sum over the lane's three slots of K_ij u_j
+__device__ __forceinline__ void kt_rows(const float4 *kr, const float4 *ur, float &r0, float &r1, float &r2)
+{
+	float k[28];
+#pragma unroll
+	for(int q = 0; q < 7; ++q)
+	{
+		const float4 v = kr[q];
+		k[4 * q] = v.x;
+		k[4 * q + 1] = v.y;
+		k[4 * q + 2] = v.z;
+		k[4 * q + 3] = v.w;
+	}
+	r0 = r1 = r2 = 0.f;
+#pragma unroll
+	for(int kk = 0; kk < 3; ++kk)
+	{
+		const float4 u = ur[kk];
+		r0 += k[9 * kk + 0] * u.x + k[9 * kk + 1] * u.y + k[9 * kk + 2] * u.z;
+		r1 += k[9 * kk + 3] * u.x + k[9 * kk + 4] * u.y + k[9 * kk + 5] * u.z;
+		r2 += k[9 * kk + 6] * u.x + k[9 * kk + 7] * u.y + k[9 * kk + 8] * u.z;
+	}
+}
+
+// sum of a row value over the nine lanes 9*sub .. 9*sub+8 of a node; the
+// total is valid in lane 9*sub (all 32 lanes must call it)
+__device__ __forceinline__ float kt_sum9(float v, int lane)
+{
+	v += __shfl_sync(0xffffffffu, v, min(lane + 1, 31)) + __shfl_sync(0xffffffffu, v, min(lane + 2, 31));
+	v += __shfl_sync(0xffffffffu, v, min(lane + 3, 31)) + __shfl_sync(0xffffffffu, v, min(lane + 6, 31));
+	return v;
+}
+
+// All sweeps of one gauss_seidel call on a small FP32 level (up to about a
+// thousand nodes) in one CTA: three nodes per warp (27 lanes), all warps on
+// the nodes of one colour, a barrier between colours.  KS: the padded
+// stencil is staged in shared memory (coarsest levels), else read through L2
+// in every phase.  All threads stage; only the first `nwork` warps relax,
+// synchronising on a named barrier, and the others leave.
+template <bool KS>
+__global__ void __launch_bounds__(1024) k_gs_tiny(Lvl L, const float4 *__restrict__ Kt, const float *__restrict__ BI,
+                                                  const float *__restrict__ F, float *d, int cycles, int zero_start, int nwork)
+{
+	pdl_begin();
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	const int HZ = L.noz + 2, HXZ = (L.nox + 2) * HZ, HN = HXZ * (L.noy + 2);
+	float4 *sK = reinterpret_cast<float4 *>(smem_raw);     // 63 * nno when KS
+	float4 *sd = sK + (KS ? (size_t)63 * L.nno : 0);         // halo grid, (d_x, d_y, d_z, 0)
+	float4 *sF = sd + HN;                                    // (F_x, F_y, F_z, 0) of position p
+	float4 *sB = sF + L.nno;                                 // 1/diag of position p
+	int *shp = reinterpret_cast<int *>(sB + L.nno);          // halo index of position p
+	if(KS)
+	{
+		const int n16 = 63 * L.nno;
+		for(int b = threadIdx.x; b < n16; b += 4 * blockDim.x)
+		{
+			float4 v[4];
+#pragma unroll
+			for(int k = 0; k < 4; ++k)
+				if(b + k * (int)blockDim.x < n16)
+					v[k] = __ldg(Kt + b + k * blockDim.x);
+#pragma unroll
+			for(int k = 0; k < 4; ++k)
+				if(b + k * (int)blockDim.x < n16)
+					sK[b + k * blockDim.x] = v[k];
+		}
+	}
+	for(int t = threadIdx.x; t < HN; t += blockDim.x)
+		sd[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+	for(int p = threadIdx.x; p < L.nno; p += blockDim.x)
+		sB[p] = make_float4(BI[3 * p], BI[3 * p + 1], BI[3 * p + 2], 0.f);
+	__syncthreads();
+	for(int n = threadIdx.x; n < L.nno; n += blockDim.x)
+	{
+		const int z = n % L.noz, x = (n / L.noz) % L.nox, y = n / (L.noz * L.nox);
+		const int p = cg_pos(L, x, y, z), hp = (z + 1) + HZ * (x + 1) + HXZ * (y + 1);
+		shp[p] = hp;
+		sF[p] = make_float4(F[3 * n], F[3 * n + 1], F[3 * n + 2], 0.f);
+		if(!zero_start)
+			sd[hp] = make_float4(d[3 * n], d[3 * n + 1], d[3 * n + 2], 0.f);
+	}
+	__syncthreads();
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	if(warp >= nwork)
+		return;
+	const int nthr = 32 * nwork;
+	const int sub = lane / 9, r9 = lane - 9 * sub;
+	// first of the lane's three neighbour cells relative to the node
+	const int uoff = -1 + HZ * (r9 % 3 - 1) + HXZ * (r9 / 3 - 1);
+	const float4 *Kb = KS ? sK : Kt;
+	for(int cyc = 0; cyc < cycles; ++cyc)
+		for(int c = 0; c < 8; ++c)
+		{
+			const int c0 = L.coff[c], nc = L.coff[c + 1] - c0;
+			for(int q0 = 3 * warp; q0 < nc; q0 += 3 * nwork)
+			{
+				const int q = q0 + sub;
+				const bool active = lane < 27 && q < nc;
+				const int p = c0 + (active ? q : 0);
+				float r0 = 0.f, r1 = 0.f, r2 = 0.f;
+				int hp = 0;
+				if(active)
+				{
+					hp = shp[p];
+					const float4 *kr = Kb + (size_t)63 * p + 7 * r9;
+					if(KS)
+						kt_rows(kr, sd + hp + uoff, r0, r1, r2);
+					else
+					{
+						float4 kg[7];
+#pragma unroll
+						for(int t = 0; t < 7; ++t)
+							kg[t] = __ldg(kr + t);
+						kt_rows(kg, sd + hp + uoff, r0, r1, r2);
+					}
+				}
+				r0 = kt_sum9(r0, lane);
+				r1 = kt_sum9(r1, lane);
+				r2 = kt_sum9(r2, lane);
+				if(active && r9 == 0)
+				{
+					float4 dv = sd[hp];
+					const float4 f = sF[p], bi = sB[p];
+					dv.x += (f.x - r0) * bi.x;
+					dv.y += (f.y - r1) * bi.y;
+					dv.z += (f.z - r2) * bi.z;
+					sd[hp] = dv;
+				}
+			}
+			asm volatile("bar.sync 1, %0;" ::"r"(nthr) : "memory");
+		}
+	for(int n = threadIdx.x; n < L.nno; n += nthr)
+	{
+		const int z = n % L.noz, x = (n / L.noz) % L.nox, y = n / (L.noz * L.nox);
+		const float4 v = sd[(z + 1) + HZ * (x + 1) + HXZ * (y + 1)];
+		d[3 * n] = v.x;
+		d[3 * n + 1] = v.y;
+		d[3 * n + 2] = v.z;
+	}
+}
+
+// the padded stencil from the node-by-node FP32 stencil (one thread per word)
+__global__ void k_tiny_stencil(Lvl L, const float *__restrict__ K, float *__restrict__ Kt)
+{
+	pdl_begin();
+	const int t = blockIdx.x * blockDim.x + threadIdx.x;
+	if(t >= KT_WORDS * L.nno)
+		return;
+	const int p = t / KT_WORDS, w = t - KT_WORDS * p, r9 = w / 28, e = w - 28 * r9;
+	float v = 0.f;
+	if(e < 27)
+	{
+		const int k = e / 9, i = (e / 3) % 3, j = e % 3;
+		v = K[cg_kidx(L, 3 * r9 + k, i, j, p)];
+	}
+	Kt[t] = v;
 }
 
 // ---------------------------------------------------------------- transfers
@@ -1570,14 +1759,50 @@ static size_t gs_smem_bytes(const Lvl &L, size_t word, int stage)
 }
 constexpr size_t GS_SMEM_MAX = 200 * 1024;
 
+// k_gs_tiny: [padded stencil], halo-padded correction vector, F, 1/diag, halo index
+static size_t gs_tiny_bytes(const Lvl &L, bool ks)
+{
+	const size_t hn = (size_t)(L.nox + 2) * (L.noy + 2) * (L.noz + 2);
+	return (ks ? (size_t)KT_WORDS * L.nno * sizeof(float) : 0) + hn * 16 + (size_t)2 * L.nno * 16 + (size_t)L.nno * sizeof(int);
+}
+
+bool gs_tiny_fits(const Lvl &L, size_t word)
+{
+	return L.aos != 0 && word == sizeof(float) && gs_tiny_bytes(L, false) <= GS_SMEM_MAX;
+}
+
 int kernels_init()
 {
 	// opt in to large dynamic shared memory once, outside any stream capture
-	cudaError_t e[3];
+	cudaError_t e[5];
 	e[0] = cudaFuncSetAttribute(k_gs_small<float, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GS_SMEM_MAX);
 	e[1] = cudaFuncSetAttribute(k_gs_small<float, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GS_SMEM_MAX);
 	e[2] = cudaFuncSetAttribute(k_gs_small<float, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GS_SMEM_MAX);
-	return (e[0] == cudaSuccess && e[1] == cudaSuccess && e[2] == cudaSuccess) ? 0 : -1;
+	e[3] = cudaFuncSetAttribute(k_gs_tiny<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GS_SMEM_MAX);
+	e[4] = cudaFuncSetAttribute(k_gs_tiny<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GS_SMEM_MAX);
+	for(cudaError_t x : e)
+		if(x != cudaSuccess)
+			return -1;
+	return 0;
+}
+
+void launch_tiny_stencil(cudaStream_t st, const Lvl &L, const float *K32, float4 *Kt)
+{
+	launch_k(k_tiny_stencil, nblocks(KT_WORDS * (long)L.nno), TPB, st, L, K32, reinterpret_cast<float *>(Kt));
+}
+
+void launch_gs_tiny(cudaStream_t st, const Lvl &L, const float4 *Kt, const float *BI, const float *F, float *d, int cycles,
+                    int zero_start)
+{
+	int maxc = 0;
+	for(int c = 0; c < 8; ++c)
+		maxc = std::max(maxc, L.coff[c + 1] - L.coff[c]);
+	const int nwork = std::max(1, std::min(32, (maxc + 2) / 3));
+	if(gs_tiny_bytes(L, true) <= GS_SMEM_MAX)
+		launch_k_smem(k_gs_tiny<true>, dim3(1), dim3(1024), gs_tiny_bytes(L, true), st, L, Kt, BI, F, d, cycles, zero_start, nwork);
+	else
+		launch_k_smem(k_gs_tiny<false>, dim3(1), dim3(1024), gs_tiny_bytes(L, false), st, L, Kt, BI, F, d, cycles, zero_start,
+		              nwork);
 }
 
 template <typename T>

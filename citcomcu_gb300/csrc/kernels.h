@@ -53,6 +53,11 @@ template <typename T> void launch_project(cudaStream_t st, const Lvl &Lf, const 
 template <typename T> void launch_interp(cudaStream_t st, const Lvl &Lc, const Lvl &Lf, const T *AD, T *AU);
 template <typename T> void launch_vel_update(cudaStream_t st, int n, T *vel, const T *del, T *res, const T *AU, const double *alpha_num_den, int update_res);
 bool gs_small_fits(const Lvl &L, size_t word);
+// small FP32 levels: one CTA, vectors in shared memory, padded stencil Kt (63 float4 per node)
+bool gs_tiny_fits(const Lvl &L, size_t word);
+void launch_tiny_stencil(cudaStream_t st, const Lvl &L, const float *K32, float4 *Kt);
+void launch_gs_tiny(cudaStream_t st, const Lvl &L, const float4 *Kt, const float *BI, const float *F, float *d, int cycles,
+                    int zero_start);
 
 // FP64 element operators
 void launch_div(cudaStream_t st, const Lvl &L, const Geo *geo, const double *U, double *divU);

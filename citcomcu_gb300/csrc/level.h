@@ -19,7 +19,7 @@ struct Lvl
 	int nno, nel, neq;
 	int elx, ely, elz;
 	int npad;        // stride of the structure-of-arrays coefficient storage
-	int aos;         // 1: small level, stencil stored node by node (243 contiguous words per node)
+	int aos;         // 1: small level, stencil stored node by node (243 contiguous words per node, slot fastest)
 	int cnt[3][2];   // number of indices of parity p along axis (0 x, 1 y, 2 z)
 	int coff[9];     // colour offsets in colour-major order
 	double h[3];     // element edge lengths (uniform per axis)
@@ -71,11 +71,13 @@ CG_HD int cg_loc(int a, int d)
 // stencil coefficient (neighbour slot s = (dz+1) + 3(dx+1) + 9(dy+1), row i,
 // column j) of the node at colour-major position p: 81 arrays of 3*npad
 // words; the three rows of a node are adjacent, so the three threads that own
-// a node's rows read consecutive words
+// a node's rows read consecutive words.  Small levels keep a node's 243 words
+// together with the slot fastest, so the 27 lanes of a warp that relax one
+// node read 27 consecutive words per (row, column) entry.
 CG_HD size_t cg_kidx(const Lvl &L, int s, int i, int j, int p)
 {
 	if(L.aos)
-		return (size_t)243 * p + 9 * s + 3 * i + j;
+		return (size_t)243 * p + 27 * (3 * i + j) + s;
 	return (size_t)(3 * s + j) * 3 * (size_t)L.npad + 3 * (size_t)p + i;
 }
 

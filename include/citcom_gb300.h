@@ -166,7 +166,8 @@ int citcom_gpu_stokes_residuals(citcom_gpu *h, double out[2]);
 /* n_assemble_del2_u (Element_calculations.c:552), stripped */
 int citcom_gpu_op_kmul(citcom_gpu *h, int lev, const double *u, double *Au);
 /* gauss_seidel (General_matrix_functions.c:1160), 8-colour order; d0 in/out
- * when guess != 0; Ad = K d0 on return */
+ * when guess != 0; Ad = K d0 on return.  In the mixed configuration it runs
+ * the FP32 smoother of a level below the finest (values rounded to float). */
 int citcom_gpu_op_gauss_seidel(citcom_gpu *h, int lev, double *d0, const double *F, double *Ad, int cycles, int guess);
 /* project_vector (Solver_multigrid.c:72) fine_lev -> fine_lev-1, stripped */
 int citcom_gpu_op_project(citcom_gpu *h, int fine_lev, const double *AU, double *AD);

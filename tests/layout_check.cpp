@@ -69,9 +69,9 @@ int main()
 						if(used[k]++)
 							return fail("kidx unique", p, s);
 						// slot_partial: structure-of-arrays kc = K + 3s*s3 + 3p, loads kc + j*s3 + i;
-						// node-by-node kc = K + 243p + 9s, loads kc + 3i + j
+						// node-by-node kc = K + 243p + s, loads kc + 27(3i + j)
 						const size_t s3 = 3 * (size_t)L.npad;
-						const size_t expect = aos ? (size_t)243 * p + 9 * s + 3 * i + j
+						const size_t expect = aos ? (size_t)243 * p + s + 27 * (3 * i + j)
 						                          : 3 * (size_t)p + i + (size_t)(3 * s) * s3 + j * s3;
 						if(expect != k)
 							return fail("gather pattern", p, s);

@@ -106,6 +106,31 @@ def test_gauss_seidel_colour_sweeps(small_ops, lev):
     assert rel(d2, d2r) < 1e-12
 
 
+@pytest.fixture(scope="module")
+def small_ops_mixed(cg, olib, small_ops):
+    _, o, T0 = small_ops
+    s = cg.Solver(cg.Config.like(small_case(), precision=cg.MIXED))
+    s.get_system_viscosity(T0)
+    s.construct_stiffness_B_matrix()
+    yield s, o
+    s.close()
+
+
+@pytest.mark.parametrize("lev", [0, 1])
+def test_gauss_seidel_fp32_levels(small_ops_mixed, lev):
+    # the FP32 single-CTA smoother (level 0: stencil in shared memory, 36
+    # nodes; level 1: stencil read through L2, 175 nodes) against the FP64
+    # 8-colour oracle; FP32 rounding of the stencil and the sums: 2e-5
+    s, o = small_ops_mixed
+    F = o.strip(lev, tv(o.dims[lev]["neq"], 0.19, 0.7))
+    d, ad = s.op_gauss_seidel(lev, F, 3)
+    dr, adr = o.gauss_seidel(lev, F, 3)
+    assert rel(d, dr) < 2e-5 and rel(ad, adr) < 2e-5
+    d2, _ = s.op_gauss_seidel(lev, F, 20, d0=d)
+    d2r, _ = o.gauss_seidel(lev, F, 20, d0=dr)
+    assert rel(d2, d2r) < 2e-5
+
+
 @pytest.mark.parametrize("lev", [1, 2])
 def test_transfers(small_ops, lev):
     s, o, _ = small_ops
