@@ -24,6 +24,7 @@ namespace {
 enum Slot
 {
 	S_RES = 0,    // r.r of the solve_del2_u residual after a multigrid pass
+	S_ERR = 1,    // set by the cluster program when one of its waits timed out
 	S_LS = 2,     // line search (AU.res, AU.AU)
 	S_R0 = 4,     // scratch dots
 	S_DOT = 8,    // 4 dots
@@ -81,6 +82,15 @@ struct citcom_gpu
 	bool no_graph;
 	bool level_timing;            // CITCOM_GPU_LEVEL_TIMING: time every smoother call (no graph)
 	bool no_tiny;                 // CITCOM_GPU_NO_TINY: coarsest FP32 levels use k_gs_small instead of k_gs_tiny
+	// FP32 multigrid work of levels 0..co_LC runs as one cluster program per
+	// stretch of consecutive coarse operations (co_LC = -1: off;
+	// CITCOM_GPU_NO_CLUSTER disables it)
+	int co_LC;
+	int co_cluster;
+	size_t co_smem;
+	bool co_local[CITCOM_MAX_LEVELS];
+	CoLevels co_lv;
+	CoProg co_prog;
 	double lt_ms[CITCOM_MAX_LEVELS];
 	long lt_calls[CITCOM_MAX_LEVELS];
 	long lt_sweeps[CITCOM_MAX_LEVELS];
@@ -194,6 +204,51 @@ template <typename T> void gs_inner(citcom_gpu *h, MG<T> &B, int lev, T *d, cons
 // Gauss-Seidel call; on the finest level the call is bracketed by timing
 // events (captured into the multigrid graph) so that the dominant kernel's
 // device time is measured live during every solve.
+// vector `id` (CoVec) of level lev
+template <typename T> T *mg_vec(MG<T> &B, int lev, int id)
+{
+	switch(id)
+	{
+	case CO_VEL: return B.vel[lev];
+	case CO_DEL: return B.del[lev];
+	case CO_RHS: return B.rhs[lev];
+	case CO_RES: return B.res[lev];
+	case CO_FL: return B.fl[lev];
+	default: return B.AU[lev];
+	}
+}
+
+// queued coarse operations run as one cluster program
+void co_flush(citcom_gpu *h)
+{
+	if(h->co_prog.n > 0)
+	{
+		launch_coarse(h->st, h->co_lv, h->co_prog, h->co_cluster, h->co_smem);
+		h->co_prog.n = 0;
+	}
+}
+
+template <typename T> bool co_level(citcom_gpu *h, int lev)
+{
+	return std::is_same<T, float>::value && lev <= h->co_LC;
+}
+
+void co_push(citcom_gpu *h, int type, int lev, int a, int b, int c, int cycles = 0, int zero = 0)
+{
+	if(h->co_prog.n == CO_MAX_OPS)
+		co_flush(h);
+	CoOp &op = h->co_prog.op[h->co_prog.n++];
+	op.type = (unsigned char)type;
+	op.lev = (unsigned char)lev;
+	op.a = (unsigned char)a;
+	op.b = (unsigned char)b;
+	op.c = (unsigned char)c;
+	op.zero = (unsigned char)zero;
+	op.local = (unsigned char)(type == CO_GS && h->co_local[lev]);
+	op.pad = 0;
+	op.cycles = (unsigned short)cycles;
+}
+
 template <typename T> void gs(citcom_gpu *h, MG<T> &B, int lev, T *d, const T *F, int cycles, int zero_start)
 {
 	const bool timed = (lev == h->L - 1) && h->n_gs_pairs < 4 && !gs_small_fits(h->lv[lev], sizeof(T));
@@ -251,42 +306,111 @@ template <typename T> void gs_inner(citcom_gpu *h, MG<T> &B, int lev, T *d, cons
 
 // ---------------------------------------------------------------- multi_grid
 
+// The operations of a pass, by level and vector id: levels 0..co_LC of the
+// FP32 solver are queued for the cluster program, the others launched at once
+// (after the queue is flushed, so the order of the pass is kept).
+template <typename T> void mg_gs(citcom_gpu *h, MG<T> &B, int lev, int d, int f, int cycles, int zero)
+{
+	if(!co_level<T>(h, lev))
+	{
+		co_flush(h);
+		gs<T>(h, B, lev, mg_vec(B, lev, d), mg_vec(B, lev, f), cycles, zero);
+		return;
+	}
+	if(!h->level_timing)
+	{
+		co_push(h, CO_GS, lev, d, f, 0, cycles, zero);
+		return;
+	}
+	co_flush(h);
+	cudaEventRecord(h->ev_gs[4], h->st);
+	co_push(h, CO_GS, lev, d, f, 0, cycles, zero);
+	co_flush(h);
+	cudaEventRecord(h->ev_gs[5], h->st);
+	cudaEventSynchronize(h->ev_gs[5]);
+	float ms = 0.f;
+	cudaEventElapsedTime(&ms, h->ev_gs[4], h->ev_gs[5]);
+	h->lt_ms[lev] += ms;
+	h->lt_calls[lev] += 1;
+	h->lt_sweeps[lev] += cycles;
+}
+
+// vec r = vec f - K vec d
+template <typename T> void mg_res(citcom_gpu *h, MG<T> &B, int lev, int f, int d, int r)
+{
+	if(co_level<T>(h, lev))
+		return co_push(h, CO_RESID, lev, f, d, r);
+	co_flush(h);
+	launch_residual<T>(h->st, h->lv[lev], B.K[lev], mg_vec(B, lev, f), mg_vec(B, lev, d), mg_vec(B, lev, r));
+}
+
+// vec dst (level lev-1) = projection of vec src (level lev)
+template <typename T> void mg_proj(citcom_gpu *h, MG<T> &B, int lev, int src, int dst)
+{
+	if(co_level<T>(h, lev))
+		return co_push(h, CO_PROJ, lev, src, dst, 0);
+	co_flush(h);
+	launch_project<T>(h->st, h->lv[lev], h->lv[lev - 1], mg_vec(B, lev, src), mg_vec(B, lev - 1, dst));
+}
+
+// vec dst (level lev) = interpolation of vec src (level lev-1)
+template <typename T> void mg_interp(citcom_gpu *h, MG<T> &B, int lev, int src, int dst)
+{
+	if(co_level<T>(h, lev))
+		return co_push(h, CO_INTERP, lev, src, dst, 0);
+	co_flush(h);
+	launch_interp<T>(h->st, h->lv[lev - 1], h->lv[lev], mg_vec(B, lev - 1, src), mg_vec(B, lev, dst));
+}
+
+// line search of the upward leg: AU = K del, vel += (AU.res / AU.AU) del
+// (and res -= alpha AU on the finest level)
+template <typename T> void mg_linesearch(citcom_gpu *h, MG<T> &B, int lev, bool finest)
+{
+	if(co_level<T>(h, lev) && !finest)
+	{
+		co_push(h, CO_KDOT, lev, CO_DEL, CO_RES, CO_AU);
+		co_push(h, CO_UPD, lev, CO_VEL, CO_DEL, 0);
+		return;
+	}
+	co_flush(h);
+	const Lvl &L = h->lv[lev];
+	launch_kmul_linesearch<T>(h->st, L, B.K[lev], B.del[lev], B.res[lev], B.AU[lev], red_of(h), h->dscal + S_LS);
+	launch_vel_update<T>(h->st, L.neq, B.vel[lev], B.del[lev], B.res[lev], B.AU[lev], h->dscal + S_LS, finest);
+}
+
 // One full-multigrid pass (multi_grid, General_matrix_functions.c:525-653).
 // Input: fl[lmax].  Output: vel[lmax] (the correction) and res[lmax].
 template <typename T> void mg_pass(citcom_gpu *h, MG<T> &B)
 {
 	const citcom_gpu_config &c = h->cfg;
 	const int lmax = h->L - 1, lmin = 0;
-	cudaStream_t st = h->st;
 	for(int lev = lmax; lev > lmin; --lev)
-		launch_project<T>(st, h->lv[lev], h->lv[lev - 1], B.fl[lev], B.fl[lev - 1]);
-	gs<T>(h, B, lmin, B.vel[lmin], B.fl[lmin], c.vlowstep, 1);
+		mg_proj<T>(h, B, lev, CO_FL, CO_FL);
+	mg_gs<T>(h, B, lmin, CO_VEL, CO_FL, c.vlowstep, 1);
 	for(int lev = lmin + 1; lev <= lmax; ++lev)
 	{
-		launch_interp<T>(st, h->lv[lev - 1], h->lv[lev], B.vel[lev - 1], B.vel[lev]);
+		mg_interp<T>(h, B, lev, CO_VEL, CO_VEL);
 		for(int Vn = 1; Vn <= c.mg_cycle; ++Vn)
 		{
 			for(int dlev = lev; dlev >= lmin + 1; --dlev)
 			{
 				const int cyc = (dlev == lmax) ? c.vhighstep : c.down_heavy;
-				const T *rhs = (dlev == lev) ? B.fl[lev] : B.rhs[dlev];
-				gs<T>(h, B, dlev, B.vel[dlev], rhs, cyc, dlev != lev);
-				launch_residual<T>(st, h->lv[dlev], B.K[dlev], rhs, B.vel[dlev], B.res[dlev]);
-				launch_project<T>(st, h->lv[dlev], h->lv[dlev - 1], B.res[dlev], B.rhs[dlev - 1]);
+				const int rhs = (dlev == lev) ? CO_FL : CO_RHS;
+				mg_gs<T>(h, B, dlev, CO_VEL, rhs, cyc, dlev != lev);
+				mg_res<T>(h, B, dlev, rhs, CO_VEL, CO_RES);
+				mg_proj<T>(h, B, dlev, CO_RES, CO_RHS);
 			}
-			gs<T>(h, B, lmin, B.vel[lmin], B.rhs[lmin], c.vlowstep, 1);
+			mg_gs<T>(h, B, lmin, CO_VEL, CO_RHS, c.vlowstep, 1);
 			for(int ulev = lmin + 1; ulev <= lev; ++ulev)
 			{
 				const int cyc = (ulev == lmax) ? c.vhighstep : c.up_heavy;
-				const Lvl &Lu = h->lv[ulev];
-				launch_interp<T>(st, h->lv[ulev - 1], Lu, B.vel[ulev - 1], B.del[ulev]);
-				gs<T>(h, B, ulev, B.del[ulev], B.res[ulev], cyc, 0);
-				launch_kmul_linesearch<T>(st, Lu, B.K[ulev], B.del[ulev], B.res[ulev], B.AU[ulev], red_of(h), h->dscal + S_LS);
-				launch_vel_update<T>(st, Lu.neq, B.vel[ulev], B.del[ulev], B.res[ulev], B.AU[ulev], h->dscal + S_LS,
-				                     ulev == lmax);
+				mg_interp<T>(h, B, ulev, CO_VEL, CO_DEL);
+				mg_gs<T>(h, B, ulev, CO_DEL, CO_RES, cyc, 0);
+				mg_linesearch<T>(h, B, ulev, ulev == lmax);
 			}
 		}
 	}
+	co_flush(h);
 }
 
 // the pass plus solve_del2_u's bookkeeping; FP64: r (= fl[lmax]) <- res, d0 += vel;
@@ -353,7 +477,7 @@ int solve_del2_u(citcom_gpu *h, double acc, int *valid)
 	CK(cudaMemcpyAsync(r, h->Ah, sizeof(double) * neq, cudaMemcpyDeviceToDevice, h->st));
 	CK(cudaMemsetAsync(h->u1, 0, sizeof(double) * (neq + 2), h->st));
 	launch_dot(h->st, neq, r, r, red_of(h), h->dscal + S_RES);
-	TRY(readback(h, S_RES, 1));
+	TRY(readback(h, S_RES, 2));
 	const double r0 = std::sqrt(h->hscal[S_RES] / neq);
 	double residual = r0;
 	if(r0 * h->cfg.accuracy > acc)
@@ -366,7 +490,9 @@ int solve_del2_u(citcom_gpu *h, double acc, int *valid)
 			return fail(h, CITCOM_GPU_ERR_NOCONV, "solve_del2_u: no convergence after %d multigrid passes (residual %g > %g)",
 			            count, residual, acc);
 		TRY(run_pass(h));
-		TRY(readback(h, S_RES, 1));
+		TRY(readback(h, S_RES, 2));
+		if(h->hscal[S_ERR] != 0.0)
+			return fail(h, CITCOM_GPU_ERR_CUDA, "solve_del2_u: a wait of the cluster smoother timed out");
 		residual = std::sqrt(h->hscal[S_RES] / neq);
 		for(int k = 0; k < h->n_gs_pairs; ++k)
 		{
@@ -687,6 +813,8 @@ int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 		const char *q = getenv("CITCOM_GPU_NO_PDL");
 		if(q && q[0] && q[0] != '0')
 			g_use_pdl = 0;
+		const char *nc = getenv("CITCOM_GPU_NO_CLUSTER");
+		h->co_LC = (nc && nc[0] && nc[0] != '0') ? -2 : -1;
 	}
 	memset(&h->stats, 0, sizeof(h->stats));
 	int r = CITCOM_GPU_OK;
@@ -716,6 +844,27 @@ int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 			make_level(*cfg, l, h->lv[l]);
 		const int lmax = h->L - 1;
 		const Lvl &Lf = h->lv[lmax];
+		// the coarse levels that the cluster program serves (mixed precision)
+		{
+			const bool allowed = h->co_LC == -1 && cfg->precision == CITCOM_GPU_MIXED;
+			h->co_LC = -1;
+			h->co_cluster = 0;
+			h->co_smem = 0;
+			if(allowed && coarse_init(&h->co_cluster) == 0)
+			{
+				for(int l = 0; l < lmax && l < CO_MAX_LEV; ++l)
+				{
+					if(!coarse_level_ok(h->lv[l], l, h->co_cluster, &h->co_local[l]))
+						break;
+					h->co_LC = l;
+					h->co_smem = std::max(h->co_smem, coarse_smem(h->lv[l], h->co_local[l]));
+				}
+				if(h->co_LC < 1)
+					h->co_LC = -1;
+			}
+			cudaGetLastError();
+			h->co_prog.n = 0;
+		}
 		for(int l = 0; l < h->L; ++l)
 		{
 			const Lvl &L = h->lv[l];
@@ -744,7 +893,7 @@ int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 			{
 				TRYC(dalloc(h, &h->K32[l], (size_t)243 * L.npad));
 				TRYC(dalloc(h, &h->BI32[l], (size_t)3 * L.npad));
-				if(gs_tiny_fits(L, sizeof(float)))
+				if(gs_tiny_fits(L, sizeof(float)) || l <= h->co_LC)
 					TRYC(dalloc(h, &h->Kt32[l], (size_t)63 * L.nno));
 			}
 			h->mg64.K[l] = h->K64[l];
@@ -756,6 +905,16 @@ int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 			TRYC(alloc_mg(h, h->mg64));
 		else
 			TRYC(alloc_mg(h, h->mg32));
+		memset(&h->co_lv, 0, sizeof(h->co_lv));
+		h->co_lv.nlev = h->co_LC + 1;
+		for(int l = 0; l <= h->co_LC; ++l)
+		{
+			h->co_lv.L[l] = h->lv[l];
+			h->co_lv.Kt[l] = h->Kt32[l];
+			h->co_lv.BI[l] = h->BI32[l];
+			for(int v = 0; v < CO_NVEC; ++v)
+				h->co_lv.vec[l][v] = mg_vec(h->mg32, l, v);
+		}
 		TRYC(dalloc(h, &h->BPI, Lf.nel));
 		TRYC(dalloc(h, &h->visc_work[0], Lf.nno));
 		TRYC(dalloc(h, &h->visc_work[1], Lf.nno));
@@ -782,6 +941,7 @@ int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 		TRYC(dalloc(h, &h->Tdot1, Lf.nno));
 		TRYC(dalloc(h, &h->hf_work, Lf.nno + Lf.nel));
 		TRYC(dalloc(h, &h->dscal, S_COUNT));
+		h->co_lv.err = h->dscal + S_ERR;
 		TRYC(dalloc(h, &h->red.partials, (size_t)RED_MAX_BLOCKS * 8));
 		TRYC(dalloc(h, &h->red.counter, 1));
 		if(cudaMallocHost((void **)&h->hscal, S_COUNT * sizeof(double)) != cudaSuccess)
@@ -1139,7 +1299,8 @@ int citcom_gpu_op_gauss_seidel(citcom_gpu *h, int lev, double *d0, const double 
 		}
 		TRY(h2d(h, B.rhs[lev], f.data(), sizeof(float) * L.neq));
 		TRY(h2d(h, B.vel[lev], v.data(), sizeof(float) * L.neq));
-		gs<float>(h, B, lev, B.vel[lev], B.rhs[lev], cycles, !guess);
+		mg_gs<float>(h, B, lev, CO_VEL, CO_RHS, cycles, !guess);
+		co_flush(h);
 		launch_kmul<float>(h->st, L, B.K[lev], B.vel[lev], B.AU[lev]);
 		TRY(d2h(h, v.data(), B.vel[lev], sizeof(float) * L.neq));
 		TRY(d2h(h, f.data(), B.AU[lev], sizeof(float) * L.neq));
@@ -1235,12 +1396,35 @@ int citcom_gpu_op_grad(citcom_gpu *h, int lev, const double *P, double *gradP)
 int citcom_gpu_op_multi_grid(citcom_gpu *h, double *d1, double *F, double *residual)
 {
 	TRY(check_handle(h));
-	if(h->cfg.precision != CITCOM_GPU_FP64)
-		return fail(h, CITCOM_GPU_ERR_STATE, "op_multi_grid is provided for the FP64 configuration");
 	if(!h->stiffness_ready)
 		return fail(h, CITCOM_GPU_ERR_STATE, "construct_stiffness_B_matrix has not been called");
 	const int lmax = h->L - 1;
 	const Lvl &Lf = h->lv[lmax];
+	if(h->cfg.precision != CITCOM_GPU_FP64)
+	{
+		// mixed configuration: one FP32 pass (F rounded to float)
+		MG<float> &B = h->mg32;
+		TRY(h2d(h, h->r64, F, sizeof(double) * Lf.neq));
+		launch_copy_d2f(h->st, Lf.neq, B.fl[lmax], h->r64);
+		const int pairs = h->n_gs_pairs;
+		h->n_gs_pairs = 4;
+		mg_pass<float>(h, B);
+		h->n_gs_pairs = pairs;
+		std::vector<float> v(Lf.neq), r(Lf.neq);
+		TRY(d2h(h, v.data(), B.vel[lmax], sizeof(float) * Lf.neq));
+		TRY(d2h(h, r.data(), B.res[lmax], sizeof(float) * Lf.neq));
+		TRY(sync(h));
+		double rr = 0.0;
+		for(int i = 0; i < Lf.neq; ++i)
+		{
+			d1[i] = v[i];
+			F[i] = r[i];
+			rr += (double)r[i] * r[i];
+		}
+		if(residual)
+			*residual = std::sqrt(rr / Lf.neq);
+		return CITCOM_GPU_OK;
+	}
 	TRY(h2d(h, h->mg64.fl[lmax], F, sizeof(double) * Lf.neq));
 	const int pairs = h->n_gs_pairs;
 	h->n_gs_pairs = 4;  // no smoother timing outside the captured pass

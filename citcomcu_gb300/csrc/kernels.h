@@ -59,6 +59,55 @@ void launch_tiny_stencil(cudaStream_t st, const Lvl &L, const float *K32, float4
 void launch_gs_tiny(cudaStream_t st, const Lvl &L, const float4 *Kt, const float *BI, const float *F, float *d, int cycles,
                     int zero_start);
 
+// The coarse levels of an FP32 multigrid pass as one program run by one
+// thread-block cluster (coarse.cu).  Vectors of a level by id:
+enum CoVec
+{
+	CO_VEL,
+	CO_DEL,
+	CO_RHS,
+	CO_RES,
+	CO_FL,
+	CO_AU,
+	CO_NVEC
+};
+enum CoOpType
+{
+	CO_GS,      // Gauss-Seidel: vec a relaxed against vec b, `cycles` sweeps, zero start if `zero`
+	CO_RESID,   // vec c = vec a - K vec b
+	CO_PROJ,    // vec b (level lev-1) = projection of vec a (level lev), stripped
+	CO_INTERP,  // vec b (level lev) = interpolation of vec a (level lev-1), stripped
+	CO_KDOT,    // vec c = K vec a; alpha = (c . vec b) / (c . c), FP64
+	CO_UPD      // vec a += alpha vec b
+};
+#define CO_MAX_LEV 6
+#define CO_MAX_OPS 96
+#define CO_SMEM_MAX (200 * 1024)
+struct CoOp
+{
+	unsigned char type, lev, a, b, c, zero, local, pad;
+	unsigned short cycles;
+};
+struct CoProg
+{
+	int n;
+	CoOp op[CO_MAX_OPS];
+};
+struct CoLevels
+{
+	int nlev;  // levels 0 .. nlev-1
+	Lvl L[CO_MAX_LEV];
+	const float4 *Kt[CO_MAX_LEV];  // padded stencils
+	const float *BI[CO_MAX_LEV];
+	float *vec[CO_MAX_LEV][CO_NVEC];
+	double *err;  // set to 1 if a wait of the cluster smoother timed out
+};
+// cluster size the device supports for the program (16 or 8); -1 if none
+int coarse_init(int *cluster_size);
+bool coarse_level_ok(const Lvl &L, int level, int cluster, bool *local);
+size_t coarse_smem(const Lvl &L, bool local);
+void launch_coarse(cudaStream_t st, const CoLevels &D, const CoProg &P, int cluster, size_t smem);
+
 // FP64 element operators
 void launch_div(cudaStream_t st, const Lvl &L, const Geo *geo, const double *U, double *divU);
 void launch_grad(cudaStream_t st, const Lvl &L, const Geo *geo, const double *P, double *gradP);

@@ -176,7 +176,8 @@ int citcom_gpu_op_interp(citcom_gpu *h, int coarse_lev, const double *AD, double
 /* assemble_div_u / assemble_grad_p (Element_calculations.c:691, 727) */
 int citcom_gpu_op_div(citcom_gpu *h, int lev, const double *U, double *divU);
 int citcom_gpu_op_grad(citcom_gpu *h, int lev, const double *P, double *gradP);
-/* multi_grid (General_matrix_functions.c:525): d1 out, F in/out (residual) */
+/* multi_grid (General_matrix_functions.c:525): d1 out, F in/out (residual);
+ * in the mixed configuration one FP32 pass on F rounded to float */
 int citcom_gpu_op_multi_grid(citcom_gpu *h, double *d1, double *F, double *residual);
 /* solve_del2_u (General_matrix_functions.c:368) on the finest level */
 int citcom_gpu_op_solve_del2_u(citcom_gpu *h, double *d0, const double *F, double acc, int *valid);

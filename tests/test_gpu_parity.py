@@ -106,10 +106,18 @@ def test_gauss_seidel_colour_sweeps(small_ops, lev):
     assert rel(d2, d2r) < 1e-12
 
 
-@pytest.fixture(scope="module")
-def small_ops_mixed(cg, olib, small_ops):
+@pytest.fixture(scope="module", params=["cluster", "single-cta"])
+def small_ops_mixed(request, cg, olib, small_ops):
+    # "cluster": the coarse levels run as one thread-block-cluster program
+    # (level 0 relaxed by one CTA, level 1 by the whole cluster);
+    # "single-cta": the same levels through the one-CTA smoother kernel
     _, o, T0 = small_ops
-    s = cg.Solver(cg.Config.like(small_case(), precision=cg.MIXED))
+    if request.param == "single-cta":
+        os.environ["CITCOM_GPU_NO_CLUSTER"] = "1"
+    try:
+        s = cg.Solver(cg.Config.like(small_case(), precision=cg.MIXED))
+    finally:
+        os.environ.pop("CITCOM_GPU_NO_CLUSTER", None)
     s.get_system_viscosity(T0)
     s.construct_stiffness_B_matrix()
     yield s, o
@@ -118,9 +126,8 @@ def small_ops_mixed(cg, olib, small_ops):
 
 @pytest.mark.parametrize("lev", [0, 1])
 def test_gauss_seidel_fp32_levels(small_ops_mixed, lev):
-    # the FP32 single-CTA smoother (level 0: stencil in shared memory, 36
-    # nodes; level 1: stencil read through L2, 175 nodes) against the FP64
-    # 8-colour oracle; FP32 rounding of the stencil and the sums: 2e-5
+    # the FP32 smoothers of the coarse levels (36 and 175 nodes) against the
+    # FP64 8-colour oracle; FP32 rounding of the stencil and the sums: 2e-5
     s, o = small_ops_mixed
     F = o.strip(lev, tv(o.dims[lev]["neq"], 0.19, 0.7))
     d, ad = s.op_gauss_seidel(lev, F, 3)
@@ -129,6 +136,17 @@ def test_gauss_seidel_fp32_levels(small_ops_mixed, lev):
     d2, _ = s.op_gauss_seidel(lev, F, 20, d0=d)
     d2r, _ = o.gauss_seidel(lev, F, 20, d0=dr)
     assert rel(d2, d2r) < 2e-5
+
+
+def test_multigrid_pass_fp32(small_ops_mixed):
+    # one FP32 multigrid pass (every level's smoother, residuals, transfers
+    # and line searches) against the FP64 oracle pass: FP32 rounding, 1e-4
+    s, o = small_ops_mixed
+    F = o.F()[: o.fine["neq"]].copy()
+    d1, res, r = s.op_multi_grid(F)
+    d1r, resr, rr = o.multi_grid(F)
+    assert rel(d1, d1r) < 1e-4 and rel(res, resr) < 1e-4
+    assert abs(r - rr) <= 1e-4 * rr
 
 
 @pytest.mark.parametrize("lev", [1, 2])
