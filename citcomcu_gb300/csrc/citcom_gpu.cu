@@ -909,6 +909,7 @@ int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 		h->co_lv.nlev = h->co_LC + 1;
 		for(int l = 0; l <= h->co_LC; ++l)
 		{
+			h->co_lv.win[l] = coarse_window(h->lv[l], h->co_cluster);
 			h->co_lv.L[l] = h->lv[l];
 			h->co_lv.Kt[l] = h->Kt32[l];
 			h->co_lv.BI[l] = h->BI32[l];

@@ -26,6 +26,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 
 #include "kernels.h"
 
@@ -90,18 +91,35 @@ __device__ __forceinline__ bool co_mbar_test(unsigned bar, unsigned parity)
 	return ok != 0;
 }
 
-// bounded wait for the phase of `bar` with this parity; on time-out the
-// error word is set and the kernel goes on (its results are then invalid)
-constexpr long CO_WAIT_LIMIT = 1L << 24;
-__device__ __forceinline__ void co_mbar_wait(unsigned bar, unsigned parity, double *err)
+// suspends the thread until the phase completes or about `ns` pass
+__device__ __forceinline__ bool co_mbar_try(unsigned bar, unsigned parity, unsigned ns)
+{
+	unsigned ok;
+	asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+	             : "=r"(ok)
+	             : "r"(bar), "r"(parity), "r"(ns)
+	             : "memory");
+	return ok != 0;
+}
+
+// bounded wait (about a second at most) for the phase of `bar` with this
+// parity; on time-out the error word is set and false returned (the caller
+// then stops arming and storing: an arrival on a barrier whose phase is
+// still open is not allowed)
+#ifndef CO_SPIN
+#define CO_SPIN 0
+#endif
+constexpr long CO_WAIT_LIMIT = CO_SPIN ? (1L << 24) : (1L << 17);
+__device__ __forceinline__ bool co_mbar_wait(unsigned bar, unsigned parity, double *err)
 {
 	long it = 0;
-	while(!co_mbar_test(bar, parity))
+	while(!(CO_SPIN ? co_mbar_test(bar, parity) : co_mbar_try(bar, parity, 10000u)))
 		if(++it > CO_WAIT_LIMIT)
 		{
 			*err = 1.0;
-			break;
+			return false;
 		}
+	return true;
 }
 
 // the level's vector d (node order) into the halo grid sd, zero halo
@@ -132,7 +150,7 @@ __device__ void co_fill_halo(const Lvl &L, const float *d, bool zero, float4 *sd
 // so no value is overwritten before it is read.  Ends with d written back.
 template <bool LOCAL>
 __device__ void co_gs(cgp::cluster_group &cl, const Lvl &L, const float4 *Kt, const float *BI, float *d, const float *f, int cycles,
-                      bool zero, float4 *arena, unsigned long long *bars, double *err)
+                      bool zero, int win, float4 *arena, unsigned long long *bars, double *err)
 {
 	const int rank = LOCAL ? 0 : (int)cl.block_rank();
 	const int ncta = LOCAL ? 1 : (int)cl.num_blocks();
@@ -192,11 +210,16 @@ __device__ void co_gs(cgp::cluster_group &cl, const Lvl &L, const float4 *Kt, co
 	const int sub = lane / 9, r9 = lane - 9 * sub, j = 3 * warp + sub;
 	const int uoff = -1 + HZ * (r9 % 3 - 1) + HXZ * (r9 / 3 - 1);
 	const unsigned sd_a = co_smem_addr(sd), bar_a = co_smem_addr(bars);
-	unsigned ra0 = 0, ra1 = 0;  // the two CTAs this lane stores to (r9, r9 + 9)
+	// a node's value goes to the CTAs within `win` ranks of its owner (they
+	// hold all its neighbours): this lane stores to wlo + r9 and wlo + r9 + 9
+	const int wlo = max(0, rank - win), whi = min(ncta - 1, rank + win);
+	unsigned ra0 = 0xffffffffu, ra1 = 0xffffffffu;
 	if(!LOCAL)
 	{
-		ra0 = r9 < ncta ? (unsigned)r9 : 0xffffffffu;
-		ra1 = r9 + 9 < ncta ? (unsigned)(r9 + 9) : 0xffffffffu;
+		if(wlo + r9 <= whi)
+			ra0 = (unsigned)(wlo + r9);
+		if(wlo + r9 + 9 <= whi)
+			ra1 = (unsigned)(wlo + r9 + 9);
 	}
 	const int nph = 8 * cycles;
 	// stencil words of the lane's node of the current colour (prefetched one colour ahead)
@@ -216,11 +239,16 @@ __device__ void co_gs(cgp::cluster_group &cl, const Lvl &L, const float4 *Kt, co
 		for(int t = 0; t < 7; ++t)
 			kc[t] = __ldg(Kb + (size_t)63 * p + 7 * r9 + t);
 	unsigned uses0 = 0, uses1 = 0;  // completed phases of the two barriers
+	bool ok = true;                 // false after a timed-out wait: no more arrivals or stores
 	for(int ph = 0; ph < nph; ++ph)
 	{
 		const int c = ph & 7, b = ph & 1;
-		if(!LOCAL && threadIdx.x == 0)
-			co_mbar_expect(bar_a + 8 * b, (unsigned)(16 * (L.coff[c + 1] - L.coff[c])));
+		if(!LOCAL && threadIdx.x == 0 && ok)
+		{
+			// the values of colour c owned by the ranks wlo .. whi
+			const int nc = L.coff[c + 1] - L.coff[c];
+			co_mbar_expect(bar_a + 8 * b, (unsigned)(16 * (nc * (whi + 1) / ncta - nc * wlo / ncta)));
+		}
 		float4 dv = make_float4(0.f, 0.f, 0.f, 0.f), fv = dv, bv = dv;
 		float r0 = 0.f, r1 = 0.f, r2 = 0.f;
 		if(act)
@@ -264,7 +292,7 @@ __device__ void co_gs(cgp::cluster_group &cl, const Lvl &L, const float4 *Kt, co
 			dv.x = __shfl_sync(0xffffffffu, dv.x, src);
 			dv.y = __shfl_sync(0xffffffffu, dv.y, src);
 			dv.z = __shfl_sync(0xffffffffu, dv.z, src);
-			if(act_c)
+			if(act_c && ok)
 			{
 				const unsigned off = 16u * (unsigned)hp_c;
 				if(ra0 != 0xffffffffu)
@@ -272,7 +300,8 @@ __device__ void co_gs(cgp::cluster_group &cl, const Lvl &L, const float4 *Kt, co
 				if(ra1 != 0xffffffffu)
 					co_st_async(co_mapa(sd_a + off, ra1), dv, co_mapa(bar_a + 8 * b, ra1));
 			}
-			co_mbar_wait(bar_a + 8 * b, (b ? uses1 : uses0) & 1u, err);
+			if(ok)
+				ok = co_mbar_wait(bar_a + 8 * b, (b ? uses1 : uses0) & 1u, err);
 			if(b)
 				++uses1;
 			else
@@ -308,19 +337,23 @@ __device__ void co_kmul(const Lvl &L, const float4 *Kt, const float4 *sd, const 
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	const int sub = lane / 9, r9 = lane - 9 * sub;
 	const int uoff = -1 + HZ * (r9 % 3 - 1) + HXZ * (r9 / 3 - 1);
-	int lo, cnt;
-	co_chunk(L.nno, rank, ncta, lo, cnt);
-	for(int b = 0; b < cnt; b += CO_NODES)
+	// the CTA's nodes are its chunks of every colour, as in the smoother, so
+	// that the halo values the smoother left are the ones needed here
+	for(int c = 0; c < 8; ++c)
 	{
+		int lo, cnt;
+		co_chunk(L.coff[c + 1] - L.coff[c], rank, ncta, lo, cnt);
+		for(int b = 0; b < cnt; b += CO_NODES)
+		{
 		const int q = b + 3 * warp + sub;
 		const bool act = lane < 27 && q < cnt;
 		float r0 = 0.f, r1 = 0.f, r2 = 0.f;
 		int n = 0;
 		if(act)
 		{
-			const int p = lo + q;
-			int c, x, y, z;
-			pos_xyz(L, p, c, x, y, z);
+			const int p = L.coff[c] + lo + q;
+			int x, y, z;
+			cg_decode(L, c, lo + q, x, y, z);
 			n = cg_node(L, x, y, z);
 			float4 k[7];
 			const float4 *kr = Kt + (size_t)63 * p + 7 * r9;
@@ -349,6 +382,7 @@ __device__ void co_kmul(const Lvl &L, const float4 *Kt, const float4 *sd, const 
 				      (double)r2 * (double)__ldcg(f + 3 * n + 2);
 				aa += (double)r0 * (double)r0 + (double)r1 * (double)r1 + (double)r2 * (double)r2;
 			}
+		}
 		}
 	}
 }
@@ -391,12 +425,12 @@ __global__ void __launch_bounds__(CO_THREADS) k_coarse(const __grid_constant__ C
 			if(op.local)
 			{
 				if(rank == 0)
-					co_gs<true>(cl, L, D.Kt[l], D.BI[l], D.vec[l][op.a], D.vec[l][op.b], op.cycles, op.zero != 0, arena, bars, D.err);
+					co_gs<true>(cl, L, D.Kt[l], D.BI[l], D.vec[l][op.a], D.vec[l][op.b], op.cycles, op.zero != 0, D.win[l], arena, bars, D.err);
 				halo_lev = -1;
 			}
 			else
 			{
-				co_gs<false>(cl, L, D.Kt[l], D.BI[l], D.vec[l][op.a], D.vec[l][op.b], op.cycles, op.zero != 0, arena, bars, D.err);
+				co_gs<false>(cl, L, D.Kt[l], D.BI[l], D.vec[l][op.a], D.vec[l][op.b], op.cycles, op.zero != 0, D.win[l], arena, bars, D.err);
 				halo_lev = l;
 				halo_vec = op.a;
 			}
@@ -555,6 +589,8 @@ bool coarse_level_ok(const Lvl &L, int level, int cluster, bool *local)
 }
 
 size_t coarse_smem(const Lvl &L, bool local) { return co_gs_bytes(L, local); }
+
+int coarse_window(const Lvl &L, int cluster) { return cg_owner_window(L, cluster); }
 
 void launch_coarse(cudaStream_t st, const CoLevels &D, const CoProg &P, int cluster, size_t smem)
 {

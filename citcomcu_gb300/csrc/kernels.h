@@ -100,11 +100,15 @@ struct CoLevels
 	const float4 *Kt[CO_MAX_LEV];  // padded stencils
 	const float *BI[CO_MAX_LEV];
 	float *vec[CO_MAX_LEV][CO_NVEC];
-	double *err;  // set to 1 if a wait of the cluster smoother timed out
+	int win[CO_MAX_LEV];  // ranks on either side of a node's owner that hold its neighbours
+	double *err;          // set to 1 if a wait of the cluster smoother timed out
 };
 // cluster size the device supports for the program (16 or 8); -1 if none
 int coarse_init(int *cluster_size);
 bool coarse_level_ok(const Lvl &L, int level, int cluster, bool *local);
+// the rank window of a level (host): the largest rank distance between a
+// node's owner and the owner of one of its neighbours
+int coarse_window(const Lvl &L, int cluster);
 size_t coarse_smem(const Lvl &L, bool local);
 void launch_coarse(cudaStream_t st, const CoLevels &D, const CoProg &P, int cluster, size_t smem);
 

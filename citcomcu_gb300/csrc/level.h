@@ -85,6 +85,45 @@ CG_HD size_t cg_kidx(const Lvl &L, int s, int i, int j, int p)
 // by one CTA (warp per node)
 #define CG_SMALL_LEVEL_NODES 1400
 
+// Chunked ownership of the colour-major positions among `nranks` workers:
+// worker r owns positions [n_c r / nranks, n_c (r+1) / nranks) (integer
+// division) of every colour c, n_c the colour's size.
+CG_HD int cg_owner(const Lvl &L, int x, int y, int z, int nranks)
+{
+	const int c = cg_colour(x, y, z), nc = L.coff[c + 1] - L.coff[c];
+	const int q = cg_pos(L, x, y, z) - L.coff[c];
+	int r = (int)((long)q * nranks / nc);
+	while(r > 0 && nc * r / nranks > q)
+		--r;
+	while(r + 1 < nranks && nc * (r + 1) / nranks <= q)
+		++r;
+	return r;
+}
+
+// the largest rank distance between the owner of a node and the owner of one
+// of its 27 neighbours (host only)
+inline int cg_owner_window(const Lvl &L, int nranks)
+{
+	int w = 0;
+	for(int y = 0; y < L.noy; ++y)
+		for(int x = 0; x < L.nox; ++x)
+			for(int z = 0; z < L.noz; ++z)
+			{
+				const int r = cg_owner(L, x, y, z, nranks);
+				for(int dy = -1; dy <= 1; ++dy)
+					for(int dx = -1; dx <= 1; ++dx)
+						for(int dz = -1; dz <= 1; ++dz)
+						{
+							const int X = x + dx, Y = y + dy, Z = z + dz;
+							if(X < 0 || Y < 0 || Z < 0 || X >= L.nox || Y >= L.noy || Z >= L.noz)
+								continue;
+							const int d = cg_owner(L, X, Y, Z, nranks) - r;
+							w = d > w ? d : (-d > w ? -d : w);
+						}
+			}
+	return w;
+}
+
 CG_HD int cg_local_index(int ox, int oy, int oz)
 {
 	// inverse of cg_loc

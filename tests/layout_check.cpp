@@ -84,6 +84,25 @@ int main()
 			if(cg_local_index(cg_loc(a, 0), cg_loc(a, 1), cg_loc(a, 2)) != a)
 				return fail("local index", a, 0);
 	}
+	// chunked ownership: every position has exactly the owner whose chunk
+	// holds it, and the neighbour window of the cubes the 64^3 multigrid uses
+	// (16 ranks): 5^3 -> 7, 9^3 -> 4, 17^3 -> 2, 33^3 -> 1
+	const int cube[4][2] = {{4, 7}, {8, 4}, {16, 2}, {32, 1}};
+	for(auto &cw : cube)
+	{
+		Lvl L = make(cw[0], cw[0], cw[0]);
+		for(int y = 0; y < L.noy; ++y)
+			for(int x = 0; x < L.nox; ++x)
+				for(int z = 0; z < L.noz; ++z)
+				{
+					const int c = cg_colour(x, y, z), nc = L.coff[c + 1] - L.coff[c];
+					const int q = cg_pos(L, x, y, z) - L.coff[c], r = cg_owner(L, x, y, z, 16);
+					if(!(nc * r / 16 <= q && q < nc * (r + 1) / 16))
+						return fail("owner chunk", q, r);
+				}
+		if(cg_owner_window(L, 16) != cw[1])
+			return fail("owner window", cw[0], cg_owner_window(L, 16));
+	}
 	printf("OK\n");
 	return 0;
 }
