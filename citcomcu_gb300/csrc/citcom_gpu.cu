@@ -368,8 +368,7 @@ template <typename T> void mg_linesearch(citcom_gpu *h, MG<T> &B, int lev, bool 
 {
 	if(co_level<T>(h, lev) && !finest)
 	{
-		co_push(h, CO_KDOT, lev, CO_DEL, CO_RES, CO_AU);
-		co_push(h, CO_UPD, lev, CO_VEL, CO_DEL, 0);
+		co_push(h, CO_KDOT, lev, CO_DEL, CO_RES, CO_AU, 0, 1);  // with the update vel += alpha del
 		return;
 	}
 	co_flush(h);

@@ -122,20 +122,52 @@ __device__ __forceinline__ bool co_mbar_wait(unsigned bar, unsigned parity, doub
 	return true;
 }
 
-// the level's vector d (node order) into the halo grid sd, zero halo
-__device__ void co_fill_halo(const Lvl &L, const float *d, bool zero, float4 *sd)
+// a vector (written by other CTAs) into this CTA's shared memory, eight
+// loads in flight per thread; ends with a CTA barrier.  Not inlined: its
+// registers would otherwise weigh on the allocation of the smoother loop.
+__device__ __noinline__ void co_stage(const float *v, int n, float *s)
+{
+	for(int b = threadIdx.x; b < n; b += 8 * blockDim.x)
+	{
+		float x[8];
+#pragma unroll
+		for(int k = 0; k < 8; ++k)
+			if(b + k * (int)blockDim.x < n)
+				x[k] = __ldcg(v + b + k * blockDim.x);
+#pragma unroll
+		for(int k = 0; k < 8; ++k)
+			if(b + k * (int)blockDim.x < n)
+				s[b + k * blockDim.x] = x[k];
+	}
+	__syncthreads();
+}
+
+// the level's vector d (node order) into the halo grid sd, zero halo; four
+// cells (twelve loads) in flight per thread.  Not inlined (as co_stage).
+__device__ __noinline__ void co_fill_halo(const Lvl &L, const float *d, bool zero, float4 *sd)
 {
 	const int HZ = L.noz + 2, HX = L.nox + 2, HN = HZ * HX * (L.noy + 2);
-	for(int t = threadIdx.x; t < HN; t += blockDim.x)
+	for(int b = threadIdx.x; b < HN; b += 4 * blockDim.x)
 	{
-		const int hz = t % HZ, hx = (t / HZ) % HX, hy = t / (HZ * HX);
-		float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-		if(!zero && hz >= 1 && hz <= L.noz && hx >= 1 && hx <= L.nox && hy >= 1 && hy <= L.noy)
+		float4 v[4];
+		int n[4];
+#pragma unroll
+		for(int k = 0; k < 4; ++k)
 		{
-			const int n = cg_node(L, hx - 1, hy - 1, hz - 1);
-			v = make_float4(__ldcg(d + 3 * n), __ldcg(d + 3 * n + 1), __ldcg(d + 3 * n + 2), 0.f);
+			const int t = b + k * blockDim.x;
+			const int hz = t % HZ, hx = (t / HZ) % HX, hy = t / (HZ * HX);
+			n[k] = (!zero && t < HN && hz >= 1 && hz <= L.noz && hx >= 1 && hx <= L.nox && hy >= 1 && hy <= L.noy)
+			           ? cg_node(L, hx - 1, hy - 1, hz - 1)
+			           : -1;
 		}
-		sd[t] = v;
+#pragma unroll
+		for(int k = 0; k < 4; ++k)
+			v[k] = n[k] >= 0 ? make_float4(__ldcg(d + 3 * n[k]), __ldcg(d + 3 * n[k] + 1), __ldcg(d + 3 * n[k] + 2), 0.f)
+			                 : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+		for(int k = 0; k < 4; ++k)
+			if(b + k * (int)blockDim.x < HN)
+				sd[b + k * blockDim.x] = v[k];
 	}
 }
 
@@ -326,41 +358,77 @@ __device__ void co_gs(cgp::cluster_group &cl, const Lvl &L, const float4 *Kt, co
 	}
 }
 
-// K u over this CTA's share of the level's positions, u in the halo grid sd.
-// MODE 0 (residual): out = f - K u.  MODE 1 (line search): out = K u and the
-// lane accumulates out.res and out.out in FP64 (lane r9 == 0 of each node).
+// K u over this CTA's nodes (its chunk of every colour, as in the smoother,
+// so that the halo values the smoother left are the ones needed here), u in
+// the halo grid sd.  MODE 0 (residual): out = f - K u.  MODE 1 (line search):
+// out = K u, and lane r9 == 0 of each node accumulates out.f and out.out
+// (in FP32 over its few nodes; the lanes' partials are then added in FP64).
+// The CTA's nodes are listed first (position, halo index, node index
+// in sloc, their count in *stot), then taken 48 at a time (one pass on the
+// small levels).
+constexpr int CO_MAX_OWN = 8 * CO_NODES;
+
+__device__ void co_list(const Lvl &L, int rank, int ncta, int4 *sloc, int *stot)
+{
+	__shared__ int pre[9], los[8];
+	if(threadIdx.x == 0)
+	{
+		int acc = 0;
+		for(int c = 0; c < 8; ++c)
+		{
+			int lo, cnt;
+			co_chunk(L.coff[c + 1] - L.coff[c], rank, ncta, lo, cnt);
+			pre[c] = acc;
+			los[c] = lo;
+			acc += cnt;
+		}
+		pre[8] = acc;
+		*stot = acc;
+	}
+	__syncthreads();
+	for(int t = threadIdx.x; t < pre[8]; t += blockDim.x)
+	{
+		int c = 0;
+		for(int k = 1; k < 8; ++k)
+			c += (t >= pre[k]);
+		const int q = los[c] + t - pre[c];
+		int x, y, z;
+		cg_decode(L, c, q, x, y, z);
+		sloc[t] = make_int4(L.coff[c] + q, co_halo(L, x, y, z), cg_node(L, x, y, z), 0);
+	}
+	__syncthreads();
+}
+
 template <int MODE>
-__device__ void co_kmul(const Lvl &L, const float4 *Kt, const float4 *sd, const float *f, float *out, int rank, int ncta, double &ab,
-                        double &aa)
+__device__ void co_kmul(const Lvl &L, const float4 *Kt, const float4 *sd, const float *f, float *out, float &ab, float &aa,
+                        const int4 *sloc, int tot)
 {
 	const int HZ = L.noz + 2, HXZ = (L.nox + 2) * HZ;
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	const int sub = lane / 9, r9 = lane - 9 * sub;
 	const int uoff = -1 + HZ * (r9 % 3 - 1) + HXZ * (r9 / 3 - 1);
-	// the CTA's nodes are its chunks of every colour, as in the smoother, so
-	// that the halo values the smoother left are the ones needed here
-	for(int c = 0; c < 8; ++c)
+	for(int b = 0; b < tot; b += CO_NODES)
 	{
-		int lo, cnt;
-		co_chunk(L.coff[c + 1] - L.coff[c], rank, ncta, lo, cnt);
-		for(int b = 0; b < cnt; b += CO_NODES)
-		{
-		const int q = b + 3 * warp + sub;
-		const bool act = lane < 27 && q < cnt;
-		float r0 = 0.f, r1 = 0.f, r2 = 0.f;
+		const int t = b + 3 * warp + sub;
+		const bool act = lane < 27 && t < tot;
+		float r0 = 0.f, r1 = 0.f, r2 = 0.f, f0 = 0.f, f1 = 0.f, f2 = 0.f;
 		int n = 0;
 		if(act)
 		{
-			const int p = L.coff[c] + lo + q;
-			int x, y, z;
-			cg_decode(L, c, lo + q, x, y, z);
-			n = cg_node(L, x, y, z);
+			const int4 e = sloc[t];
+			n = e.z;
+			if(r9 == 0)
+			{
+				f0 = __ldcg(f + 3 * n);
+				f1 = __ldcg(f + 3 * n + 1);
+				f2 = __ldcg(f + 3 * n + 2);
+			}
 			float4 k[7];
-			const float4 *kr = Kt + (size_t)63 * p + 7 * r9;
+			const float4 *kr = Kt + (size_t)63 * e.x + 7 * r9;
 #pragma unroll
-			for(int t = 0; t < 7; ++t)
-				k[t] = __ldg(kr + t);
-			kt_rows(k, sd + co_halo(L, x, y, z) + uoff, r0, r1, r2);
+			for(int u = 0; u < 7; ++u)
+				k[u] = __ldg(kr + u);
+			kt_rows(k, sd + e.y + uoff, r0, r1, r2);
 		}
 		r0 = kt_sum9(r0, lane);
 		r1 = kt_sum9(r1, lane);
@@ -369,21 +437,38 @@ __device__ void co_kmul(const Lvl &L, const float4 *Kt, const float4 *sd, const 
 		{
 			if(MODE == 0)
 			{
-				out[3 * n] = __ldcg(f + 3 * n) - r0;
-				out[3 * n + 1] = __ldcg(f + 3 * n + 1) - r1;
-				out[3 * n + 2] = __ldcg(f + 3 * n + 2) - r2;
+				out[3 * n] = f0 - r0;
+				out[3 * n + 1] = f1 - r1;
+				out[3 * n + 2] = f2 - r2;
 			}
 			else
 			{
 				out[3 * n] = r0;
 				out[3 * n + 1] = r1;
 				out[3 * n + 2] = r2;
-				ab += (double)r0 * (double)__ldcg(f + 3 * n) + (double)r1 * (double)__ldcg(f + 3 * n + 1) +
-				      (double)r2 * (double)__ldcg(f + 3 * n + 2);
-				aa += (double)r0 * (double)r0 + (double)r1 * (double)r1 + (double)r2 * (double)r2;
+				ab += r0 * f0 + r1 * f1 + r2 * f2;
+				aa += r0 * r0 + r1 * r1 + r2 * r2;
 			}
 		}
+	}
+}
+
+// vel += alpha del over this CTA's nodes (listed by co_list)
+__device__ void co_update(float *vel, const float *del, float alpha, const int4 *sloc, int tot)
+{
+	for(int t = threadIdx.x; t < tot; t += blockDim.x)
+	{
+		const int n = sloc[t].z;
+		float v[3], e[3];
+#pragma unroll
+		for(int i = 0; i < 3; ++i)
+		{
+			v[i] = __ldcg(vel + 3 * n + i);
+			e[i] = __ldcg(del + 3 * n + i);
 		}
+#pragma unroll
+		for(int i = 0; i < 3; ++i)
+			vel[3 * n + i] = v[i] + alpha * e[i];
 	}
 }
 
@@ -394,6 +479,8 @@ __global__ void __launch_bounds__(CO_THREADS) k_coarse(const __grid_constant__ C
 	__shared__ double wsum[CO_WARPS][2];
 	__shared__ double csum[CO_MAX_CLUSTER][2];  // per-CTA line-search partials, written by every CTA
 	__shared__ __align__(8) unsigned long long bars[2];  // transaction barriers of the cluster smoother
+	__shared__ int4 sloc[CO_MAX_OWN];                     // the CTA's nodes (co_list)
+	__shared__ int stot;
 	float4 *arena = reinterpret_cast<float4 *>(smem_raw);
 	cgp::cluster_group cl = cgp::this_cluster();
 	const int rank = (int)cl.block_rank(), ncta = (int)cl.num_blocks();
@@ -447,12 +534,14 @@ __global__ void __launch_bounds__(CO_THREADS) k_coarse(const __grid_constant__ C
 				halo_lev = l;
 				halo_vec = uvec;
 			}
-			double ab = 0.0, aa = 0.0;
+			float abf = 0.f, aaf = 0.f;
+			co_list(L, rank, ncta, sloc, &stot);
 			if(op.type == CO_RESID)
-				co_kmul<0>(L, D.Kt[l], arena, D.vec[l][op.a], D.vec[l][op.c], rank, ncta, ab, aa);
+				co_kmul<0>(L, D.Kt[l], arena, D.vec[l][op.a], D.vec[l][op.c], abf, aaf, sloc, stot);
 			else
 			{
-				co_kmul<1>(L, D.Kt[l], arena, D.vec[l][op.b], D.vec[l][op.c], rank, ncta, ab, aa);
+				co_kmul<1>(L, D.Kt[l], arena, D.vec[l][op.b], D.vec[l][op.c], abf, aaf, sloc, stot);
+				double ab = abf, aa = aaf;
 				// fixed-order sums: lanes, warps, then CTAs in rank order
 				for(int s = 16; s > 0; s >>= 1)
 				{
@@ -478,13 +567,25 @@ __global__ void __launch_bounds__(CO_THREADS) k_coarse(const __grid_constant__ C
 					dst[2 * rank + 1] = s1;
 				}
 				cl.sync();
-				double s0 = 0.0, s1 = 0.0;
-				for(int r = 0; r < ncta; ++r)
+				if(threadIdx.x == 0)
 				{
-					s0 += csum[r][0];
-					s1 += csum[r][1];
+					double s0 = 0.0, s1 = 0.0;
+					for(int r = 0; r < ncta; ++r)
+					{
+						s0 += csum[r][0];
+						s1 += csum[r][1];
+					}
+					wsum[0][0] = s0 / s1;  // one FP64 division, not one per thread
 				}
-				alpha = s0 / s1;
+				__syncthreads();
+				alpha = wsum[0][0];
+				if(op.zero)
+				{
+					// the update of the line search on the same nodes (vel += alpha del)
+					co_update(D.vec[l][CO_VEL], D.vec[l][op.a], (float)alpha, sloc, stot);
+					if(halo_lev == l && halo_vec == CO_VEL)
+						halo_lev = -1;
+				}
 			}
 			if(halo_lev == l && halo_vec == op.c)
 				halo_lev = -1;
@@ -506,27 +607,31 @@ __global__ void __launch_bounds__(CO_THREADS) k_coarse(const __grid_constant__ C
 		case CO_PROJ:
 		{
 			// vec b of level l-1 = projection of vec a of level l, stripped
+			// (the fine vector staged in shared memory, sums in FP32)
 			const Lvl &Lc = D.L[l - 1];
+			float *sv = reinterpret_cast<float *>(arena);
+			co_stage(D.vec[l][op.a], L.neq, sv);
 			int lo, cnt;
 			co_chunk(Lc.nno, rank, ncta, lo, cnt);
 			for(int b = 8 * lo; b < 8 * (lo + cnt); b += blockDim.x)
 			{
 				const int t = b + threadIdx.x;
-				project_lanes<true, float>(L, Lc, D.vec[l][op.a], D.vec[l - 1][op.b], t < 8 * (lo + cnt) ? t : 8 * Lc.nno);
+				project_lanes<false, float, float>(L, Lc, sv, D.vec[l - 1][op.b], t < 8 * (lo + cnt) ? t : 8 * Lc.nno);
 			}
-			if(halo_lev == l - 1 && halo_vec == op.b)
-				halo_lev = -1;
+			halo_lev = -1;
 			break;
 		}
 		case CO_INTERP:
 		{
 			// vec b of level l = interpolation of vec a of level l-1, stripped
+			// (the coarse vector staged in shared memory)
+			float *sv = reinterpret_cast<float *>(arena);
+			co_stage(D.vec[l - 1][op.a], D.L[l - 1].neq, sv);
 			int lo, cnt;
 			co_chunk(L.nno, rank, ncta, lo, cnt);
 			for(int n = lo + threadIdx.x; n < lo + cnt; n += blockDim.x)
-				interp_node<true, float>(D.L[l - 1], L, D.vec[l - 1][op.a], D.vec[l][op.b], n);
-			if(halo_lev == l && halo_vec == op.b)
-				halo_lev = -1;
+				interp_node<false, float>(D.L[l - 1], L, sv, D.vec[l][op.b], n);
+			halo_lev = -1;
 			break;
 		}
 		default:

@@ -94,11 +94,12 @@ template <bool CG, typename T> __device__ __forceinline__ T ldv(const T *p)
 // fine sub-element of that corner); the lanes' sums are added by shuffles.
 // Followed by strip_bcs_from_residual on the coarse level.  t is the lane's
 // global index (coarse node t / 8); all 32 lanes of a warp must call it.
-template <bool CG, typename T>
+// ACC: the type the sums are formed in.
+template <bool CG, typename T, typename ACC = double>
 __device__ __forceinline__ void project_lanes(const Lvl &Lf, const Lvl &Lc, const T *AU, T *AD, int t)
 {
 	const int N = t >> 3, a = t & 7;
-	double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+	ACC s0 = 0, s1 = 0, s2 = 0;
 	int cnt = 0;
 	int X = 0, Y = 0, Z = 0;
 	if(N < Lc.nno)
@@ -112,18 +113,18 @@ __device__ __forceinline__ void project_lanes(const Lvl &Lf, const Lvl &Lc, cons
 		{
 			cnt = 1;
 			const int fx = 2 * ex + ox, fy = 2 * ey + oy, fz = 2 * ez + oz;
-			double t0 = 0.0, t1 = 0.0, t2 = 0.0;
+			ACC t0 = 0, t1 = 0, t2 = 0;
 #pragma unroll
 			for(int b = 0; b < 8; ++b)
 			{
 				const int m = cg_node(Lf, fx + cg_loc(b, 0), fy + cg_loc(b, 1), fz + cg_loc(b, 2));
-				t0 += (double)ldv<CG>(AU + 3 * m);
-				t1 += (double)ldv<CG>(AU + 3 * m + 1);
-				t2 += (double)ldv<CG>(AU + 3 * m + 2);
+				t0 += (ACC)ldv<CG>(AU + 3 * m);
+				t1 += (ACC)ldv<CG>(AU + 3 * m + 1);
+				t2 += (ACC)ldv<CG>(AU + 3 * m + 2);
 			}
-			s0 = Lc.J * t0;
-			s1 = Lc.J * t1;
-			s2 = Lc.J * t2;
+			s0 = (ACC)Lc.J * t0;
+			s1 = (ACC)Lc.J * t1;
+			s2 = (ACC)Lc.J * t2;
 		}
 	}
 	// fixed-order sum over the 8 corners (lane a of the group holds corner a)
@@ -136,7 +137,7 @@ __device__ __forceinline__ void project_lanes(const Lvl &Lf, const Lvl &Lc, cons
 	}
 	if(N < Lc.nno && a == 0)
 	{
-		const double mass = 1.0 / ((double)cnt * Lc.J);
+		const ACC mass = (ACC)1 / ((ACC)cnt * (ACC)Lc.J);
 		const unsigned f = cg_vflag(Lc, X, Y, Z);
 		AD[3 * N] = (f & 1u) ? (T)0 : (T)(s0 * mass);
 		AD[3 * N + 1] = (f & 2u) ? (T)0 : (T)(s1 * mass);

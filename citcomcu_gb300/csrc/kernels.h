@@ -77,7 +77,7 @@ enum CoOpType
 	CO_RESID,   // vec c = vec a - K vec b
 	CO_PROJ,    // vec b (level lev-1) = projection of vec a (level lev), stripped
 	CO_INTERP,  // vec b (level lev) = interpolation of vec a (level lev-1), stripped
-	CO_KDOT,    // vec c = K vec a; alpha = (c . vec b) / (c . c), FP64
+	CO_KDOT,    // vec c = K vec a; alpha = (c . vec b) / (c . c), FP64; if `zero`: then vel += alpha vec a
 	CO_UPD      // vec a += alpha vec b
 };
 #define CO_MAX_LEV 6
