@@ -33,6 +33,7 @@ enum Slot
 	S_MIN = 20,
 	S_MAX = 21,
 	S_UZ = 22,    // Uzawa scalars: r1.z1, r0.z0, s2.Ahat, alpha, error flag
+	S_TERR = 31,  // (host mirror only) the tile kernels' error word
 	S_COUNT = 32
 };
 
@@ -159,9 +160,7 @@ void make_level(const citcom_gpu_config &c, int l, Lvl &L)
 	for(int a = 0; a < 3; ++a)
 		for(int p = 0; p < 2; ++p)
 			L.cnt[a][p] = (N[a] - p + 1) / 2;
-	L.coff[0] = 0;
-	for(int col = 0; col < 8; ++col)
-		L.coff[col + 1] = L.coff[col] + L.cnt[2][col & 1] * L.cnt[0][(col >> 1) & 1] * L.cnt[1][(col >> 2) & 1];
+	cg_set_offsets(L);
 	L.h[0] = c.dimen[0] / L.elx;
 	L.h[1] = c.dimen[1] / L.ely;
 	L.h[2] = c.dimen[2] / L.elz;
@@ -489,9 +488,13 @@ int solve_del2_u(citcom_gpu *h, double acc, int *valid)
 			return fail(h, CITCOM_GPU_ERR_NOCONV, "solve_del2_u: no convergence after %d multigrid passes (residual %g > %g)",
 			            count, residual, acc);
 		TRY(run_pass(h));
+		if(tile_error_async(h->hscal + S_TERR, h->st) != 0)
+			return fail(h, CITCOM_GPU_ERR_CUDA, "solve_del2_u: reading the tile kernels' error word failed");
 		TRY(readback(h, S_RES, 2));
 		if(h->hscal[S_ERR] != 0.0)
 			return fail(h, CITCOM_GPU_ERR_CUDA, "solve_del2_u: a wait of the cluster smoother timed out");
+		if(h->hscal[S_TERR] != 0.0)
+			return fail(h, CITCOM_GPU_ERR_CUDA, "solve_del2_u: a stencil tile copy did not arrive");
 		residual = std::sqrt(h->hscal[S_RES] / neq);
 		for(int k = 0; k < h->n_gs_pairs; ++k)
 		{
@@ -884,13 +887,13 @@ int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 			h->BI32[l] = nullptr;
 			if(need64)
 			{
-				TRYC(dalloc(h, &h->K64[l], (size_t)243 * L.npad));
+				TRYC(dalloc(h, &h->K64[l], cg_kwords(L)));
 				TRYC(dalloc(h, &h->BI64[l], (size_t)3 * L.npad));
 			}
 			h->Kt32[l] = nullptr;
 			if(need32)
 			{
-				TRYC(dalloc(h, &h->K32[l], (size_t)243 * L.npad));
+				TRYC(dalloc(h, &h->K32[l], cg_kwords(L)));
 				TRYC(dalloc(h, &h->BI32[l], (size_t)3 * L.npad));
 				if(gs_tiny_fits(L, sizeof(float)) || l <= h->co_LC)
 					TRYC(dalloc(h, &h->Kt32[l], (size_t)63 * L.nno));

@@ -1566,14 +1566,19 @@ static int max_colour(const Lvl &L)
 	return m;
 }
 
+// tiled levels go to the bulk-copy kernels of tile.cu, small levels to the slot kernels here
 template <typename T> void launch_kmul(cudaStream_t st, const Lvl &L, const T *K, const T *u, T *Au)
 {
+	if(!L.aos)
+		return launch_tile_kmul<T>(st, L, K, u, Au);
 	dim3 grid((max_colour(L) + NB - 1) / NB, 8);
 	launch_k(k_kmul<T, 0>, grid, SLOT_THREADS, st, L, K, u, (const T *)nullptr, Au);
 }
 
 template <typename T> void launch_residual(cudaStream_t st, const Lvl &L, const T *K, const T *f, const T *u, T *r)
 {
+	if(!L.aos)
+		return launch_tile_residual<T>(st, L, K, f, u, r);
 	dim3 grid((max_colour(L) + NB - 1) / NB, 8);
 	launch_k(k_kmul<T, 1>, grid, SLOT_THREADS, st, L, K, u, f, r);
 }
@@ -1587,6 +1592,8 @@ void launch_kmul_linesearch(cudaStream_t st, const Lvl &L, const T *K, const T *
 
 template <typename T> void launch_gs_colour(cudaStream_t st, const Lvl &L, const T *K, const T *BI, const T *F, T *d, int c)
 {
+	if(!L.aos)
+		return launch_tile_gs<T>(st, L, K, BI, F, d, c);
 	const int n = L.coff[c + 1] - L.coff[c];
 	if(n > 0)
 	{
@@ -1633,7 +1640,7 @@ int kernels_init()
 	for(cudaError_t x : e)
 		if(x != cudaSuccess)
 			return -1;
-	return 0;
+	return tile_init();
 }
 
 void launch_tiny_stencil(cudaStream_t st, const Lvl &L, const float *K32, float4 *Kt)

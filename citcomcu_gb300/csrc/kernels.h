@@ -112,6 +112,14 @@ int coarse_window(const Lvl &L, int cluster);
 size_t coarse_smem(const Lvl &L, bool local);
 void launch_coarse(cudaStream_t st, const CoLevels &D, const CoProg &P, int cluster, size_t smem);
 
+// Stencil kernels of the tiled (large) levels, tile.cu: persistent CTAs
+// streaming tiles through shared memory with bulk copies
+int tile_init();                                   // attributes and grid sizes; 0 on success
+int tile_error_async(double *host, cudaStream_t st);  // 1 in *host if a stage wait ever timed out
+template <typename T> void launch_tile_gs(cudaStream_t st, const Lvl &L, const T *K, const T *BI, const T *F, T *d, int colour);
+template <typename T> void launch_tile_kmul(cudaStream_t st, const Lvl &L, const T *K, const T *u, T *out);
+template <typename T> void launch_tile_residual(cudaStream_t st, const Lvl &L, const T *K, const T *f, const T *u, T *out);
+
 // FP64 element operators
 void launch_div(cudaStream_t st, const Lvl &L, const Geo *geo, const double *U, double *divU);
 void launch_grad(cudaStream_t st, const Lvl &L, const Geo *geo, const double *P, double *gradP);

@@ -18,10 +18,12 @@ struct Lvl
 	int nox, noy, noz;
 	int nno, nel, neq;
 	int elx, ely, elz;
-	int npad;        // stride of the structure-of-arrays coefficient storage
-	int aos;         // 1: small level, stencil stored node by node (243 contiguous words per node, slot fastest)
+	int npad;        // nno rounded up to a multiple of 32 (length of the per-node arrays)
+	int aos;         // 1: small level, stencil stored node by node (243 contiguous words per node, slot fastest);
+	                 // 0: stencil stored by tiles of 16 positions of one colour
 	int cnt[3][2];   // number of indices of parity p along axis (0 x, 1 y, 2 z)
 	int coff[9];     // colour offsets in colour-major order
+	int toff[9];     // first tile of each colour (tiles of CG_TILE positions, a colour's last one partial)
 	double h[3];     // element edge lengths (uniform per axis)
 	double J;        // Jacobian determinant hx*hy*hz/8
 };
@@ -68,17 +70,44 @@ CG_HD int cg_loc(int a, int d)
 	return d == 0 ? (((a & 3) == 1) || ((a & 3) == 2)) : d == 1 ? ((a & 3) >= 2) : (a >= 4);
 }
 
-// stencil coefficient (neighbour slot s = (dz+1) + 3(dx+1) + 9(dy+1), row i,
-// column j) of the node at colour-major position p: 81 arrays of 3*npad
-// words; the three rows of a node are adjacent, so the three threads that own
-// a node's rows read consecutive words.  Small levels keep a node's 243 words
-// together with the slot fastest, so the 27 lanes of a warp that relax one
-// node read 27 consecutive words per (row, column) entry.
+// Stencil coefficient (neighbour slot s = (dz+1) + 3(dx+1) + 9(dy+1), row i,
+// column j) of the node at colour-major position p.  Large levels: tiles of
+// CG_TILE consecutive positions of one colour, each tile one contiguous block
+// of 243 * CG_TILE words ordered [s][j][node][i] -- one bulk copy brings a
+// tile into shared memory, where the 32 lanes of a warp (32 nodes, one slot)
+// read a word each without bank conflicts.  Small levels keep a node's 243
+// words together with the slot fastest, so the 27 lanes of a warp that relax
+// one node read 27 consecutive words per (row, column) entry.
+#define CG_TILE 32
+#define CG_TILE_WORDS (243 * CG_TILE)
 CG_HD size_t cg_kidx(const Lvl &L, int s, int i, int j, int p)
 {
 	if(L.aos)
 		return (size_t)243 * p + 27 * (3 * i + j) + s;
-	return (size_t)(3 * s + j) * 3 * (size_t)L.npad + 3 * (size_t)p + i;
+	int c = 0;
+	for(int k = 1; k < 8; ++k)
+		c += (p >= L.coff[k]);
+	const int q = p - L.coff[c];
+	return (size_t)(L.toff[c] + q / CG_TILE) * CG_TILE_WORDS + (size_t)((3 * s + j) * CG_TILE + q % CG_TILE) * 3 + i;
+}
+
+// words of the stencil storage of a level
+CG_HD size_t cg_kwords(const Lvl &L)
+{
+	return L.aos ? (size_t)243 * L.npad : (size_t)L.toff[8] * CG_TILE_WORDS;
+}
+
+// colour offsets and tile offsets from the per-axis parity counts
+CG_HD void cg_set_offsets(Lvl &L)
+{
+	L.coff[0] = 0;
+	L.toff[0] = 0;
+	for(int c = 0; c < 8; ++c)
+	{
+		const int n = L.cnt[2][c & 1] * L.cnt[0][(c >> 1) & 1] * L.cnt[1][(c >> 2) & 1];
+		L.coff[c + 1] = L.coff[c] + n;
+		L.toff[c + 1] = L.toff[c] + (n + CG_TILE - 1) / CG_TILE;
+	}
 }
 
 // levels up to this many nodes keep the node-by-node layout and are smoothed

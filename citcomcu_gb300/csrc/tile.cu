@@ -1,0 +1,318 @@
+// Stencil kernels of the large levels (K u, residual, one Gauss-Seidel
+// colour) on the tile-major stencil (level.h: tiles of 32 positions of one
+// colour, 243 * 32 words each).
+//
+// These kernels are bound by HBM bandwidth: a colour sweep of the finest
+// FP32 level streams 38 MB of stencil and reuses the L2-resident vector.  The
+// CTAs are persistent; each walks its tiles (blockIdx.x, + gridDim.x, ...) and
+// keeps S of them in flight: one thread issues a bulk copy (cp.async.bulk,
+// the TMA engine, no registers) of a whole tile into a shared-memory stage
+// and arms the stage's transaction barrier, so a tile's 31 KB (FP32) or 62 KB
+// (FP64) arrive while the CTA computes on the stage before.  A CTA is nine
+// warps: warp g takes the column of three slots (dx, dy) = (g % 3 - 1,
+// g / 3 - 1), dz = -1, 0, 1, for the 32 nodes of the tile (lane = node), so
+// a lane reads its node's three neighbours in that column (loaded one tile
+// ahead, overlapping the copy), multiplies them by 27 stencil words of the
+// stage (lane-consecutive, conflict-free) and leaves three partial rows in
+// shared memory; the owner threads of (node, row) add the nine partials in
+// column order and update.  Few instructions per node, so the copy engine and
+// HBM set the pace.  Waits are bounded: a stage that does not arrive sets an
+// error word, no further copy is issued, and the CTA waits (bounded) for the
+// copies it has in flight before it leaves.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "kernels.h"
+
+namespace {
+
+#include "device.cuh"
+
+constexpr int TB = CG_TILE;  // nodes per tile = lanes of a warp
+constexpr int TT = 9 * 32;   // threads: nine warps, one per column of three slots
+static_assert(TB == 32, "one lane per node of a tile");
+template <typename T> struct TileCfg
+{
+	static constexpr int STAGES = sizeof(T) == 4 ? 3 : 2;
+	static constexpr int MIN_CTAS = sizeof(T) == 4 ? 2 : 1;  // per SM
+	static constexpr unsigned BYTES = CG_TILE_WORDS * sizeof(T);
+	static constexpr size_t SMEM = (size_t)STAGES * CG_TILE_WORDS * sizeof(T) + 2 * 27 * TB * sizeof(T);
+};
+
+enum
+{
+	TK_GS = 0,   // out = d: one Gauss-Seidel colour
+	TK_KU = 1,   // out = K u
+	TK_RES = 2   // out = f - K u
+};
+
+__device__ __forceinline__ unsigned t_smem(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void t_issue(unsigned bar, unsigned dst, const void *src, unsigned bytes)
+{
+	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+	asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst), "l"(src),
+	             "r"(bytes), "r"(bar)
+	             : "memory");
+}
+
+// bounded wait (about a second at most) for the phase of `bar` with this parity
+__device__ __forceinline__ bool t_wait(unsigned bar, unsigned parity)
+{
+	for(int it = 0; it < (1 << 17); ++it)
+	{
+		unsigned ok;
+		asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+		             : "=r"(ok)
+		             : "r"(bar), "r"(parity), "r"(10000u)
+		             : "memory");
+		if(ok)
+			return true;
+	}
+	return false;
+}
+
+__device__ double g_tile_err;  // 1 when a stage wait timed out
+
+template <typename T, int KIND>
+__global__ void __launch_bounds__(TT, TileCfg<T>::MIN_CTAS) k_tile(Lvl L, const T *__restrict__ K, const T *__restrict__ BI,
+                                                                  const T *__restrict__ f, const T *u, T *out, int colour)
+{
+	pdl_begin();
+	constexpr int S = TileCfg<T>::STAGES;
+	extern __shared__ __align__(128) unsigned char smem_raw[];
+	T *stage = reinterpret_cast<T *>(smem_raw);
+	T *part = stage + S * CG_TILE_WORDS;  // two buffers of 81 * TB partial rows
+	__shared__ __align__(8) unsigned long long bar[S];
+	const int t0 = KIND == TK_GS ? L.toff[colour] : 0;
+	const int t1 = KIND == TK_GS ? L.toff[colour + 1] : L.toff[8];
+	const int ntile = t1 - t0;
+	const int nmine = (int)blockIdx.x < ntile ? (ntile - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+	const unsigned bar0 = t_smem(bar), st0 = t_smem(stage);
+	auto issue = [&](int k) {
+		const int b = k % S;
+		const size_t tile = (size_t)t0 + blockIdx.x + (size_t)k * gridDim.x;
+		t_issue(bar0 + 8 * b, st0 + b * TileCfg<T>::BYTES, K + tile * CG_TILE_WORDS, TileCfg<T>::BYTES);
+	};
+	if(threadIdx.x == 0)
+	{
+		for(int b = 0; b < S; ++b)
+			asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0 + 8 * b) : "memory");
+		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+	}
+	__syncthreads();
+	int issued = 0;
+	if(threadIdx.x == 0)
+		for(; issued < S && issued < nmine; ++issued)
+			issue(issued);
+	bool ok = true;
+	const int ln = threadIdx.x & 31, g = threadIdx.x >> 5;
+	const int dx = g % 3 - 1, dy = g / 3 - 1;
+	const int oq = threadIdx.x / 3, oi = threadIdx.x % 3;  // owner (node, row), threadIdx.x < 3 * cnt
+	// a tile's owner data and the lane's nine neighbour values, loaded one
+	// tile ahead so that their latency overlaps the previous tile's work
+	struct Pre
+	{
+		int cnt, on;
+		T fi, bi, di;
+		T uv[9];  // [dz + 1][component]
+	};
+	auto prefetch = [&](int k, Pre &q) {
+		q.cnt = 0;
+		if(k >= nmine)
+			return;
+		const int tile = t0 + blockIdx.x + k * gridDim.x;
+		int cc = colour;
+		if(KIND != TK_GS)
+		{
+			cc = 0;
+#pragma unroll
+			for(int m = 1; m < 8; ++m)
+				cc += (tile >= L.toff[m]);
+		}
+		const int q0 = (tile - L.toff[cc]) * TB;
+		q.cnt = min(TB, L.coff[cc + 1] - L.coff[cc] - q0);
+		q.on = 0;
+		q.fi = q.bi = q.di = 0;
+		if((int)threadIdx.x < 3 * q.cnt)
+		{
+			int x, y, z;
+			cg_decode(L, cc, q0 + oq, x, y, z);
+			q.on = cg_node(L, x, y, z);
+			if(KIND != TK_KU)
+				q.fi = f[3 * q.on + oi];
+			if(KIND == TK_GS)
+			{
+				q.bi = BI[3 * (size_t)(L.coff[cc] + q0 + oq) + oi];
+				q.di = u[3 * q.on + oi];
+			}
+		}
+#pragma unroll
+		for(int e = 0; e < 9; ++e)
+			q.uv[e] = 0;
+		if(ln < q.cnt)
+		{
+			int x, y, z;
+			cg_decode(L, cc, q0 + ln, x, y, z);
+			const int col = cg_node(L, clampi(x + dx, 0, L.nox - 1), clampi(y + dy, 0, L.noy - 1), 0);
+#pragma unroll
+			for(int kz = 0; kz < 3; ++kz)
+			{
+				// missing neighbours are clamped onto the node: their stencil block is zero
+				const int m = col + clampi(z + kz - 1, 0, L.noz - 1);
+				q.uv[3 * kz] = u[3 * m];
+				q.uv[3 * kz + 1] = u[3 * m + 1];
+				q.uv[3 * kz + 2] = u[3 * m + 2];
+			}
+		}
+	};
+	Pre cur;
+	prefetch(0, cur);
+	for(int k = 0; k < nmine; ++k)
+	{
+		const int b = k % S;
+		if(ok)
+			ok = t_wait(bar0 + 8 * b, (unsigned)((k / S) & 1));
+		T *pb = part + (k & 1) * 27 * TB;
+		const int cnt = cur.cnt;
+		if(ln < cnt)
+		{
+			// slots 3g .. 3g+2 (dz = -1, 0, 1): word ((3s + j) * TB + ln) * 3 + i of the stage
+			const T *ks = stage + (size_t)b * CG_TILE_WORDS + (9 * g * TB + ln) * 3;
+			T a0 = 0, a1 = 0, a2 = 0;
+#pragma unroll
+			for(int kz = 0; kz < 3; ++kz)
+#pragma unroll
+				for(int j = 0; j < 3; ++j)
+				{
+					const T *kw = ks + (3 * kz + j) * TB * 3;
+					const T uj = cur.uv[3 * kz + j];
+					a0 += kw[0] * uj;
+					a1 += kw[1] * uj;
+					a2 += kw[2] * uj;
+				}
+			pb[(g * 3 + 0) * TB + ln] = a0;
+			pb[(g * 3 + 1) * TB + ln] = a1;
+			pb[(g * 3 + 2) * TB + ln] = a2;
+		}
+		const int on = cur.on;
+		const T fi = cur.fi, bi = cur.bi, di = cur.di;
+		// a Gauss-Seidel colour never reads values of its own colour, so the
+		// next tile's loads may start before this tile's updates land
+		prefetch(k + 1, cur);
+		__syncthreads();  // stage b read by every thread; partials complete
+		if(threadIdx.x == 0 && ok && issued < nmine)
+		{
+			// the threads' reads of stage b are ordered before the copy that refills it
+			asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+			issue(issued++);
+		}
+		if((int)threadIdx.x < 3 * cnt)
+		{
+			T r = 0;
+#pragma unroll
+			for(int gg = 0; gg < 9; ++gg)
+				r += pb[(gg * 3 + oi) * TB + oq];
+			if(KIND == TK_GS)
+				out[3 * on + oi] = di + (fi - r) * bi;
+			else if(KIND == TK_KU)
+				out[3 * on + oi] = r;
+			else
+				out[3 * on + oi] = fi - r;
+		}
+	}
+	if(!ok)
+	{
+		g_tile_err = 1.0;
+		// thread 0 issued every copy: the ones still in flight land before the CTA leaves
+		if(threadIdx.x == 0)
+			for(int k = max(0, issued - S); k < issued; ++k)
+				t_wait(bar0 + 8 * (k % S), (unsigned)((k / S) & 1));
+	}
+}
+
+template <typename T> struct TileGrid
+{
+	static int ctas;  // persistent CTAs: SMs x resident CTAs per SM
+};
+template <typename T> int TileGrid<T>::ctas = 0;
+
+template <typename T> int tile_init_t(int sms)
+{
+	const int smem = (int)TileCfg<T>::SMEM;
+	cudaError_t e = cudaSuccess;
+	int occ = 0;
+	for(auto fn : {k_tile<T, TK_GS>, k_tile<T, TK_KU>, k_tile<T, TK_RES>})
+	{
+		if(e == cudaSuccess)
+			e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+		int o = 0;
+		if(e == cudaSuccess)
+			e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, fn, TT, smem);
+		occ = occ ? std::min(occ, o) : o;
+	}
+	if(e != cudaSuccess || occ < 1)
+		return -1;
+	TileGrid<T>::ctas = sms * occ;
+	return 0;
+}
+
+template <typename T, int KIND>
+void launch_tile(cudaStream_t st, const Lvl &L, const T *K, const T *BI, const T *f, const T *u, T *out, int colour)
+{
+	const int ntile = KIND == TK_GS ? L.toff[colour + 1] - L.toff[colour] : L.toff[8];
+	if(ntile <= 0)
+		return;
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim = dim3(std::min(ntile, std::max(1, TileGrid<T>::ctas)));
+	cfg.blockDim = dim3(TT);
+	cfg.dynamicSmemBytes = TileCfg<T>::SMEM;
+	cfg.stream = st;
+	cudaLaunchAttribute attr[1];
+	attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+	attr[0].val.programmaticStreamSerializationAllowed = 1;
+	cfg.attrs = attr;
+	cfg.numAttrs = g_use_pdl ? 1 : 0;
+	cudaLaunchKernelEx(&cfg, k_tile<T, KIND>, L, K, BI, f, u, out, colour);
+	++g_kernel_launches;
+}
+
+} // namespace
+
+int tile_init()
+{
+	int dev = 0, sms = 0;
+	if(cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+		return -1;
+	if(tile_init_t<float>(sms) != 0 || tile_init_t<double>(sms) != 0)
+		return -1;
+	return 0;
+}
+
+int tile_error_async(double *host, cudaStream_t st)
+{
+	return cudaMemcpyFromSymbolAsync(host, g_tile_err, sizeof(double), 0, cudaMemcpyDeviceToHost, st) == cudaSuccess ? 0 : -1;
+}
+
+template <typename T> void launch_tile_gs(cudaStream_t st, const Lvl &L, const T *K, const T *BI, const T *F, T *d, int colour)
+{
+	launch_tile<T, TK_GS>(st, L, K, BI, F, d, d, colour);
+}
+
+template <typename T> void launch_tile_kmul(cudaStream_t st, const Lvl &L, const T *K, const T *u, T *out)
+{
+	launch_tile<T, TK_KU>(st, L, K, (const T *)nullptr, (const T *)nullptr, u, out, 0);
+}
+
+template <typename T> void launch_tile_residual(cudaStream_t st, const Lvl &L, const T *K, const T *f, const T *u, T *out)
+{
+	launch_tile<T, TK_RES>(st, L, K, (const T *)nullptr, f, u, out, 0);
+}
+
+#define TILE_INST(T)                                                                                         \
+	template void launch_tile_gs<T>(cudaStream_t, const Lvl &, const T *, const T *, const T *, T *, int);   \
+	template void launch_tile_kmul<T>(cudaStream_t, const Lvl &, const T *, const T *, T *);                 \
+	template void launch_tile_residual<T>(cudaStream_t, const Lvl &, const T *, const T *, const T *, T *);
+TILE_INST(float)
+TILE_INST(double)

@@ -21,8 +21,7 @@ static Lvl make(int ex, int ey, int ez)
 	for(int a = 0; a < 3; ++a)
 		for(int p = 0; p < 2; ++p)
 			L.cnt[a][p] = (N[a] - p + 1) / 2;
-	for(int c = 0; c < 8; ++c)
-		L.coff[c + 1] = L.coff[c] + L.cnt[2][c & 1] * L.cnt[0][(c >> 1) & 1] * L.cnt[1][(c >> 2) & 1];
+	cg_set_offsets(L);
 	return L;
 }
 
@@ -57,22 +56,27 @@ int main()
 		for(int n = 0; n < L.nno; ++n)
 			if(seen[n] != 1)
 				return fail("bijection", n, seen[n]);
-		std::vector<unsigned char> used((size_t)243 * L.npad, 0);
+		std::vector<unsigned char> used(cg_kwords(L), 0);
 		for(int p = 0; p < L.nno; ++p)
 			for(int s = 0; s < 27; ++s)
 				for(int i = 0; i < 3; ++i)
 					for(int j = 0; j < 3; ++j)
 					{
 						const size_t k = cg_kidx(L, s, i, j, p);
-						if(k >= (size_t)243 * L.npad)
+						if(k >= cg_kwords(L))
 							return fail("kidx range", p, s);
 						if(used[k]++)
 							return fail("kidx unique", p, s);
-						// slot_partial: structure-of-arrays kc = K + 3s*s3 + 3p, loads kc + j*s3 + i;
+						// tiled: a tile is CG_TILE consecutive positions of one colour, the
+						// lane of node ln reads tile word ((3s + j) * CG_TILE + ln) * 3 + i;
 						// node-by-node kc = K + 243p + s, loads kc + 27(3i + j)
-						const size_t s3 = 3 * (size_t)L.npad;
+						int c = 0;
+						while(p >= L.coff[c + 1])
+							++c;
+						const int q = p - L.coff[c];
 						const size_t expect = aos ? (size_t)243 * p + s + 27 * (3 * i + j)
-						                          : 3 * (size_t)p + i + (size_t)(3 * s) * s3 + j * s3;
+						                          : (size_t)(L.toff[c] + q / CG_TILE) * 243 * CG_TILE +
+						                                ((3 * s + j) * CG_TILE + q % CG_TILE) * 3 + i;
 						if(expect != k)
 							return fail("gather pattern", p, s);
 					}
