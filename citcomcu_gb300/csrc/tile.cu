@@ -79,7 +79,6 @@ template <typename T, int KIND>
 __global__ void __launch_bounds__(TT, TileCfg<T>::MIN_CTAS) k_tile(Lvl L, const T *__restrict__ K, const T *__restrict__ BI,
                                                                   const T *__restrict__ f, const T *u, T *out, int colour)
 {
-	pdl_begin();
 	constexpr int S = TileCfg<T>::STAGES;
 	extern __shared__ __align__(128) unsigned char smem_raw[];
 	T *stage = reinterpret_cast<T *>(smem_raw);
@@ -106,6 +105,11 @@ __global__ void __launch_bounds__(TT, TileCfg<T>::MIN_CTAS) k_tile(Lvl L, const 
 	if(threadIdx.x == 0)
 		for(; issued < S && issued < nmine; ++issued)
 			issue(issued);
+	// The stencil is written only by the assembly, long before any launch
+	// here, so its first copies start before the wait on the preceding kernel
+	// (under programmatic dependent launch they overlap that kernel's tail);
+	// the vectors, which the preceding kernel may write, are read after it.
+	pdl_begin();
 	bool ok = true;
 	const int ln = threadIdx.x & 31, g = threadIdx.x >> 5;
 	const int dx = g % 3 - 1, dy = g / 3 - 1;

@@ -14,6 +14,12 @@ def test_device_index_arithmetic_on_host():
         assert out.returncode == 0 and out.stdout.strip() == "OK", out.stdout
 
 
+# Kernels that start work before their wait on the predecessor, and what that
+# work reads: the tile kernels start the bulk copies of their first stencil
+# tiles (the stencil is written only by the assembly, several kernels earlier).
+EARLY_WORK = {"tile.cu:k_tile": "cp.async.bulk of stencil tiles"}
+
+
 def test_every_kernel_waits_for_its_predecessor():
     # every kernel is launched with programmatic dependent launch, so each
     # must execute griddepcontrol.wait (pdl_begin) before it touches memory
@@ -26,8 +32,14 @@ def test_every_kernel_waits_for_its_predecessor():
             continue
         src = open(os.path.join(csrc, name)).read()
         for m in re.finditer(r"__global__[^{;]*?\b(k_\w+)\s*\([^)]*\)\s*\{", src, re.S):
+            key = f"{name}:{m.group(1)}"
+            if key in EARLY_WORK:
+                body = src[m.end():m.end() + 4000]
+                if "pdl_begin()" not in body:
+                    missing.append(key)
+                continue
             body = src[m.end():m.end() + 600]
             first = body.split(";")[0]
             if "pdl_begin()" not in first:
-                missing.append(f"{name}:{m.group(1)}")
+                missing.append(key)
     assert not missing, missing
