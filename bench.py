@@ -12,13 +12,18 @@ loop (forces, viscosity, operator assembly, Uzawa/multigrid solve, V), on
 state resident in HBM.  Every step therefore does the same work, and the CPU
 baseline (the same solve by the reference's algorithm) is directly
 comparable.  `value` is the mean device time per solve in the headline
-configuration (FP32 multigrid inside FP64 refinement); the FP64 plain path is
-timed the same way and reported beside it; `ms_per_step` adds one SUPG
-time step (PG_timestep).  `e2e` times the same solve through the C ABI with
+configuration: FP32 multigrid inside FP64 refinement, started from the learned
+warm start (the network's guess when its Uzawa initial residual beats the zero
+start).  The network is trained online first, on converged solves of other
+seeds (1..10: each seed's cold solve and the 4 time steps after it, 50
+snapshots, 1000 Adam steps); the training time is reported, not timed into
+`value`.  The same solve without the network and the FP64 plain path are
+timed the same way and reported beside it; `ms_per_step` adds one SUPG time
+step (PG_timestep).  `e2e` times the headline solve through the C ABI with
 host buffers (pinned), the copies included.
 
   python bench.py [--steps K] [--warmup W] [--gpus N] [--impl reference]
-                  [--size 64|32] [--no-cpu]
+                  [--size 64|32] [--no-cpu] [--no-learned]
 """
 from __future__ import annotations
 
@@ -54,8 +59,8 @@ def workload(size: int):
                   viscE=(math.log(1e3),), viscT=(0.0,), accuracy=1e-6, piterations=375)
 
 
-def seeded_T0(case):
-    rng = np.random.Generator(np.random.PCG64(0))
+def seeded_T0(case, seed: int = 0):
+    rng = np.random.Generator(np.random.PCG64(seed))
     z = np.linspace(0.0, case.dimen[2], case.noz)
     T = np.empty((case.noy, case.nox, case.noz))
     T[:] = 1.0 - z / case.dimen[2]
@@ -160,6 +165,58 @@ def run_mode(cg, case, precision, T0, steps, warmup):
 TRAFFIC_PER_LAUNCH_64 = 38.57e6
 
 
+def train_warm_start(cg, case, T0_of, seeds: int, steps_per_seed: int, train_steps: int):
+    """The learned warm start, trained online on the plain solver's own
+    converged solves: for each training seed (never the benchmark's seed 0) a
+    cold solve of its initial state and the time steps that follow, each
+    recorded; then Adam steps on random minibatches of the snapshots."""
+    s = cg.Solver(cg.Config.like(case, precision=cg.MIXED))
+    f = s.fine
+    n = cg.WarmStart(s, seed=7, capacity=seeds * (steps_per_seed + 1))
+    zn, zu, zp = np.zeros(f["nno"]), np.zeros(f["neq"]), np.zeros(f["nel"])
+    t0 = time.perf_counter()
+    for seed in range(1, seeds + 1):
+        s.load_state(T=T0_of(seed), Tdot=zn, U=zu, P=zp)
+        s.stokes_resident()
+        n.record()
+        for _ in range(steps_per_seed):
+            s.step_resident(0.0)
+            n.record()
+    t1 = time.perf_counter()
+    losses = [n.train(1, 4, 1e-3)]
+    for _ in range(4):
+        losses.append(n.train(train_steps // 4, 4, 1e-3))
+    t2 = time.perf_counter()
+    info = {"snapshots": n.recorded, "seeds": seeds, "steps_per_seed": steps_per_seed, "adam_steps": train_steps,
+            "batch": 4, "lr": 1e-3, "loss_first": losses[0], "loss_final": losses[-1], "record_s": t1 - t0,
+            "train_s": t2 - t1, "network_grid": list(n.grid), "params": n.n_params}
+    return s, n, info
+
+
+def run_learned(cg, case, T0, steps, warmup, solver, net):
+    """Cold solves of the benchmark state with the warm start attached: each
+    solve runs the network on the state, compares the Uzawa initial residual
+    of its guess with that of the zero start and iterates from the better."""
+    s, n = solver, net
+    f = s.fine
+    n.attach(True)
+    zn, zu, zp = np.zeros(f["nno"]), np.zeros(f["neq"]), np.zeros(f["nel"])
+    recs = []
+    l0 = None
+    for i in range(warmup + steps):
+        s.load_state(T=T0, Tdot=zn, U=zu, P=zp)
+        if i == warmup:
+            l0 = s.stats()["kernel_launches"]
+        s.stokes_resident()
+        if i >= warmup:
+            recs.append(s.stats())
+    launches = s.stats()["kernel_launches"] - l0
+    res = s.stokes_residuals()
+    nu = s.heat_flux()
+    vr = s.vrms()
+    return recs, launches, res, nu, vr
+
+
 def bytes_per_sweep(nno: int, word: int) -> int:
     """Algorithmic bytes of one Gauss-Seidel sweep (8 colour launches) on a
     level with stored 27-block stencils: the 243 coefficients and 3 inverse
@@ -168,11 +225,10 @@ def bytes_per_sweep(nno: int, word: int) -> int:
     return nno * word * (243 + 3 + 3 + 3 + 8 * 3)
 
 
-def e2e_mode(cg, case, T0, steps, warmup):
+def e2e_mode(cg, s, T0, steps, warmup):
     """The same cold solve through the C ABI with host buffers: each call
     copies T, U, P host->device and U, P, V device->host (pinned memory)."""
     import torch
-    s = cg.Solver(cg.Config.like(case, precision=cg.MIXED))
     f = s.fine
 
     def pinned(n):
@@ -189,7 +245,6 @@ def e2e_mode(cg, case, T0, steps, warmup):
         t1 = time.perf_counter()
         if i >= warmup:
             ms.append(1e3 * (t1 - t0))
-    s.close()
     h2d = 8 * (f["nno"] + f["neq"] + f["nel"])
     d2h = 8 * (f["neq"] + f["nel"] + 3 * f["nno"])
     return float(np.mean(ms)), h2d, d2h
@@ -264,6 +319,11 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--modes", default="both", choices=["both", "mixed"],
                     help="'mixed' skips the FP64 plain comparison (profiling runs)")
+    ap.add_argument("--no-learned", action="store_true",
+                    help="headline without the learned warm start (profiling runs)")
+    ap.add_argument("--learn-seeds", type=int, default=10)
+    ap.add_argument("--learn-steps", type=int, default=4, help="time steps recorded after each seed's cold solve")
+    ap.add_argument("--learn-adam", type=int, default=1000, help="Adam steps of the online training")
     ap.add_argument("--piterations", type=int, default=375,
                     help="Uzawa iteration cap; lower values only for short profiling runs")
     args = ap.parse_args()
@@ -291,21 +351,30 @@ def main():
             torch.distributed.barrier()
 
     barrier()
+    learned = None
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
         mixed, launches, res_mixed, nu_mixed, vr_mixed, energy_ms = run_mode(cg, case, cg.MIXED, T0, args.steps,
                                                                             args.warmup)
         t1 = time.perf_counter()
-    barrier()
-    if args.modes == "both":
-        fp64, _, res_fp64, nu_fp64, vr_fp64, _ = run_mode(cg, case, cg.FP64, T0, args.steps, args.warmup)
-    else:
-        fp64, res_fp64, nu_fp64, vr_fp64 = mixed, res_mixed, nu_mixed, vr_mixed
+        if args.modes == "both":
+            fp64, _, res_fp64, nu_fp64, vr_fp64, _ = run_mode(cg, case, cg.FP64, T0, args.steps, args.warmup)
+        else:
+            fp64, res_fp64, nu_fp64, vr_fp64 = mixed, res_mixed, nu_mixed, vr_mixed
+        if not args.no_learned:
+            ls, ln, train_info = train_warm_start(cg, case, lambda sd: seeded_T0(case, sd), args.learn_seeds,
+                                                  args.learn_steps, args.learn_adam)
+            t2 = time.perf_counter()
+            lrecs, llaunches, res_l, nu_l, vr_l = run_learned(cg, case, T0, args.steps, args.warmup, ls, ln)
+            t3 = time.perf_counter()
+            learned = (lrecs, llaunches, res_l, nu_l, vr_l, train_info, t3 - t2)
     barrier()
 
-    stokes_ms = float(np.mean([r["stokes_ms"] for r in mixed]))
-    step_ms = float(np.mean([r["stokes_ms"] for r in mixed])) + float(energy_ms)
+    mixed_ms = float(np.mean([r["stokes_ms"] for r in mixed]))
     stokes_ms_fp64 = float(np.mean([r["stokes_ms"] for r in fp64]))
+    head = learned[0] if learned else mixed
+    stokes_ms = float(np.mean([r["stokes_ms"] for r in head]))
+    step_ms = stokes_ms + float(energy_ms)
     if world > 1:
         t = torch.tensor([stokes_ms, step_ms], device="cuda", dtype=torch.float64)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -315,8 +384,8 @@ def main():
 
     # dominant kernel: finest-level FP32 Gauss-Seidel colour launches, timed live
     nno = case.nno
-    sweeps = sum(r["smoother_sweeps"] for r in mixed)
-    sm_ms = sum(r["smoother_ms"] for r in mixed)
+    sweeps = sum(r["smoother_sweeps"] for r in head)
+    sm_ms = sum(r["smoother_ms"] for r in head)
     per_launch_s = sm_ms * 1e-3 / max(8 * sweeps, 1)
     per_launch_bytes = bytes_per_sweep(nno, 4) / 8.0
     peak, peak_kind = peaks()
@@ -324,23 +393,28 @@ def main():
 
     if rank != 0:
         return 0
+
+    def summary(recs, res, nu, vr):
+        return {"stokes_ms_per_step": float(np.mean([r["stokes_ms"] for r in recs])),
+                "uzawa_iterations": [r["uzawa"] for r in recs], "mg_passes": [r["mg_passes"] for r in recs],
+                "residuals_final": res, "nu_top": nu[0], "vrms": vr,
+                "nu_rel_err_vs_fp64": abs(nu[0] - nu_fp64[0]) / abs(nu_fp64[0]),
+                "vrms_rel_err_vs_fp64": abs(vr - vr_fp64) / vr_fp64}
+
+    mode = "FP32 multigrid + FP64 refinement + learned warm start" if learned else "FP32 multigrid + FP64 refinement"
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": step_ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64", "data": "synthetic",
-        "config": {"workload": workload_name(case), "mode": "FP32 multigrid + FP64 refinement (headline)",
+        "config": {"workload": workload_name(case), "mode": mode + " (headline)",
                    "step": "cold Stokes solve of the seeded initial state (general_stokes_solver)",
                    "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (FP32 stencils 267 MB, FP64 fine 535 MB)",
                    "timing": "CUDA events around each Stokes solve inside the library, mean over timed steps"},
         "fp64_plain": {"stokes_ms_per_step": stokes_ms_fp64,
                        "uzawa_iterations": [r["uzawa"] for r in fp64], "mg_passes": [r["mg_passes"] for r in fp64],
                        "residuals_final": res_fp64, "nu_top": nu_fp64[0], "vrms": vr_fp64},
-        "mixed": {"stokes_ms_per_step": stokes_ms, "uzawa_iterations": [r["uzawa"] for r in mixed],
-                  "mg_passes": [r["mg_passes"] for r in mixed], "residuals_final": res_mixed,
-                  "nu_top": nu_mixed[0], "vrms": vr_mixed,
-                  "nu_rel_err_vs_fp64": abs(nu_mixed[0] - nu_fp64[0]) / abs(nu_fp64[0]),
-                  "vrms_rel_err_vs_fp64": abs(vr_mixed - vr_fp64) / vr_fp64},
-        "speedup_mixed_vs_fp64": stokes_ms_fp64 / stokes_ms,
+        "mixed": summary(mixed, res_mixed, nu_mixed, vr_mixed),
+        "speedup_vs_fp64": stokes_ms_fp64 / stokes_ms,
         "roofline": {"bound": "hbm", "kernel": "k_tile<float, 0> (finest-level Gauss-Seidel colour)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None,
@@ -348,12 +422,25 @@ def main():
                      "peak_kind": peak_kind, "bytes_per_launch": per_launch_bytes,
                      "launch_us": per_launch_s * 1e6},
         "clocks": clk.summary(),
-        "gpu_launches": int(launches),
+        "gpu_launches": int(learned[1] if learned else launches),
         "wall_s_mixed": t1 - t0,
     }
+    if learned:
+        lrecs, _, res_l, nu_l, vr_l, train_info, wall = learned
+        d = summary(lrecs, res_l, nu_l, vr_l)
+        d.update({"warm_start_used": [r["warm_start"] for r in lrecs],
+                  "initial_residual_zero_start": lrecs[-1]["base_residual"],
+                  "initial_residual_network": lrecs[-1]["warm_residual"],
+                  "speedup_vs_mixed": mixed_ms / d["stokes_ms_per_step"], "training": train_info})
+        line["learned"] = d
     if not args.no_e2e:
-        e2e_ms, h2d, d2h = e2e_mode(cg, case, T0, min(args.steps, 3), 1)
-        line["e2e"] = {"value": e2e_ms, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+        es = ls if learned else cg.Solver(cg.Config.like(case, precision=cg.MIXED))
+        e2e_ms, h2d, d2h = e2e_mode(cg, es, T0, min(args.steps, 3), 1)
+        line["e2e"] = {"value": e2e_ms, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                       "mode": mode}
+    if learned:
+        ln.close()
+        ls.close()
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_sample(case, T0)
     print(json.dumps(line))

@@ -19,7 +19,8 @@ import numpy as np
 from .build import LIB as LIB_PATH
 from .build import build as _build_lib
 
-__all__ = ["Config", "Solver", "CitcomGPUError", "load_library", "build", "heat_flux_noalloc", "FP64", "MIXED"]
+__all__ = ["Config", "Solver", "WarmStart", "CitcomGPUError", "load_library", "build", "heat_flux_noalloc", "FP64",
+           "MIXED"]
 
 FP64 = 0
 MIXED = 1
@@ -129,13 +130,15 @@ class _CStats(ctypes.Structure):
     _fields_ = [("uzawa_iterations", ctypes.c_int), ("del2_calls", ctypes.c_int), ("mg_passes", ctypes.c_int),
                 ("initial_residual", ctypes.c_double), ("stokes_ms", ctypes.c_double), ("energy_ms", ctypes.c_double),
                 ("smoother_ms", ctypes.c_double), ("smoother_sweeps", ctypes.c_int),
-                ("kernel_launches", ctypes.c_ulonglong)]
+                ("kernel_launches", ctypes.c_ulonglong), ("warm_start", ctypes.c_int),
+                ("warm_residual", ctypes.c_double), ("base_residual", ctypes.c_double)]
 
 
 # every symbol of include/citcom_gb300.h with its argument types
 _D = ctypes.POINTER(ctypes.c_double)
 _I = ctypes.POINTER(ctypes.c_int)
 _H = ctypes.c_void_p
+_F = ctypes.POINTER(ctypes.c_float)
 _SIGNATURES = {
     "citcom_gpu_create": (ctypes.c_int, [ctypes.POINTER(_CConfig), ctypes.POINTER(ctypes.c_void_p)]),
     "citcom_gpu_destroy": (None, [_H]),
@@ -171,6 +174,20 @@ _SIGNATURES = {
     "citcom_gpu_op_diagonals": (ctypes.c_int, [_H, ctypes.c_int, _D, _D]),
     "citcom_gpu_heat_flux_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _D, ctypes.c_void_p,
                                                     ctypes.c_void_p, _D, _D]),
+    "citcom_nn_create": (ctypes.c_int, [_H, ctypes.c_int, ctypes.c_uint, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    "citcom_nn_destroy": (None, [_H]),
+    "citcom_nn_error_string": (ctypes.c_char_p, [_H]),
+    "citcom_nn_info": (ctypes.c_int, [_H, _I]),
+    "citcom_nn_get_params": (ctypes.c_int, [_H, _F]),
+    "citcom_nn_set_params": (ctypes.c_int, [_H, _F]),
+    "citcom_nn_get_scales": (ctypes.c_int, [_H, _D]),
+    "citcom_nn_set_scales": (ctypes.c_int, [_H, _D]),
+    "citcom_nn_record": (ctypes.c_int, [_H]),
+    "citcom_nn_train": (ctypes.c_int, [_H, ctypes.c_int, ctypes.c_int, ctypes.c_double, _D]),
+    "citcom_nn_attach": (ctypes.c_int, [_H, ctypes.c_int]),
+    "citcom_nn_predict": (ctypes.c_int, [_H, _D, _D]),
+    "citcom_nn_forward": (ctypes.c_int, [_H, _F, _F]),
+    "citcom_nn_loss_grad": (ctypes.c_int, [_H, _F, _F, _D, _F]),
 }
 
 _lib = None
@@ -302,7 +319,8 @@ class Solver:
         self._check(self.lib.citcom_gpu_last_stats(self.h, ctypes.byref(s)))
         return dict(uzawa=s.uzawa_iterations, del2_calls=s.del2_calls, mg_passes=s.mg_passes,
                     initial_residual=s.initial_residual, stokes_ms=s.stokes_ms, energy_ms=s.energy_ms,
-                    smoother_ms=s.smoother_ms, smoother_sweeps=s.smoother_sweeps, kernel_launches=s.kernel_launches)
+                    smoother_ms=s.smoother_ms, smoother_sweeps=s.smoother_sweeps, kernel_launches=s.kernel_launches,
+                    warm_start=s.warm_start, warm_residual=s.warm_residual, base_residual=s.base_residual)
 
     def stokes_residuals(self):
         """(|F - K U - G P| / |F|, |div U| / (|U| sqrt(npno/neq))) of the resident solution."""
@@ -460,3 +478,103 @@ class Solver:
         bpi = np.zeros(self.dims[lev]["nel"]) if lev == len(self.dims) - 1 else None
         self._check(self.lib.citcom_gpu_op_diagonals(self.h, lev, _dp(bi), _dp(bpi) if bpi is not None else None))
         return bi, bpi
+
+
+def _fp(a: np.ndarray):
+    if a.dtype != np.float32 or not a.flags["C_CONTIGUOUS"]:
+        raise TypeError("arrays passed to the network must be C-contiguous float32")
+    return a.ctypes.data_as(_F)
+
+
+class WarmStart:
+    """Learned warm start of a Solver's Stokes solves (a `citcom_nn` handle).
+
+    A 3D convolutional encoder-decoder on the node grid of multigrid level
+    `level` (-1: the second finest) maps (T, log10 viscosity) to (u, v, w, p).
+    `record()` adds the solver's converged state to the training set,
+    `train()` runs Adam steps on it, `attach()` makes every Stokes solve of the
+    solver start from the network's guess when that guess has the smaller
+    momentum residual.  Destroy (close) it before its solver."""
+
+    def __init__(self, solver: Solver, level: int = -1, seed: int = 0, capacity: int = 64):
+        self.solver = solver
+        self.lib = solver.lib
+        h = ctypes.c_void_p()
+        solver._check(self.lib.citcom_nn_create(solver.h, level, seed, capacity, ctypes.byref(h)))
+        self.h = h
+        info = (ctypes.c_int * 6)()
+        self._check(self.lib.citcom_nn_info(self.h, info))
+        self.grid = (info[0], info[1], info[2])
+        self.n_params = info[3]
+        self.level = info[5]
+        self.voxels = info[0] * info[1] * info[2]
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.citcom_nn_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != 0:
+            msg = self.lib.citcom_nn_error_string(self.h)
+            raise CitcomGPUError(f"{_ERRORS.get(rc, rc)}: {msg.decode() if msg else ''}")
+
+    @property
+    def recorded(self) -> int:
+        info = (ctypes.c_int * 6)()
+        self._check(self.lib.citcom_nn_info(self.h, info))
+        return info[4]
+
+    def get_params(self) -> np.ndarray:
+        w = np.zeros(self.n_params, dtype=np.float32)
+        self._check(self.lib.citcom_nn_get_params(self.h, _fp(w)))
+        return w
+
+    def set_params(self, w):
+        self._check(self.lib.citcom_nn_set_params(self.h, _fp(np.ascontiguousarray(w, dtype=np.float32))))
+
+    def get_scales(self):
+        s = np.zeros(3)
+        self._check(self.lib.citcom_nn_get_scales(self.h, _dp(s)))
+        return tuple(float(x) for x in s)
+
+    def set_scales(self, s):
+        self._check(self.lib.citcom_nn_set_scales(self.h, _dp(np.ascontiguousarray(s, dtype=np.float64))))
+
+    def record(self):
+        self._check(self.lib.citcom_nn_record(self.h))
+
+    def train(self, steps: int, batch: int = 4, lr: float = 1e-3) -> float:
+        loss = ctypes.c_double()
+        self._check(self.lib.citcom_nn_train(self.h, steps, batch, lr, ctypes.byref(loss)))
+        return loss.value
+
+    def attach(self, on: bool = True):
+        self._check(self.lib.citcom_nn_attach(self.h, int(on)))
+
+    def predict(self):
+        f = self.solver.fine
+        U, P = np.zeros(f["neq"]), np.zeros(f["nel"])
+        self._check(self.lib.citcom_nn_predict(self.h, _dp(U), _dp(P)))
+        return U, P
+
+    def forward(self, x: np.ndarray) -> np.ndarray:
+        """x: (V, 2) float32 scaled inputs -> (V, 4) scaled outputs."""
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(self.voxels, 2)
+        y = np.zeros((self.voxels, 4), dtype=np.float32)
+        self._check(self.lib.citcom_nn_forward(self.h, _fp(x), _fp(y)))
+        return y
+
+    def loss_grad(self, x: np.ndarray, t: np.ndarray):
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(self.voxels, 2)
+        t = np.ascontiguousarray(t, dtype=np.float32).reshape(self.voxels, 4)
+        g = np.zeros(self.n_params, dtype=np.float32)
+        loss = ctypes.c_double()
+        self._check(self.lib.citcom_nn_loss_grad(self.h, _fp(x), _fp(t), ctypes.byref(loss), _fp(g)))
+        return loss.value, g

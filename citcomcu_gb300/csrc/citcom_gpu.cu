@@ -16,8 +16,11 @@
 #include <type_traits>
 #include <vector>
 
+#include <cuda_bf16.h>
+
 #include "../../include/citcom_gb300.h"
 #include "kernels.h"
+#include "nn.h"
 
 namespace {
 
@@ -96,6 +99,30 @@ struct citcom_gpu
 	long lt_calls[CITCOM_MAX_LEVELS];
 	long lt_sweeps[CITCOM_MAX_LEVELS];
 	citcom_gpu_stats stats;
+	std::vector<void *> allocs;
+	citcom_nn *warm;   // warm-start network attached to the Stokes solve (not owned), or null
+	char err[512];
+};
+
+// The warm-start network of one solver handle and its training set.
+struct citcom_nn
+{
+	citcom_gpu *h;          // the solver (null once it is destroyed)
+	NnNet *net;
+	int lev, r;             // network level; node spacing ratio to the finest level
+	int V;                  // network nodes
+	int capacity, count, next;
+	__nv_bfloat16 *xs;      // training inputs, capacity x V x 16
+	float *ts;              // training targets, capacity x V x 4
+	__nv_bfloat16 *x;       // inputs of the current state
+	float *y;               // network output, V x 16
+	double *Uv[CITCOM_MAX_LEVELS];  // guessed velocity on the levels lev .. finest - 1
+	double *Ug, *Pg;        // guess on the finest level
+	double *work;           // FP64 scratch of the input/target/guess kernels
+	double su, sp, mp;      // output scales per unit anomaly RMS: velocity, pressure; pressure offset
+	bool scaled;
+	bool attached;
+	unsigned long long rng;
 	std::vector<void *> allocs;
 	char err[512];
 };
@@ -518,7 +545,36 @@ int solve_del2_u(citcom_gpu *h, double acc, int *valid)
 
 // ---------------------------------------------------------------- Uzawa
 
-// solve_Ahat_p_fhat (Stokes_flow_Incomp.c:295-497) on device buffers.
+int nn_guess(citcom_nn *n);
+
+// The head of solve_Ahat_p_fhat (Stokes_flow_Incomp.c:360-371): the velocity
+// correction V += K^-1 (F - G P - K V) for the pressure P, then r1 = B V and
+// the initial residual |r1| / sqrt(npno) that the function returns.
+int uzawa_start(citcom_gpu *h, double *V, const double *P, const double *F, double acc, double *residual)
+{
+	const int lmax = h->L - 1;
+	const Lvl &Lf = h->lv[lmax];
+	const Geo *geo = h->geo[lmax];
+	cudaStream_t st = h->st;
+	int valid;
+	launch_grad(st, Lf, geo, P, h->Ah);
+	launch_kmul<double>(st, Lf, h->K64[lmax], V, h->u1);
+	launch_sub3(st, Lf.neq, h->Ah, F, h->Ah, h->u1);
+	launch_strip(st, Lf, h->Ah);
+	TRY(solve_del2_u(h, acc, &valid));
+	launch_strip(st, Lf, h->u1);
+	launch_axpby(st, Lf.neq, V, 1.0, h->u1, 1.0);
+	launch_div(st, Lf, geo, V, h->r1);
+	launch_dot(st, Lf.nel, h->r1, h->r1, red_of(h), h->dscal + S_R0);
+	TRY(readback(h, S_R0, 1));
+	*residual = std::sqrt(h->hscal[S_R0] / Lf.nel);
+	return CITCOM_GPU_OK;
+}
+
+// solve_Ahat_p_fhat (Stokes_flow_Incomp.c:295-497) on device buffers.  With a
+// warm-start network attached, the head runs for the network's guess as well
+// as for the given V, P, and the loop continues from the pair with the smaller
+// initial residual.
 int uzawa(citcom_gpu *h, double *V, double *P, const double *F, double imp, int *steps_max, double *initial_residual)
 {
 	const int lmax = h->L - 1;
@@ -526,7 +582,6 @@ int uzawa(citcom_gpu *h, double *V, double *P, const double *F, double imp, int 
 	const int neq = Lf.neq, npno = Lf.nel;
 	const Geo *geo = h->geo[lmax];
 	cudaStream_t st = h->st;
-	double *r0 = h->r0, *r1 = h->r1, *r2 = h->r2, *z0 = h->z0, *z1 = h->z1, *s1 = h->s1, *s2 = h->s2, *sh;
 	double *Ah = h->Ah, *u1 = h->u1;
 	int valid;
 	if(!h->stiffness_ready)
@@ -536,17 +591,33 @@ int uzawa(citcom_gpu *h, double *V, double *P, const double *F, double imp, int 
 	TRY(readback(h, S_R0, 1));
 	const double v_res = std::sqrt(h->hscal[S_R0] / neq);
 
-	launch_grad(st, Lf, geo, P, Ah);
-	launch_kmul<double>(st, Lf, h->K64[lmax], V, u1);
-	launch_sub3(st, neq, Ah, F, Ah, u1);
-	launch_strip(st, Lf, Ah);
-	TRY(solve_del2_u(h, imp * v_res, &valid));
-	launch_strip(st, Lf, u1);
-	launch_axpby(st, neq, V, 1.0, u1, 1.0);
-	launch_div(st, Lf, geo, V, r1);
-	launch_dot(st, npno, r1, r1, red_of(h), h->dscal + S_R0);
-	TRY(readback(h, S_R0, 1));
-	const double residual = std::sqrt(h->hscal[S_R0] / npno);
+	h->stats.warm_start = 0;
+	h->stats.warm_residual = 0.0;
+	h->stats.base_residual = 0.0;
+	double residual = 0.0;
+	citcom_nn *n = h->warm;
+	if(n && n->scaled)
+	{
+		double r_net = 0.0;
+		TRY(nn_guess(n));
+		TRY(uzawa_start(h, n->Ug, n->Pg, F, imp * v_res, &r_net));
+		TRY(uzawa_start(h, V, P, F, imp * v_res, &residual));
+		if(nn_device_error(n->net) != 0)
+			return fail(h, CITCOM_GPU_ERR_CUDA, "warm-start network: a tensor-core wait timed out");
+		h->stats.warm_residual = r_net;
+		h->stats.base_residual = residual;
+		if(r_net < residual)
+		{
+			CK(cudaMemcpyAsync(V, n->Ug, sizeof(double) * neq, cudaMemcpyDeviceToDevice, st));
+			CK(cudaMemcpyAsync(P, n->Pg, sizeof(double) * npno, cudaMemcpyDeviceToDevice, st));
+			launch_div(st, Lf, geo, V, h->r1);
+			residual = r_net;
+			h->stats.warm_start = 1;
+		}
+	}
+	else
+		TRY(uzawa_start(h, V, P, F, imp * v_res, &residual));
+	double *r0 = h->r0, *r1 = h->r1, *r2 = h->r2, *z0 = h->z0, *z1 = h->z1, *s1 = h->s1, *s2 = h->s2, *sh;
 
 	int count = 0;
 	double dpressure = 1.0, dvelocity = 1.0;
@@ -970,6 +1041,8 @@ void citcom_gpu_destroy(citcom_gpu *h)
 {
 	if(!h)
 		return;
+	if(h->warm)
+		h->warm->h = nullptr;
 	if(h->level_timing)
 		for(int l = 0; l < h->L; ++l)
 			fprintf(stderr, "level %d (%d nodes, %s): %ld smoother calls, %ld sweeps, %.3f ms total, %.2f us/call, %.2f us/sweep\n",
@@ -1494,6 +1567,343 @@ int citcom_gpu_op_diagonals(citcom_gpu *h, int lev, double *BI, double *BPI)
 		TRY(d2h(h, BPI, h->BPI, sizeof(double) * L.nel));
 	}
 	return sync(h);
+}
+
+} // extern "C"
+
+// ================================================================ warm start
+
+namespace {
+
+int nn_fail(citcom_nn *n, int code, const char *fmt, ...)
+{
+	va_list ap;
+	va_start(ap, fmt);
+	vsnprintf(n->err, sizeof(n->err), fmt, ap);
+	va_end(ap);
+	return code;
+}
+
+// the network's guess of U (finest level) and P from the resident T and viscosity
+int nn_guess(citcom_nn *n)
+{
+	citcom_gpu *h = n->h;
+	const int lmax = h->L - 1;
+	const Lvl &Lf = h->lv[lmax], &Lc = h->lv[n->lev];
+	launch_nn_inputs(h->st, Lf, Lc, n->r, h->T, h->evi[n->lev], n->x, n->work);
+	if(nn_forward(n->net, n->x, n->y) != 0)
+		return fail(h, CITCOM_GPU_ERR_CUDA, "warm-start network: forward launch failed");
+	launch_nn_guess(h->st, Lf, Lc, n->r, n->y, n->su, n->sp, n->mp, n->work, n->Uv[n->lev], n->Pg);
+	for(int l = n->lev; l < lmax; ++l)
+	{
+		double *dst = (l + 1 == lmax) ? n->Ug : n->Uv[l + 1];
+		launch_interp<double>(h->st, h->lv[l], h->lv[l + 1], n->Uv[l], dst);
+		launch_strip(h->st, h->lv[l + 1], dst);
+	}
+	CK(cudaGetLastError());
+	return CITCOM_GPU_OK;
+}
+
+template <typename T> int nn_alloc(citcom_nn *n, T **p, size_t count)
+{
+	void *q = nullptr;
+	if(cudaMalloc(&q, (count ? count : 1) * sizeof(T)) != cudaSuccess)
+		return nn_fail(n, CITCOM_GPU_ERR_CUDA, "cudaMalloc of %zu bytes failed", count * sizeof(T));
+	cudaMemset(q, 0, (count ? count : 1) * sizeof(T));
+	n->allocs.push_back(q);
+	*p = (T *)q;
+	return CITCOM_GPU_OK;
+}
+
+int nn_check(citcom_nn *n)
+{
+	if(!n)
+		return CITCOM_GPU_ERR_ARG;
+	if(!n->h)
+		return nn_fail(n, CITCOM_GPU_ERR_STATE, "the solver of this network was destroyed");
+	return CITCOM_GPU_OK;
+}
+
+#define NTRY(call)               \
+	do                           \
+	{                            \
+		int r_ = (call);         \
+		if(r_ != CITCOM_GPU_OK)  \
+			return r_;           \
+	} while(0)
+
+// host (V x 2 FP32) -> device network input (V x 16 BF16)
+int nn_upload_inputs(citcom_nn *n, const float *x)
+{
+	std::vector<__nv_bfloat16> hb((size_t)n->V * NN_CH, __float2bfloat16_rn(0.f));
+	for(int v = 0; v < n->V; ++v)
+		for(int c = 0; c < NN_IN; ++c)
+			hb[(size_t)v * NN_CH + c] = __float2bfloat16_rn(x[(size_t)v * NN_IN + c]);
+	if(cudaMemcpyAsync(n->x, hb.data(), hb.size() * sizeof(__nv_bfloat16), cudaMemcpyHostToDevice, n->h->st) != cudaSuccess ||
+	   cudaStreamSynchronize(n->h->st) != cudaSuccess)
+		return nn_fail(n, CITCOM_GPU_ERR_CUDA, "input upload failed");
+	return CITCOM_GPU_OK;
+}
+
+unsigned long long nn_rand(citcom_nn *n)
+{
+	n->rng = n->rng * 6364136223846793005ull + 1442695040888963407ull;
+	return n->rng >> 17;
+}
+
+} // namespace
+
+extern "C" {
+
+int citcom_nn_create(citcom_gpu *h, int level, unsigned seed, int capacity, citcom_nn **out)
+{
+	TRY(check_handle(h));
+	if(!out)
+		return fail(h, CITCOM_GPU_ERR_ARG, "null argument");
+	*out = nullptr;
+	const int lmax = h->L - 1;
+	if(level < 0)
+		level = lmax - 1;
+	if(level < 1 || level >= lmax)
+		return fail(h, CITCOM_GPU_ERR_ARG, "warm-start level %d: needs 1 <= level < %d", level, lmax);
+	if(capacity < 1)
+		return fail(h, CITCOM_GPU_ERR_ARG, "training-set capacity must be positive");
+	citcom_nn *n = new citcom_nn();
+	n->h = h;
+	n->lev = level;
+	n->r = 1 << (lmax - level);
+	n->capacity = capacity;
+	n->rng = 0x2545F4914F6CDD1Dull ^ seed;
+	const Lvl &Lc = h->lv[level];
+	if(nn_create(Lc.nox, Lc.noy, Lc.noz, seed, h->st, &n->net, n->err, sizeof(n->err)) != 0)
+	{
+		int r = fail(h, CITCOM_GPU_ERR_ARG, "%s", n->err);
+		delete n;
+		return r;
+	}
+	n->V = nn_voxels(n->net);
+	int r = CITCOM_GPU_OK;
+	r = r ? r : nn_alloc(n, &n->xs, (size_t)capacity * n->V * NN_CH);
+	r = r ? r : nn_alloc(n, &n->ts, (size_t)capacity * n->V * NN_OUT);
+	r = r ? r : nn_alloc(n, &n->x, (size_t)n->V * NN_CH);
+	r = r ? r : nn_alloc(n, &n->y, (size_t)n->V * NN_CH);
+	for(int l = level; l < lmax && !r; ++l)
+		r = nn_alloc(n, &n->Uv[l], (size_t)h->lv[l].neq + 2);
+	r = r ? r : nn_alloc(n, &n->Ug, (size_t)h->lv[lmax].neq + 2);
+	r = r ? r : nn_alloc(n, &n->Pg, (size_t)h->lv[lmax].nel);
+	r = r ? r : nn_alloc(n, &n->work, (size_t)Lc.nno + Lc.noz + 2);
+	if(r != CITCOM_GPU_OK)
+	{
+		fail(h, r, "%s", n->err);
+		citcom_nn_destroy(n);
+		return r;
+	}
+	*out = n;
+	return CITCOM_GPU_OK;
+}
+
+void citcom_nn_destroy(citcom_nn *n)
+{
+	if(!n)
+		return;
+	if(n->h)
+	{
+		cudaStreamSynchronize(n->h->st);
+		if(n->h->warm == n)
+			n->h->warm = nullptr;
+	}
+	nn_destroy(n->net);
+	for(void *p : n->allocs)
+		cudaFree(p);
+	delete n;
+}
+
+const char *citcom_nn_error_string(const citcom_nn *n) { return n ? n->err : "null network"; }
+
+int citcom_nn_info(const citcom_nn *n, int info[6])
+{
+	if(!n || !info)
+		return CITCOM_GPU_ERR_ARG;
+	const Lvl &Lc = n->h ? n->h->lv[n->lev] : Lvl();
+	info[0] = Lc.nox;
+	info[1] = Lc.noy;
+	info[2] = Lc.noz;
+	info[3] = nn_param_count(n->net);
+	info[4] = n->count;
+	info[5] = n->lev;
+	return CITCOM_GPU_OK;
+}
+
+int citcom_nn_get_params(citcom_nn *n, float *w)
+{
+	NTRY(nn_check(n));
+	if(!w)
+		return nn_fail(n, CITCOM_GPU_ERR_ARG, "null argument");
+	return nn_get_params(n->net, w) == 0 ? CITCOM_GPU_OK : nn_fail(n, CITCOM_GPU_ERR_CUDA, "parameter download failed");
+}
+
+int citcom_nn_set_params(citcom_nn *n, const float *w)
+{
+	NTRY(nn_check(n));
+	if(!w)
+		return nn_fail(n, CITCOM_GPU_ERR_ARG, "null argument");
+	return nn_set_params(n->net, w) == 0 ? CITCOM_GPU_OK : nn_fail(n, CITCOM_GPU_ERR_CUDA, "parameter upload failed");
+}
+
+int citcom_nn_get_scales(const citcom_nn *n, double s[3])
+{
+	if(!n || !s)
+		return CITCOM_GPU_ERR_ARG;
+	s[0] = n->su;
+	s[1] = n->sp;
+	s[2] = n->mp;
+	return n->scaled ? CITCOM_GPU_OK : CITCOM_GPU_ERR_STATE;
+}
+
+int citcom_nn_set_scales(citcom_nn *n, const double s[3])
+{
+	NTRY(nn_check(n));
+	if(!s || !(s[0] > 0.0) || !(s[1] > 0.0))
+		return nn_fail(n, CITCOM_GPU_ERR_ARG, "scales must be positive");
+	n->su = s[0];
+	n->sp = s[1];
+	n->mp = s[2];
+	n->scaled = true;
+	return CITCOM_GPU_OK;
+}
+
+int citcom_nn_record(citcom_nn *n)
+{
+	NTRY(nn_check(n));
+	citcom_gpu *h = n->h;
+	const int lmax = h->L - 1;
+	const Lvl &Lf = h->lv[lmax], &Lc = h->lv[n->lev];
+	if(!h->visc_ready)
+		return nn_fail(n, CITCOM_GPU_ERR_STATE, "no viscosity: record after a Stokes solve");
+	__nv_bfloat16 *xs = n->xs + (size_t)n->next * n->V * NN_CH;
+	float *ts = n->ts + (size_t)n->next * n->V * NN_OUT;
+	launch_nn_inputs(h->st, Lf, Lc, n->r, h->T, h->evi[n->lev], xs, n->work);
+	if(!n->scaled)
+	{
+		// output scales from the first recorded solution: RMS velocity dof and
+		// RMS pressure deviation, per unit anomaly RMS
+		std::vector<double> U(Lf.neq), P(Lf.nel);
+		double ss = 0.0;
+		if(d2h(h, U.data(), h->U, sizeof(double) * Lf.neq) || d2h(h, P.data(), h->P, sizeof(double) * Lf.nel) ||
+		   d2h(h, &ss, n->work + Lc.nno + Lc.noz, sizeof(double)) || sync(h))
+			return nn_fail(n, CITCOM_GPU_ERR_CUDA, "state download failed");
+		const double a = std::sqrt(ss / Lc.nno);
+		double uu = 0.0, pm = 0.0, pp = 0.0;
+		for(double u : U)
+			uu += u * u;
+		for(double p : P)
+			pm += p;
+		pm /= Lf.nel;
+		for(double p : P)
+			pp += (p - pm) * (p - pm);
+		if(!(a > 0.0) || !(uu > 0.0) || !(pp > 0.0))
+			return nn_fail(n, CITCOM_GPU_ERR_STATE, "the recorded state has no temperature anomaly or no flow");
+		n->su = std::sqrt(uu / Lf.neq) / a;
+		n->sp = std::sqrt(pp / Lf.nel) / a;
+		n->mp = 0.0;
+		n->scaled = true;
+	}
+	launch_nn_targets(h->st, Lf, Lc, n->r, h->U, h->P, n->su, n->sp, n->work, ts);
+	n->next = (n->next + 1) % n->capacity;
+	if(n->count < n->capacity)
+		n->count++;
+	if(cudaGetLastError() != cudaSuccess)
+		return nn_fail(n, CITCOM_GPU_ERR_CUDA, "record kernels failed to launch");
+	return CITCOM_GPU_OK;
+}
+
+int citcom_nn_train(citcom_nn *n, int steps, int batch, double lr, double *loss)
+{
+	NTRY(nn_check(n));
+	if(n->count < 1)
+		return nn_fail(n, CITCOM_GPU_ERR_STATE, "the training set is empty");
+	if(steps < 1 || batch < 1 || !(lr > 0.0))
+		return nn_fail(n, CITCOM_GPU_ERR_ARG, "steps, batch and lr must be positive");
+	const float scale = 1.f / ((float)n->V * NN_OUT * batch);
+	for(int s = 0; s < steps; ++s)
+	{
+		nn_zero_grads(n->net);
+		for(int b = 0; b < batch; ++b)
+		{
+			const int i = (int)(nn_rand(n) % (unsigned long long)n->count);
+			nn_accumulate(n->net, n->xs + (size_t)i * n->V * NN_CH, n->ts + (size_t)i * n->V * NN_OUT, scale);
+		}
+		nn_adam(n->net, (float)lr, 0.9f, 0.999f, 1e-8f);
+	}
+	double l = 0.0;
+	if(nn_loss(n->net, &l) != 0)
+		return nn_fail(n, CITCOM_GPU_ERR_CUDA, "training failed: %s", cudaGetErrorString(cudaGetLastError()));
+	if(nn_device_error(n->net) != 0)
+		return nn_fail(n, CITCOM_GPU_ERR_CUDA, "training: a tensor-core wait timed out");
+	if(loss)
+		*loss = l;
+	return CITCOM_GPU_OK;
+}
+
+int citcom_nn_attach(citcom_nn *n, int on)
+{
+	NTRY(nn_check(n));
+	n->attached = on != 0;
+	n->h->warm = n->attached ? n : (n->h->warm == n ? nullptr : n->h->warm);
+	return CITCOM_GPU_OK;
+}
+
+int citcom_nn_predict(citcom_nn *n, double *U, double *P)
+{
+	NTRY(nn_check(n));
+	citcom_gpu *h = n->h;
+	if(!n->scaled)
+		return nn_fail(n, CITCOM_GPU_ERR_STATE, "no output scales: record a solution or set the scales first");
+	if(!h->visc_ready)
+		return nn_fail(n, CITCOM_GPU_ERR_STATE, "no viscosity: call get_system_viscosity or solve first");
+	const Lvl &Lf = h->lv[h->L - 1];
+	if(nn_guess(n) != CITCOM_GPU_OK)
+		return nn_fail(n, CITCOM_GPU_ERR_CUDA, "%s", h->err);
+	if((U && d2h(h, U, n->Ug, sizeof(double) * Lf.neq)) || (P && d2h(h, P, n->Pg, sizeof(double) * Lf.nel)) || sync(h))
+		return nn_fail(n, CITCOM_GPU_ERR_CUDA, "guess download failed");
+	return nn_device_error(n->net) == 0 ? CITCOM_GPU_OK : nn_fail(n, CITCOM_GPU_ERR_CUDA, "a tensor-core wait timed out");
+}
+
+int citcom_nn_forward(citcom_nn *n, const float *x, float *y)
+{
+	NTRY(nn_check(n));
+	if(!x || !y)
+		return nn_fail(n, CITCOM_GPU_ERR_ARG, "null argument");
+	NTRY(nn_upload_inputs(n, x));
+	nn_forward(n->net, n->x, n->y);
+	std::vector<float> hy((size_t)n->V * NN_CH);
+	if(cudaMemcpyAsync(hy.data(), n->y, hy.size() * sizeof(float), cudaMemcpyDeviceToHost, n->h->st) != cudaSuccess ||
+	   cudaStreamSynchronize(n->h->st) != cudaSuccess)
+		return nn_fail(n, CITCOM_GPU_ERR_CUDA, "forward failed: %s", cudaGetErrorString(cudaGetLastError()));
+	if(nn_device_error(n->net) != 0)
+		return nn_fail(n, CITCOM_GPU_ERR_CUDA, "forward: a tensor-core wait timed out");
+	for(int v = 0; v < n->V; ++v)
+		for(int c = 0; c < NN_OUT; ++c)
+			y[(size_t)v * NN_OUT + c] = hy[(size_t)v * NN_CH + c];
+	return CITCOM_GPU_OK;
+}
+
+int citcom_nn_loss_grad(citcom_nn *n, const float *x, const float *t, double *loss, float *grad)
+{
+	NTRY(nn_check(n));
+	if(!x || !t || !loss || !grad)
+		return nn_fail(n, CITCOM_GPU_ERR_ARG, "null argument");
+	NTRY(nn_upload_inputs(n, x));
+	float *dt = n->ts;  // slot 0 of the training set as scratch for the target
+	if(cudaMemcpyAsync(dt, t, sizeof(float) * n->V * NN_OUT, cudaMemcpyHostToDevice, n->h->st) != cudaSuccess)
+		return nn_fail(n, CITCOM_GPU_ERR_CUDA, "target upload failed");
+	nn_zero_grads(n->net);
+	nn_accumulate(n->net, n->x, dt, 1.f / ((float)n->V * NN_OUT));
+	if(nn_loss(n->net, loss) != 0 || nn_get_grads(n->net, grad) != 0)
+		return nn_fail(n, CITCOM_GPU_ERR_CUDA, "gradient failed: %s", cudaGetErrorString(cudaGetLastError()));
+	if(n->count > 0)
+		n->count = 0, n->next = 0;  // slot 0 was overwritten
+	return nn_device_error(n->net) == 0 ? CITCOM_GPU_OK : nn_fail(n, CITCOM_GPU_ERR_CUDA, "a tensor-core wait timed out");
 }
 
 } // extern "C"

@@ -96,6 +96,9 @@ typedef struct citcom_gpu_stats
 	double smoother_ms;         /* device time of the finest-level Gauss-Seidel calls */
 	int smoother_sweeps;        /* finest-level sweeps (8 colour launches each) in smoother_ms */
 	unsigned long long kernel_launches;  /* kernels launched by the library since it was loaded */
+	int warm_start;             /* 1: the attached network's guess started the Uzawa solve */
+	double warm_residual;       /* |F - K U - G P| / |F| of the network's guess */
+	double base_residual;       /* the same of the resident U, P it was compared with */
 } citcom_gpu_stats;
 
 /* Allocates every device buffer the solver will use (on the current
@@ -203,6 +206,49 @@ int citcom_gpu_op_diagonals(citcom_gpu *h, int lev, double *BI, double *BPI);
 #define CITCOM_GPU_NOALLOC_MAX_ELEMENTS 262144
 int citcom_gpu_heat_flux_noalloc(int nox, int noy, int noz, const double dimen[3], const double *dT, const double *dV,
                                  double *nut, double *nub);
+
+/* Learned warm start of the Stokes solve.  No counterpart in the reference,
+ * which starts solve_Ahat_p_fhat (Stokes_flow_Incomp.c:295) from the previous
+ * time step's U and P.  A 3D convolutional encoder-decoder on the node grid of
+ * multigrid level `level` (-1: the second finest) maps T and log10 of the
+ * viscosity to velocity and pressure; BF16 weights and activations, FP32
+ * accumulation on the tensor cores, FP32 master weights trained with Adam on
+ * snapshots of converged solves of the same handle.  When attached, every
+ * Uzawa solve of the handle (solve_Ahat_p_fhat and everything that calls it)
+ * runs its head -- the velocity correction for the given pressure and the
+ * initial residual |div V| / sqrt(npno) that solve_Ahat_p_fhat returns -- for
+ * the network's guess as well as for the resident U, P (the previous solution,
+ * or zero), and iterates from the pair with the smaller initial residual.  The
+ * solve then runs to the same stopping rule, so the network changes only the
+ * iteration count (at the price of one extra velocity solve).  The network
+ * must be destroyed before its solver handle, or at least not used after it. */
+typedef struct citcom_nn citcom_nn;
+int citcom_nn_create(citcom_gpu *h, int level, unsigned seed, int capacity, citcom_nn **out);
+void citcom_nn_destroy(citcom_nn *n);
+const char *citcom_nn_error_string(const citcom_nn *n);
+/* info: nox, noy, noz of the network grid, parameter count, recorded snapshots, level */
+int citcom_nn_info(const citcom_nn *n, int info[6]);
+/* parameters, FP32, per layer W[cout][cin][27] (tap 9(dy+1)+3(dx+1)+(dz+1)) then b[cout] */
+int citcom_nn_get_params(citcom_nn *n, float *w);
+int citcom_nn_set_params(citcom_nn *n, const float *w);
+/* output scales: velocity and pressure per unit RMS of the temperature anomaly
+ * (T minus its horizontal mean), and a pressure offset; set by the first record */
+int citcom_nn_get_scales(const citcom_nn *n, double s[3]);
+int citcom_nn_set_scales(citcom_nn *n, const double s[3]);
+/* adds the handle's resident (T, viscosity, U, P) to the training set (a ring of `capacity`) */
+int citcom_nn_record(citcom_nn *n);
+/* `steps` Adam steps on random minibatches of `batch` snapshots; loss of the last step */
+int citcom_nn_train(citcom_nn *n, int steps, int batch, double lr, double *loss);
+/* on != 0: warm-start every Stokes solve of the handle */
+int citcom_nn_attach(citcom_nn *n, int on);
+/* the guess for the resident T and viscosity: U (neq), P (nel) on the host */
+int citcom_nn_predict(citcom_nn *n, double *U, double *P);
+/* checks of the network alone, host buffers in the network's scaled units:
+ * x (V x 2: temperature anomaly / its RMS, (log10 eta + 1.5) / 1.5), y and t
+ * (V x 4: u, v, w, p in units of the scales above times the anomaly RMS);
+ * loss = mean over V x 4 of (y - t)^2 and its gradient in the parameter layout */
+int citcom_nn_forward(citcom_nn *n, const float *x, float *y);
+int citcom_nn_loss_grad(citcom_nn *n, const float *x, const float *t, double *loss, float *grad);
 
 #ifdef __cplusplus
 }

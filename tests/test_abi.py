@@ -13,7 +13,7 @@ HEADER = os.path.join(ROOT, "include", "citcom_gb300.h")
 
 def header_symbols():
     txt = open(HEADER).read()
-    return sorted(set(re.findall(r"\b(citcom_gpu_[a-zA-Z0-9_]+)\s*\(", txt)))
+    return sorted(set(re.findall(r"\b(citcom_(?:gpu|nn)_[a-zA-Z0-9_]+)\s*\(", txt)))
 
 
 @pytest.fixture(scope="module")
@@ -34,7 +34,7 @@ def test_header_declares_entry_points():
 def test_library_exports_every_header_symbol(lib):
     import citcomcu_gb300 as cg
     out = subprocess.run(["nm", "-D", "--defined-only", cg.LIB_PATH], capture_output=True, text=True, check=True).stdout
-    exported = set(re.findall(r"\bT (citcom_gpu_\w+)", out))
+    exported = set(re.findall(r"\bT (citcom_(?:gpu|nn)_\w+)", out))
     missing = [s for s in header_symbols() if s not in exported]
     assert not missing, missing
     # and the Python front end binds exactly these

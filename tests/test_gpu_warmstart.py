@@ -1,0 +1,144 @@
+"""Learned warm start: the tensor-core network against its CPU oracle
+(forward pass and parameter gradient), training, and what a trained network
+gains over the method without it on held-out initial states."""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import nn_oracle as N
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def cg():
+    import citcomcu_gb300 as cg
+    cg.build()
+    return cg
+
+
+@pytest.fixture(scope="module")
+def net(cg):
+    # a non-cubic box so that the node numbering is exercised: network grid
+    # 9 x 17 x 9 nodes (level 2 of 4, mgunit 2, 4, 2)
+    s = cg.Solver(cg.Config(mgunit=(2, 4, 2), levels=4, dimen=(1.0, 2.0, 1.0), rayleigh=1e4, tdepv=True,
+                            viscE=(math.log(1e3),), precision=cg.MIXED))
+    n = cg.WarmStart(s, level=-1, seed=1, capacity=4)
+    yield n
+    n.close()
+    s.close()
+
+
+def oracle_inputs(n, seed):
+    nx, ny, nz = n.grid
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(-1, 1, (ny, nx, nz, 2)).astype(np.float32)
+    t = rng.normal(size=(ny, nx, nz, 4)).astype(np.float32)
+    return x, t
+
+
+def test_forward_matches_oracle(net):
+    assert net.grid == (9, 17, 9) and net.n_params == N.param_count()
+    p = N.init_params(5).astype(np.float32)
+    net.set_params(p)
+    assert np.array_equal(net.get_params(), p)
+    x, _ = oracle_inputs(net, 0)
+    y = net.forward(x.reshape(-1, 2)).reshape(x.shape[:3] + (4,))
+    yref, _ = N.forward(p.astype(np.float64), x.astype(np.float64))
+    # BF16 activations: the same rounding points as the oracle; differences come
+    # from FP32 vs float64 accumulation flipping an occasional BF16 rounding
+    rel = np.linalg.norm(y - yref) / np.linalg.norm(yref)
+    assert rel < 1e-2, rel
+    assert np.max(np.abs(y - yref)) < 3e-2 * np.max(np.abs(yref))
+
+
+def test_gradient_matches_oracle(net):
+    p = N.init_params(6).astype(np.float32)
+    net.set_params(p)
+    x, t = oracle_inputs(net, 1)
+    loss, g = net.loss_grad(x.reshape(-1, 2), t.reshape(-1, 4))
+    lref, gref = N.loss_grad(p.astype(np.float64), x.astype(np.float64), t.astype(np.float64))
+    assert abs(loss - lref) < 1e-2 * lref, (loss, lref)
+    assert np.linalg.norm(g - gref) < 3e-2 * np.linalg.norm(gref)
+    o = 0
+    for l, (_, ci, co, _) in enumerate(N.LAYERS):
+        k = 27 * ci * co + co
+        gl, rl = g[o:o + k], gref[o:o + k]
+        assert np.linalg.norm(gl - rl) < 5e-2 * np.linalg.norm(rl), (l, np.linalg.norm(gl - rl) / np.linalg.norm(rl))
+        o += k
+
+
+def seeded_T(case_dims, seed, amp=0.01):
+    nox, noy, noz = case_dims
+    rng = np.random.Generator(np.random.PCG64(seed))
+    z = np.linspace(0.0, 1.0, noz)
+    T = np.empty((noy, nox, noz))
+    T[:] = 1.0 - z
+    T += rng.uniform(-amp, amp, size=T.shape)
+    T[:, :, 0] = 1.0
+    T[:, :, -1] = 0.0
+    return T.reshape(-1)
+
+
+def test_trained_warm_start_gain_on_held_out_states(cg):
+    """What the trained network gains over the method without it, on states
+    of a seed it never saw: the Uzawa initial residual (the quantity
+    solve_Ahat_p_fhat returns) of its guess against the zero start, and the
+    iteration count to the same stopping rule, whose solution must not change."""
+    # 16^3 elements, 10^3 viscosity contrast, Ra 1e5; network on the 8^3 level
+    cfg = cg.Config(mgunit=(2, 2, 2), levels=4, rayleigh=1e5, tdepv=True, viscE=(math.log(1e3),),
+                    accuracy=1e-6, precision=cg.MIXED)
+    s = cg.Solver(cfg)
+    f = s.fine
+    dims = (f["nox"], f["noy"], f["noz"])
+    n = cg.WarmStart(s, seed=2, capacity=64)
+    zn, zu, zp = np.zeros(f["nno"]), np.zeros(f["neq"]), np.zeros(f["nel"])
+    # training set: converged cold solves of seeded initial states and the
+    # time steps that follow them
+    for seed in range(1, 9):
+        s.load_state(T=seeded_T(dims, seed), Tdot=zn, U=zu, P=zp)
+        s.stokes_resident()
+        n.record()
+        for _ in range(5):
+            s.step_resident(0.0)
+            n.record()
+    assert n.recorded == 48
+    l0 = n.train(1, batch=4, lr=1e-3)
+    l1 = n.train(800, batch=4, lr=1e-3)
+    assert l1 < 0.1 * l0, (l0, l1)
+
+    def cold(T, attach):
+        n.attach(attach)
+        s.load_state(T=T, Tdot=zn, U=zu, P=zp)
+        s.stokes_resident()
+        n.attach(False)
+        st = s.stats()
+        return st, s.store_state()["U"], s.heat_flux()[0]
+
+    # held out: seed 0's initial state (white noise) and its state 5 steps later
+    T0 = seeded_T(dims, 0)
+    s.load_state(T=T0, Tdot=zn, U=zu, P=zp)
+    s.stokes_resident()
+    for _ in range(5):
+        s.step_resident(0.0)
+    T5 = s.store_state()["T"]
+    for T, need in ((T0, 0.9), (T5, 0.6)):
+        base, U0, nu0 = cold(T, False)
+        warm, U1, nu1 = cold(T, True)
+        print(f"uzawa {base['uzawa']} -> {warm['uzawa']}, mg passes {base['mg_passes']} -> {warm['mg_passes']}, "
+              f"initial residual {warm['base_residual']:.3e} -> {warm['warm_residual']:.3e}")
+        assert warm["warm_start"] == 1
+        assert warm["warm_residual"] < need * warm["base_residual"]
+        assert warm["uzawa"] <= base["uzawa"] + 2
+        # same stopping rule: the two solutions agree to the solve tolerance
+        assert np.linalg.norm(U1 - U0) < 1e-4 * np.linalg.norm(U0)
+        assert abs(nu1 - nu0) < 1e-5 * abs(nu0)
+
+    # a converged previous solution beats the network: the solve keeps it
+    n.attach(True)
+    s.stokes_resident()
+    assert s.stats()["warm_start"] == 0
+    n.attach(False)
+    n.close()
+    s.close()
