@@ -62,6 +62,10 @@ class Config:
     finetunedt: float = 0.75
     fixed_timestep: float = 0.0
     precision: int = FP64
+    # Geometry=Rsphere: (theta_north, theta_south, fi_west, fi_east) in degrees,
+    # (radius_inner, radius_outer); x, y, z of the mesh are then theta, phi, r
+    # and dimen is unused.  None: the Cartesian box.
+    sphere: Optional[tuple] = None
 
     @property
     def nox(self):
@@ -118,6 +122,10 @@ class _CConfig(ctypes.Structure):
         ("finetunedt", ctypes.c_double),
         ("fixed_timestep", ctypes.c_double),
         ("precision", ctypes.c_int),
+        ("sphere", ctypes.c_int),
+        ("theta", ctypes.c_double * 2),
+        ("fi", ctypes.c_double * 2),
+        ("radius", ctypes.c_double * 2),
     ]
 
 
@@ -281,6 +289,12 @@ class Solver:
         c.finetunedt = cfg.finetunedt
         c.fixed_timestep = cfg.fixed_timestep
         c.precision = cfg.precision
+        if cfg.sphere is not None:
+            tn, ts, fw, fe, ri, ro = cfg.sphere
+            c.sphere = 1
+            c.theta[0], c.theta[1] = tn, ts
+            c.fi[0], c.fi[1] = fw, fe
+            c.radius[0], c.radius[1] = ri, ro
         self._c = c
         h = ctypes.c_void_p()
         rc = self.lib.citcom_gpu_create(ctypes.byref(c), ctypes.byref(h))

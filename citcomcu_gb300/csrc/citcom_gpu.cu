@@ -31,13 +31,13 @@ enum Slot
 	S_LS = 2,     // line search (AU.res, AU.AU)
 	S_R0 = 4,     // scratch dots
 	S_DOT = 8,    // 4 dots
-	S_NU = 16,    // Nut, Nub sums
-	S_VRMS = 18,
+	S_NU = 32,    // heat flux: top and bottom sums, top and bottom weights
+	S_VRMS = 36,  // sum of |u|^2 dV, volume
 	S_MIN = 20,
 	S_MAX = 21,
 	S_UZ = 22,    // Uzawa scalars: r1.z1, r0.z0, s2.Ahat, alpha, error flag
 	S_TERR = 31,  // (host mirror only) the tile kernels' error word
-	S_COUNT = 32
+	S_COUNT = 40
 };
 
 template <typename T> struct MG
@@ -101,6 +101,7 @@ struct citcom_gpu
 	citcom_gpu_stats stats;
 	std::vector<void *> allocs;
 	citcom_nn *warm;   // warm-start network attached to the Stokes solve (not owned), or null
+	double diff_ts;    // diffusive time-step limit of the finest level
 	char err[512];
 };
 
@@ -188,6 +189,20 @@ void make_level(const citcom_gpu_config &c, int l, Lvl &L)
 		for(int p = 0; p < 2; ++p)
 			L.cnt[a][p] = (N[a] - p + 1) / 2;
 	cg_set_offsets(L);
+	if(c.sphere)
+	{
+		// uniform theta, phi, r grid (Nodal_mesh.c:87-95, 202-217), angles in radians
+		const double rad = M_PI / 180.0;
+		L.sphere = 1;
+		L.org[0] = c.theta[0] * rad;
+		L.org[1] = c.fi[0] * rad;
+		L.org[2] = c.radius[0];
+		L.h[0] = (c.theta[1] - c.theta[0]) * rad / L.elx;
+		L.h[1] = (c.fi[1] - c.fi[0]) * rad / L.ely;
+		L.h[2] = (c.radius[1] - c.radius[0]) / L.elz;
+		L.J = 0.0;
+		return;
+	}
 	L.h[0] = c.dimen[0] / L.elx;
 	L.h[1] = c.dimen[1] / L.ely;
 	L.h[2] = c.dimen[2] / L.elz;
@@ -376,7 +391,7 @@ template <typename T> void mg_proj(citcom_gpu *h, MG<T> &B, int lev, int src, in
 	if(co_level<T>(h, lev))
 		return co_push(h, CO_PROJ, lev, src, dst, 0);
 	co_flush(h);
-	launch_project<T>(h->st, h->lv[lev], h->lv[lev - 1], mg_vec(B, lev, src), mg_vec(B, lev - 1, dst));
+	launch_project<T>(h->st, h->lv[lev], h->lv[lev - 1], h->geo[lev - 1], mg_vec(B, lev, src), mg_vec(B, lev - 1, dst));
 }
 
 // vec dst (level lev) = interpolation of vec src (level lev-1)
@@ -385,7 +400,7 @@ template <typename T> void mg_interp(citcom_gpu *h, MG<T> &B, int lev, int src, 
 	if(co_level<T>(h, lev))
 		return co_push(h, CO_INTERP, lev, src, dst, 0);
 	co_flush(h);
-	launch_interp<T>(h->st, h->lv[lev - 1], h->lv[lev], mg_vec(B, lev - 1, src), mg_vec(B, lev, dst));
+	launch_interp<T>(h->st, h->lv[lev - 1], h->lv[lev], h->geo[lev], mg_vec(B, lev - 1, src), mg_vec(B, lev, dst));
 }
 
 // line search of the upward leg: AU = K del, vel += (AU.res / AU.AU) del
@@ -684,7 +699,7 @@ int construct_stiffness(citcom_gpu *h)
 int project_viscosity(citcom_gpu *h)
 {
 	for(int l = h->L - 1; l > 0; --l)
-		launch_project_viscosity(h->st, h->lv[l], h->lv[l - 1], h->geo[l - 1], h->evi[l], h->evi[l - 1], h->visc_work[0],
+		launch_project_viscosity(h->st, h->lv[l], h->lv[l - 1], h->geo[l], h->geo[l - 1], h->evi[l], h->evi[l - 1], h->visc_work[0],
 		                         h->visc_work[1]);
 	CK(cudaGetLastError());
 	h->visc_ready = true;
@@ -701,7 +716,7 @@ int viscosity_from_device_T(citcom_gpu *h)
 int forces_from_device_T(citcom_gpu *h)
 {
 	const int lmax = h->L - 1;
-	launch_buoyancy(h->st, h->lv[lmax], h->cfg.rayleigh, h->T, h->buoy);
+	launch_buoyancy(h->st, h->lv[lmax], h->geo[lmax], h->cfg.rayleigh, h->T, h->buoy);
 	launch_forces(h->st, h->lv[lmax], h->geo[lmax], h->buoy, h->F);
 	CK(cudaGetLastError());
 	return CITCOM_GPU_OK;
@@ -750,11 +765,8 @@ int pg_timestep(citcom_gpu *h, citcom_gpu_advection *adv)
 		dt = c.fixed_timestep;
 	else
 	{
-		double diff_ts = 1.0e8;
-		for(int d = 0; d < 3; ++d)
-			diff_ts = std::fmin(diff_ts, Lf.h[d] * Lf.h[d]);
-		diff_ts *= 0.5;
-		launch_adv_timestep(st, Lf, h->V, red_of(h), h->dscal + S_MIN);
+		const double diff_ts = h->diff_ts;
+		launch_adv_timestep(st, Lf, geo, h->V, red_of(h), h->dscal + S_MIN);
 		TRY(readback(h, S_MIN, 1));
 		const double adv_ts = c.finetunedt * h->hscal[S_MIN];
 		dt = 1.0e-32 + (adv_ts < diff_ts ? adv_ts : diff_ts);
@@ -774,7 +786,7 @@ int pg_timestep(citcom_gpu *h, citcom_gpu_advection *adv)
 		for(int pass = 0; pass < c.adv_sub_iterations; ++pass)
 		{
 			launch_pg_residual(st, Lf, geo, h->T, h->Tdot, h->V, c.Q0, h->Eres);
-			launch_pg_gather(st, Lf, h->Eres, h->DTdot);
+			launch_pg_gather(st, Lf, geo, h->Eres, h->DTdot);
 			launch_corrector(st, Lf, h->T, h->Tdot, h->DTdot, dt, gamma);
 		}
 		launch_tmax(st, Lf.nno, h->T, red_of(h), h->dscal + S_MAX);
@@ -941,13 +953,24 @@ int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 		for(int l = 0; l < h->L; ++l)
 		{
 			const Lvl &L = h->lv[l];
-			Geo g;
-			geo_fill_host(L, &g);
-			TRYC(dalloc(h, &h->geo[l], 1));
-			if(cudaMemcpy(h->geo[l], &g, sizeof(Geo), cudaMemcpyHostToDevice) != cudaSuccess)
 			{
-				r = fail(h, CITCOM_GPU_ERR_CUDA, "geometry upload failed");
-				goto failed;
+				std::vector<Geo> g(geo_count(L));
+				geo_fill_host(L, g.data());
+				TRYC(dalloc(h, &h->geo[l], g.size()));
+				if(cudaMemcpy(h->geo[l], g.data(), sizeof(Geo) * g.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+				{
+					r = fail(h, CITCOM_GPU_ERR_CUDA, "geometry upload failed");
+					goto failed;
+				}
+				if(l == lmax)
+				{
+					// std_timestep's diffusive limit: half the smallest squared element size (:760-772)
+					h->diff_ts = 1.0e8;
+					for(const Geo &e : g)
+						for(int d = 0; d < 3; ++d)
+							h->diff_ts = std::fmin(h->diff_ts, e.size[d] * e.size[d]);
+					h->diff_ts *= 0.5;
+				}
 			}
 			TRYC(dalloc(h, &h->evi[l], (size_t)L.nel * 8));
 			const bool need64 = (cfg->precision == CITCOM_GPU_FP64) || l == lmax;
@@ -985,6 +1008,7 @@ int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 			h->co_lv.win[l] = coarse_window(h->lv[l], h->co_cluster);
 			h->co_lv.L[l] = h->lv[l];
 			h->co_lv.Kt[l] = h->Kt32[l];
+			h->co_lv.geo[l] = h->geo[l];
 			h->co_lv.BI[l] = h->BI32[l];
 			for(int v = 0; v < CO_NVEC; ++v)
 				h->co_lv.vec[l][v] = mg_vec(h->mg32, l, v);
@@ -1218,12 +1242,12 @@ int citcom_gpu_heat_flux(citcom_gpu *h, const double *T, const double *V, double
 	if(V)
 		TRY(h2d(h, h->V, V, sizeof(double) * 3 * Lf.nno));
 	launch_heat_flux(h->st, Lf, h->geo[lmax], dT, dV, h->hf_work, red_of(h), h->dscal + S_NU);
-	TRY(readback(h, S_NU, 2));
-	const double ns = 4.0 * (double)Lf.elx * (double)Lf.ely;
+	TRY(readback(h, S_NU, 4));
+	// Nu = sum of (4-node flux sum x element volume) / (4 x sum of volumes) (Process_buoyancy.c:163-196)
 	if(nut)
-		*nut = h->hscal[S_NU] / ns;
+		*nut = h->hscal[S_NU] / (4.0 * h->hscal[S_NU + 2]);
 	if(nub)
-		*nub = h->hscal[S_NU + 1] / ns;
+		*nub = h->hscal[S_NU + 1] / (4.0 * h->hscal[S_NU + 3]);
 	return CITCOM_GPU_OK;
 }
 
@@ -1235,9 +1259,9 @@ int citcom_gpu_vrms(citcom_gpu *h, const double *V, double *vrms)
 	if(V)
 		TRY(h2d(h, h->V, V, sizeof(double) * 3 * Lf.nno));
 	launch_vrms(h->st, Lf, h->geo[lmax], h->V, red_of(h), h->dscal + S_VRMS);
-	TRY(readback(h, S_VRMS, 1));
+	TRY(readback(h, S_VRMS, 2));
 	if(vrms)
-		*vrms = std::sqrt(h->hscal[S_VRMS] / (8.0 * Lf.J * Lf.nel));
+		*vrms = std::sqrt(h->hscal[S_VRMS] / h->hscal[S_VRMS + 1]);
 	return CITCOM_GPU_OK;
 }
 
@@ -1418,7 +1442,7 @@ int citcom_gpu_op_project(citcom_gpu *h, int fine_lev, const double *AU, double 
 		dst = h->Ah;
 	}
 	TRY(h2d(h, src, AU, sizeof(double) * Lf.neq));
-	launch_project<double>(h->st, Lf, Lc, src, dst);
+	launch_project<double>(h->st, Lf, Lc, h->geo[fine_lev - 1], src, dst);
 	TRY(d2h(h, AD, dst, sizeof(double) * Lc.neq));
 	return sync(h);
 }
@@ -1442,7 +1466,7 @@ int citcom_gpu_op_interp(citcom_gpu *h, int coarse_lev, const double *AD, double
 		dst = h->Ah;
 	}
 	TRY(h2d(h, src, AD, sizeof(double) * Lc.neq));
-	launch_interp<double>(h->st, Lc, Lf, src, dst);
+	launch_interp<double>(h->st, Lc, Lf, h->geo[coarse_lev + 1], src, dst);
 	TRY(d2h(h, AU, dst, sizeof(double) * Lf.neq));
 	return sync(h);
 }
@@ -1597,7 +1621,7 @@ int nn_guess(citcom_nn *n)
 	for(int l = n->lev; l < lmax; ++l)
 	{
 		double *dst = (l + 1 == lmax) ? n->Ug : n->Uv[l + 1];
-		launch_interp<double>(h->st, h->lv[l], h->lv[l + 1], n->Uv[l], dst);
+		launch_interp<double>(h->st, h->lv[l], h->lv[l + 1], h->geo[l + 1], n->Uv[l], dst);
 		launch_strip(h->st, h->lv[l + 1], dst);
 	}
 	CK(cudaGetLastError());

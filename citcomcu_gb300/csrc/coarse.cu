@@ -616,7 +616,7 @@ __global__ void __launch_bounds__(CO_THREADS) k_coarse(const __grid_constant__ C
 			for(int b = 8 * lo; b < 8 * (lo + cnt); b += blockDim.x)
 			{
 				const int t = b + threadIdx.x;
-				project_lanes<false, float, float>(L, Lc, sv, D.vec[l - 1][op.b], t < 8 * (lo + cnt) ? t : 8 * Lc.nno);
+				project_lanes<false, float, float>(L, Lc, D.geo[l - 1], sv, D.vec[l - 1][op.b], t < 8 * (lo + cnt) ? t : 8 * Lc.nno);
 			}
 			halo_lev = -1;
 			break;
@@ -630,7 +630,7 @@ __global__ void __launch_bounds__(CO_THREADS) k_coarse(const __grid_constant__ C
 			int lo, cnt;
 			co_chunk(L.nno, rank, ncta, lo, cnt);
 			for(int n = lo + threadIdx.x; n < lo + cnt; n += blockDim.x)
-				interp_node<false, float>(D.L[l - 1], L, sv, D.vec[l][op.b], n);
+				interp_node<false, float>(D.L[l - 1], L, D.geo[l], sv, D.vec[l][op.b], n);
 			halo_lev = -1;
 			break;
 		}

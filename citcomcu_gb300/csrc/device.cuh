@@ -91,16 +91,16 @@ template <bool CG, typename T> __device__ __forceinline__ T ldv(const T *p)
 
 // project_vector (Solver_multigrid.c:72-159), node-centred: 8 consecutive
 // lanes serve one coarse node, lane a its coarse element at corner a (the
-// fine sub-element of that corner); the lanes' sums are added by shuffles.
-// Followed by strip_bcs_from_residual on the coarse level.  t is the lane's
-// global index (coarse node t / 8); all 32 lanes of a warp must call it.
-// ACC: the type the sums are formed in.
+// fine sub-element of that corner), weighted by that element's TWW of the
+// node; the lanes' sums are added by shuffles and divided by the node's
+// lumped mass (the sum of the weights).  Followed by strip_bcs_from_residual
+// on the coarse level.  t is the lane's global index (coarse node t / 8); all
+// 32 lanes of a warp must call it.  ACC: the type the sums are formed in.
 template <bool CG, typename T, typename ACC = double>
-__device__ __forceinline__ void project_lanes(const Lvl &Lf, const Lvl &Lc, const T *AU, T *AD, int t)
+__device__ __forceinline__ void project_lanes(const Lvl &Lf, const Lvl &Lc, const Geo *gc, const T *AU, T *AD, int t)
 {
 	const int N = t >> 3, a = t & 7;
-	ACC s0 = 0, s1 = 0, s2 = 0;
-	int cnt = 0;
+	ACC s0 = 0, s1 = 0, s2 = 0, w = 0;
 	int X = 0, Y = 0, Z = 0;
 	if(N < Lc.nno)
 	{
@@ -111,7 +111,7 @@ __device__ __forceinline__ void project_lanes(const Lvl &Lf, const Lvl &Lc, cons
 		const int ex = X - ox, ey = Y - oy, ez = Z - oz;
 		if(ex >= 0 && ex < Lc.elx && ey >= 0 && ey < Lc.ely && ez >= 0 && ez < Lc.elz)
 		{
-			cnt = 1;
+			w = (ACC)gc[cg_col(Lc, ex, ez)].tww[a];
 			const int fx = 2 * ex + ox, fy = 2 * ey + oy, fz = 2 * ez + oz;
 			ACC t0 = 0, t1 = 0, t2 = 0;
 #pragma unroll
@@ -122,9 +122,9 @@ __device__ __forceinline__ void project_lanes(const Lvl &Lf, const Lvl &Lc, cons
 				t1 += (ACC)ldv<CG>(AU + 3 * m + 1);
 				t2 += (ACC)ldv<CG>(AU + 3 * m + 2);
 			}
-			s0 = (ACC)Lc.J * t0;
-			s1 = (ACC)Lc.J * t1;
-			s2 = (ACC)Lc.J * t2;
+			s0 = w * t0;
+			s1 = w * t1;
+			s2 = w * t2;
 		}
 	}
 	// fixed-order sum over the 8 corners (lane a of the group holds corner a)
@@ -133,11 +133,11 @@ __device__ __forceinline__ void project_lanes(const Lvl &Lf, const Lvl &Lc, cons
 		s0 += __shfl_xor_sync(0xffffffffu, s0, o);
 		s1 += __shfl_xor_sync(0xffffffffu, s1, o);
 		s2 += __shfl_xor_sync(0xffffffffu, s2, o);
-		cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+		w += __shfl_xor_sync(0xffffffffu, w, o);
 	}
 	if(N < Lc.nno && a == 0)
 	{
-		const ACC mass = (ACC)1 / ((ACC)cnt * (ACC)Lc.J);
+		const ACC mass = (ACC)1 / w;
 		const unsigned f = cg_vflag(Lc, X, Y, Z);
 		AD[3 * N] = (f & 1u) ? (T)0 : (T)(s0 * mass);
 		AD[3 * N + 1] = (f & 2u) ? (T)0 : (T)(s1 * mass);
@@ -147,25 +147,50 @@ __device__ __forceinline__ void project_lanes(const Lvl &Lf, const Lvl &Lc, cons
 
 // interp_vector (Solver_multigrid.c:173-298): injection, then linear fill
 // along x (y,z even), along z (y even) and along y, in that order; evaluated
-// per fine node with the same operation order.  Strips the fine level.
+// per fine node with the same operation order.  Strips the fine level.  The
+// fill weights are x2 / (x1 + x2), x1 / (x1 + x2) with x1, x2 the sizes (along
+// the fill) of the first elements of the two neighbours (element index order:
+// corner (max(X-1, 0), ., max(Z-1, 0))): 1/2 on the box; in the sphere the
+// theta and r sizes of an element depend on its column.
 template <bool CG, typename T> __device__ __forceinline__ T coarse_at(const Lvl &Lc, const T *AD, int x, int y, int z, int d)
 {
 	return ldv<CG>(AD + 3 * cg_node(Lc, x >> 1, y >> 1, z >> 1) + d);
 }
-template <bool CG, typename T> __device__ __forceinline__ T fill_x(const Lvl &Lc, const T *AD, int x, int y, int z, int d)
+template <bool CG, typename T>
+__device__ __forceinline__ T fill_x(const Lvl &Lc, const Lvl &Lf, const Geo *gf, const T *AD, int x, int y, int z, int d)
 {
 	if(x & 1)
+	{
+		if(Lf.sphere)
+		{
+			const int ez = z > 0 ? z - 1 : 0;
+			const double x1 = gf[cg_col(Lf, x >= 2 ? x - 2 : 0, ez)].size[0], x2 = gf[cg_col(Lf, x, ez)].size[0];
+			return (T)(x2 / (x1 + x2)) * coarse_at<CG>(Lc, AD, x - 1, y, z, d) +
+			       (T)(x1 / (x1 + x2)) * coarse_at<CG>(Lc, AD, x + 1, y, z, d);
+		}
 		return (T)0.5 * coarse_at<CG>(Lc, AD, x - 1, y, z, d) + (T)0.5 * coarse_at<CG>(Lc, AD, x + 1, y, z, d);
+	}
 	return coarse_at<CG>(Lc, AD, x, y, z, d);
 }
-template <bool CG, typename T> __device__ __forceinline__ T fill_z(const Lvl &Lc, const T *AD, int x, int y, int z, int d)
+template <bool CG, typename T>
+__device__ __forceinline__ T fill_z(const Lvl &Lc, const Lvl &Lf, const Geo *gf, const T *AD, int x, int y, int z, int d)
 {
 	if(z & 1)
-		return (T)0.5 * fill_x<CG>(Lc, AD, x, y, z - 1, d) + (T)0.5 * fill_x<CG>(Lc, AD, x, y, z + 1, d);
-	return fill_x<CG>(Lc, AD, x, y, z, d);
+	{
+		if(Lf.sphere)
+		{
+			const int ex = x > 0 ? x - 1 : 0;
+			const double x1 = gf[cg_col(Lf, ex, z >= 2 ? z - 2 : 0)].size[2], x2 = gf[cg_col(Lf, ex, z)].size[2];
+			return (T)(x2 / (x1 + x2)) * fill_x<CG>(Lc, Lf, gf, AD, x, y, z - 1, d) +
+			       (T)(x1 / (x1 + x2)) * fill_x<CG>(Lc, Lf, gf, AD, x, y, z + 1, d);
+		}
+		return (T)0.5 * fill_x<CG>(Lc, Lf, gf, AD, x, y, z - 1, d) + (T)0.5 * fill_x<CG>(Lc, Lf, gf, AD, x, y, z + 1, d);
+	}
+	return fill_x<CG>(Lc, Lf, gf, AD, x, y, z, d);
 }
+// the y fill's two neighbours share their first element's (x, z) column: 1/2
 template <bool CG, typename T>
-__device__ __forceinline__ void interp_node(const Lvl &Lc, const Lvl &Lf, const T *AD, T *AU, int n)
+__device__ __forceinline__ void interp_node(const Lvl &Lc, const Lvl &Lf, const Geo *gf, const T *AD, T *AU, int n)
 {
 	const int z = n % Lf.noz, x = (n / Lf.noz) % Lf.nox, y = n / (Lf.noz * Lf.nox);
 	const unsigned f = cg_vflag(Lf, x, y, z);
@@ -174,9 +199,9 @@ __device__ __forceinline__ void interp_node(const Lvl &Lc, const Lvl &Lf, const 
 	{
 		T v;
 		if(y & 1)
-			v = (T)0.5 * fill_z<CG>(Lc, AD, x, y - 1, z, d) + (T)0.5 * fill_z<CG>(Lc, AD, x, y + 1, z, d);
+			v = (T)0.5 * fill_z<CG>(Lc, Lf, gf, AD, x, y - 1, z, d) + (T)0.5 * fill_z<CG>(Lc, Lf, gf, AD, x, y + 1, z, d);
 		else
-			v = fill_z<CG>(Lc, AD, x, y, z, d);
+			v = fill_z<CG>(Lc, Lf, gf, AD, x, y, z, d);
 		AU[3 * n + d] = ((f >> d) & 1u) ? (T)0 : v;
 	}
 }

@@ -146,6 +146,7 @@ __global__ void k_assemble(Lvl L, const Geo *__restrict__ geo, const double *__r
 						if(oz + dz < 0 || oz + dz > 1 || z - oz < 0 || z - oz >= L.elz)
 							continue;
 						const int e = (z - oz) + L.elz * ((x - ox) + L.elx * (y - oy));
+						const Geo *G = geo + cg_col(L, x - ox, z - oz);
 						const int a = cg_local_index(ox, oy, oz);
 						const int b = cg_local_index(ox + dx, oy + dy, oz + dz);
 						double eta[8], mean = 0.0;
@@ -162,9 +163,9 @@ __global__ void k_assemble(Lvl L, const Geo *__restrict__ geo, const double *__r
 							double v = 0.0;
 #pragma unroll
 							for(int k = 0; k < 8; ++k)
-								v += eta[k] * geo->Mk[k][a][b][q];
+								v += eta[k] * G->Mk[k][a][b][q];
 							if(aug)
-								v += mean * lambda * geo->g[3 * a + q / 3] * geo->g[3 * b + q % 3];
+								v += mean * lambda * G->g[3 * a + q / 3] * G->g[3 * b + q % 3];
 							blk[q] += v;
 						}
 						if(s == 13)
@@ -176,9 +177,9 @@ __global__ void k_assemble(Lvl L, const Geo *__restrict__ geo, const double *__r
 								double v = 0.0;
 #pragma unroll
 								for(int k = 0; k < 8; ++k)
-									v += eta[k] * geo->Mk[k][a][a][4 * i];
+									v += eta[k] * G->Mk[k][a][a][4 * i];
 								if(aug)
-									v += mean * lambda * geo->g[3 * a + i] * geo->g[3 * a + i];
+									v += mean * lambda * G->g[3 * a + i] * G->g[3 * a + i];
 								diag[i] += v;
 							}
 						}
@@ -228,6 +229,7 @@ __global__ void k_bpi(Lvl L, const Geo *__restrict__ geo, const double *__restri
 		return;
 	}
 	const int ez = e % L.elz, ex = (e / L.elz) % L.elx, ey = e / (L.elz * L.elx);
+	const Geo *G = geo + cg_col(L, ex, ez);
 	double bu = 0.0;
 	for(int a = 0; a < 8; ++a)
 	{
@@ -235,7 +237,7 @@ __global__ void k_bpi(Lvl L, const Geo *__restrict__ geo, const double *__restri
 #pragma unroll
 		for(int i = 0; i < 3; ++i)
 		{
-			const double g = geo->g[3 * a + i];
+			const double g = G->g[3 * a + i];
 			bu += g * g * BI[3 * (size_t)p + i];
 		}
 	}
@@ -694,19 +696,22 @@ __global__ void k_tiny_stencil(Lvl L, const float *__restrict__ K, float *__rest
 // ---------------------------------------------------------------- transfers
 
 template <typename T>
-__global__ void k_project(Lvl Lf, Lvl Lc, const T *__restrict__ AU, T *__restrict__ AD)
+__global__ void k_project(Lvl Lf, Lvl Lc, const Geo *__restrict__ gc, const T *__restrict__ AU, T *__restrict__ AD)
 {
 	pdl_begin();
-	project_lanes<false, T>(Lf, Lc, AU, AD, blockIdx.x * blockDim.x + threadIdx.x);
+	// sums in the level's own precision: FP64 for the FP64 path; FP32 for the
+	// FP32 multigrid (as in the cluster program), where FP64 arithmetic would
+	// run at GB300's low FP64 rate
+	project_lanes<false, T, T>(Lf, Lc, gc, AU, AD, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 template <typename T>
-__global__ void k_interp(Lvl Lc, Lvl Lf, const T *__restrict__ AD, T *__restrict__ AU)
+__global__ void k_interp(Lvl Lc, Lvl Lf, const Geo *__restrict__ gf, const T *__restrict__ AD, T *__restrict__ AU)
 {
 	pdl_begin();
 	const int n = blockIdx.x * blockDim.x + threadIdx.x;
 	if(n < Lf.nno)
-		interp_node<false, T>(Lc, Lf, AD, AU, n);
+		interp_node<false, T>(Lc, Lf, gf, AD, AU, n);
 }
 
 // ---------------------------------------------------------------- div / grad
@@ -719,12 +724,13 @@ __global__ void k_div(Lvl L, const Geo *__restrict__ geo, const double *__restri
 	if(e >= L.nel)
 		return;
 	const int ez = e % L.elz, ex = (e / L.elz) % L.elx, ey = e / (L.elz * L.elx);
+	const Geo *G = geo + cg_col(L, ex, ez);
 	double s = 0.0;
 #pragma unroll
 	for(int a = 0; a < 8; ++a)
 	{
 		const int n = cg_node(L, ex + cg_loc(a, 0), ey + cg_loc(a, 1), ez + cg_loc(a, 2));
-		s += geo->g[3 * a] * U[3 * n] + geo->g[3 * a + 1] * U[3 * n + 1] + geo->g[3 * a + 2] * U[3 * n + 2];
+		s += G->g[3 * a] * U[3 * n] + G->g[3 * a + 1] * U[3 * n + 1] + G->g[3 * a + 2] * U[3 * n + 2];
 	}
 	divU[e] = s;
 }
@@ -744,9 +750,10 @@ __global__ void k_grad(Lvl L, const Geo *__restrict__ geo, const double *__restr
 		if(ex < 0 || ex >= L.elx || ey < 0 || ey >= L.ely || ez < 0 || ez >= L.elz)
 			continue;
 		const double p = P[ez + L.elz * (ex + L.elx * ey)];
-		g0 += geo->g[3 * a] * p;
-		g1 += geo->g[3 * a + 1] * p;
-		g2 += geo->g[3 * a + 2] * p;
+		const Geo *G = geo + cg_col(L, ex, ez);
+		g0 += G->g[3 * a] * p;
+		g1 += G->g[3 * a + 1] * p;
+		g2 += G->g[3 * a + 2] * p;
 	}
 	const unsigned f = cg_vflag(L, x, y, z);
 	gradP[3 * n] = (f & 1u) ? 0.0 : g0;
@@ -933,7 +940,8 @@ __global__ void k_visc_from_T(Lvl L, const Geo *__restrict__ geo, Rheo r, const 
 	if(e >= L.nel)
 		return;
 	const int ez = e % L.elz, ex = (e / L.elz) % L.elx, ey = e / (L.elz * L.elx);
-	const double zc = ((double)ez + 0.5) * L.h[2];
+	const double zc = L.org[2] + ((double)ez + 0.5) * L.h[2];
+	const Geo *G = geo + cg_col(L, ex, ez);
 	int layer = 0;
 	for(int i = 0; i < r.num_mat - 1; ++i)
 		if(zc >= r.z_layer[i])
@@ -960,7 +968,7 @@ __global__ void k_visc_from_T(Lvl L, const Geo *__restrict__ geo, Rheo r, const 
 			double t = 1.0e-32;
 #pragma unroll
 			for(int a = 0; a < 8; ++a)
-				t += TT[a] * geo->N[k][a];
+				t += TT[a] * G->N[k][a];
 			v = r.visc0[m] * exp(r.viscE[m] * (r.viscT[m] - t));
 		}
 		else
@@ -974,53 +982,53 @@ __global__ void k_visc_from_T(Lvl L, const Geo *__restrict__ geo, Rheo r, const 
 }
 
 // visc_from_gint_to_nodes (Nodal_mesh.c:583-615)
-__global__ void k_visc_to_nodes(Lvl L, const double *__restrict__ evi, double *__restrict__ VN)
+__global__ void k_visc_to_nodes(Lvl L, const Geo *__restrict__ geo, const double *__restrict__ evi, double *__restrict__ VN)
 {
 	pdl_begin();
 	const int n = blockIdx.x * blockDim.x + threadIdx.x;
 	if(n >= L.nno)
 		return;
 	const int z = n % L.noz, x = (n / L.noz) % L.nox, y = n / (L.noz * L.nox);
-	double s = 0.0;
-	int cnt = 0;
+	double s = 0.0, m = 0.0;
 	for(int a = 0; a < 8; ++a)
 	{
 		const int ex = x - cg_loc(a, 0), ey = y - cg_loc(a, 1), ez = z - cg_loc(a, 2);
 		if(ex < 0 || ex >= L.elx || ey < 0 || ey >= L.ely || ez < 0 || ez >= L.elz)
 			continue;
 		const int e = ez + L.elz * (ex + L.elx * ey);
+		const double w = geo[cg_col(L, ex, ez)].tww[a];
 		double t = 0.0;
 		for(int k = 0; k < 8; ++k)
 			t += evi[8 * e + k];
-		s += L.J * (t / 8.0);
-		++cnt;
+		s += w * (t / 8.0);
+		m += w;
 	}
-	VN[n] = s * (1.0 / ((double)cnt * L.J));
+	VN[n] = s * (1.0 / m);
 }
 
 // project_scalar (Solver_multigrid.c:338-394)
-__global__ void k_project_scalar(Lvl Lf, Lvl Lc, const double *__restrict__ VN, double *__restrict__ VD)
+__global__ void k_project_scalar(Lvl Lf, Lvl Lc, const Geo *__restrict__ geoc, const double *__restrict__ VN, double *__restrict__ VD)
 {
 	pdl_begin();
 	const int N = blockIdx.x * blockDim.x + threadIdx.x;
 	if(N >= Lc.nno)
 		return;
 	const int Z = N % Lc.noz, X = (N / Lc.noz) % Lc.nox, Y = N / (Lc.noz * Lc.nox);
-	double s = 0.0;
-	int cnt = 0;
+	double s = 0.0, m = 0.0;
 	for(int a = 0; a < 8; ++a)
 	{
 		const int ox = cg_loc(a, 0), oy = cg_loc(a, 1), oz = cg_loc(a, 2);
 		const int ex = X - ox, ey = Y - oy, ez = Z - oz;
 		if(ex < 0 || ex >= Lc.elx || ey < 0 || ey >= Lc.ely || ez < 0 || ez >= Lc.elz)
 			continue;
-		++cnt;
+		const double w = geoc[cg_col(Lc, ex, ez)].tww[a];
+		m += w;
 		double t = 0.0;
 		for(int b = 0; b < 8; ++b)
 			t += VN[cg_node(Lf, 2 * ex + ox + cg_loc(b, 0), 2 * ey + oy + cg_loc(b, 1), 2 * ez + oz + cg_loc(b, 2))];
-		s += (t / 8.0) * Lc.J;
+		s += (t / 8.0) * w;
 	}
-	VD[N] = s * (1.0 / ((double)cnt * Lc.J));
+	VD[N] = s * (1.0 / m);
 }
 
 // visc_from_nodes_to_gint (Nodal_mesh.c:617-640)
@@ -1031,6 +1039,7 @@ __global__ void k_visc_to_gint(Lvl L, const Geo *__restrict__ geo, const double 
 	if(e >= L.nel)
 		return;
 	const int ez = e % L.elz, ex = (e / L.elz) % L.elx, ey = e / (L.elz * L.elx);
+	const Geo *G = geo + cg_col(L, ex, ez);
 	double v[8];
 #pragma unroll
 	for(int a = 0; a < 8; ++a)
@@ -1041,24 +1050,35 @@ __global__ void k_visc_to_gint(Lvl L, const Geo *__restrict__ geo, const double 
 		double t = 0.0;
 #pragma unroll
 		for(int a = 0; a < 8; ++a)
-			t += geo->N[k][a] * v[a];
+			t += G->N[k][a] * v[a];
 		evi[8 * e + k] = t;
 	}
 }
 
 // ---------------------------------------------------------------- forces
 
-// return_horiz_ave (Global_operations.c:133-251) of Ra*T, one block per z layer
-__global__ void k_horiz_ave(Lvl L, double Ra, const double *__restrict__ T, double *__restrict__ H)
+// return_horiz_ave (Global_operations.c:133-251) of Ra*T, one block per z
+// layer: the lower faces of the layer's elements (the top node layer takes the
+// top elements' lower-face weights, as the reference does)
+__global__ void k_horiz_ave(Lvl L, const Geo *__restrict__ geo, double Ra, const double *__restrict__ T, double *__restrict__ H)
 {
 	pdl_begin();
 	const int z = blockIdx.x;
 	__shared__ double sh[2][TPB / 32];
 	double s = 0.0, w = 0.0;
 	const double dg = L.h[0] * L.h[1] / 4.0;
+	const int ez = z < L.elz ? z : L.elz - 1;
 	for(int i = threadIdx.x; i < L.elx * L.ely; i += blockDim.x)
 	{
 		const int x = i % L.elx, y = i / L.elx;
+		if(L.sphere)
+		{
+			const double *wf = geo[cg_col(L, x, ez)].wface;
+			s += Ra * T[cg_node(L, x, y, z)] * wf[0] + Ra * T[cg_node(L, x + 1, y, z)] * wf[1] +
+			     Ra * T[cg_node(L, x + 1, y + 1, z)] * wf[2] + Ra * T[cg_node(L, x, y + 1, z)] * wf[3];
+			w += wf[0] + wf[1] + wf[2] + wf[3];
+			continue;
+		}
 		s += dg * (Ra * T[cg_node(L, x, y, z)] + Ra * T[cg_node(L, x + 1, y, z)] + Ra * T[cg_node(L, x + 1, y + 1, z)] +
 		           Ra * T[cg_node(L, x, y + 1, z)]);
 		w += 4.0 * dg;
@@ -1095,7 +1115,7 @@ __global__ void k_buoyancy(Lvl L, double Ra, const double *__restrict__ T, const
 		b[n] = Ra * T[n] - H[n % L.noz];
 }
 
-// assemble_forces + get_elt_f (Element_calculations.c:74-125, 989-1075), node-centred, stripped
+// assemble_forces + get_elt_f (Element_calculations.c:74-125, 989-1120), node-centred, stripped
 __global__ void k_forces(Lvl L, const Geo *__restrict__ geo, const double *__restrict__ buoy, double *__restrict__ F)
 {
 	pdl_begin();
@@ -1103,29 +1123,35 @@ __global__ void k_forces(Lvl L, const Geo *__restrict__ geo, const double *__res
 	if(n >= L.nno)
 		return;
 	const int z = n % L.noz, x = (n / L.noz) % L.nox, y = n / (L.noz * L.nox);
-	double fz = 0.0;
+	double fn[3] = {0.0, 0.0, 0.0};
 	for(int a = 0; a < 8; ++a)
 	{
 		const int ex = x - cg_loc(a, 0), ey = y - cg_loc(a, 1), ez = z - cg_loc(a, 2);
 		if(ex < 0 || ex >= L.elx || ey < 0 || ey >= L.ely || ez < 0 || ez >= L.elz)
 			continue;
+		const Geo *G = geo + cg_col(L, ex, ez);
 		double bb[8];
 		for(int b = 0; b < 8; ++b)
 			bb[b] = buoy[cg_node(L, ex + cg_loc(b, 0), ey + cg_loc(b, 1), ez + cg_loc(b, 2))];
-		double s = 0.0;
+		double s[3] = {0.0, 0.0, 0.0};
 		for(int k = 0; k < 8; ++k)
 		{
 			double fg = 0.0;
 			for(int b = 0; b < 8; ++b)
-				fg += bb[b] * geo->N[k][b];
-			s += fg * geo->N[k][a] * L.J;
+				fg += bb[b] * G->N[k][b];
+			// the radial force of the Gauss point on node a's components
+			// (Cartesian: z only; spherical: Cc(3, i, a, k), :1086)
+			const double w = fg * G->N[k][a] * G->gda[k];
+			for(int i = 0; i < 3; ++i)
+				s[i] += w * G->cr[k][a][i];
 		}
-		fz += s;
+		for(int i = 0; i < 3; ++i)
+			fn[i] += s[i];
 	}
 	const unsigned f = cg_vflag(L, x, y, z);
-	F[3 * n] = 0.0;
-	F[3 * n + 1] = 0.0;
-	F[3 * n + 2] = (f & 4u) ? 0.0 : fz;
+	F[3 * n] = (f & 1u) ? 0.0 : fn[0];
+	F[3 * n + 1] = (f & 2u) ? 0.0 : fn[1];
+	F[3 * n + 2] = (f & 4u) ? 0.0 : fn[2];
 }
 
 // v_from_vector (Stokes_flow_Incomp.c:530-553): V[d*nno + n]; constrained dofs take VB = 0
@@ -1146,7 +1172,9 @@ __global__ void k_v_from_vector(Lvl L, const double *__restrict__ U, double *__r
 __device__ __forceinline__ bool t_dirichlet(const Lvl &L, int n) { int z = n % L.noz; return z == 0 || z == L.noz - 1; }
 
 // pg_solver's per-element work: pg_shape_fn (Advection_diffusion.c:448-555)
-// and element_residual (:564-727), Cartesian, diffusivity 1, Q = Q0
+// and element_residual (:564-727), diffusivity 1, Q = Q0; the spherical
+// branches scale the theta and phi derivatives by 1/r and 1/(r sin theta)
+// (:506-529, 620-641, 668-674), 1 in the box
 __global__ void k_pg_residual(Lvl L, const Geo *__restrict__ geo, const double *__restrict__ T, const double *__restrict__ Tdot,
                               const double *__restrict__ V, double Q0, double *__restrict__ Eres)
 {
@@ -1155,6 +1183,7 @@ __global__ void k_pg_residual(Lvl L, const Geo *__restrict__ geo, const double *
 	if(e >= L.nel)
 		return;
 	const int ez = e % L.elz, ex = (e / L.elz) % L.elx, ey = e / (L.elz * L.elx);
+	const Geo *G = geo + cg_col(L, ex, ez);
 	const double diff = 1.0, twodiff = 2.0 * diff;
 	double vn[8][3], tn[8], dtn[8];
 #pragma unroll
@@ -1177,7 +1206,7 @@ __global__ void k_pg_residual(Lvl L, const Geo *__restrict__ geo, const double *
 #pragma unroll
 	for(int d = 0; d < 3; ++d)
 	{
-		us[d] = fabs(uc[d] * L.h[d]);
+		us[d] = fabs(uc[d] * G->size[d]);
 		up[d] = (us[d] > twodiff) ? (1.0 - twodiff / us[d]) : 0.0;
 	}
 	const double unorm = uc[0] * uc[0] + uc[1] * uc[1] + uc[2] * uc[2];
@@ -1190,25 +1219,26 @@ __global__ void k_pg_residual(Lvl L, const Geo *__restrict__ geo, const double *
 	for(int k = 0; k < 8; ++k)
 	{
 		double v0 = 0, v1 = 0, v2 = 0, t0 = 0, t1 = 0, t2 = 0, dT = 0;
+		const double ri = G->rinv[k], rs = G->rsin[k], jk = G->gda[k];
 #pragma unroll
 		for(int a = 0; a < 8; ++a)
 		{
-			const double Nk = geo->N[k][a];
+			const double Nk = G->N[k][a];
 			dT += dtn[a] * Nk;
 			v0 += vn[a][0] * Nk;
 			v1 += vn[a][1] * Nk;
 			v2 += vn[a][2] * Nk;
-			t0 += geo->gnx[k][a][0] * tn[a];
-			t1 += geo->gnx[k][a][1] * tn[a];
-			t2 += geo->gnx[k][a][2] * tn[a];
+			t0 += G->gnx[k][a][0] * tn[a] * ri;
+			t1 += G->gnx[k][a][1] * tn[a] * rs;
+			t2 += G->gnx[k][a][2] * tn[a];
 		}
 		const double adv = dT - Q0 + v0 * t0 + v1 * t1 + v2 * t2;
 #pragma unroll
 		for(int a = 0; a < 8; ++a)
 		{
-			const double g0 = geo->gnx[k][a][0], g1 = geo->gnx[k][a][1], g2 = geo->gnx[k][a][2];
-			const double pg = geo->N[k][a] + adiff * (v0 * g0 + v1 * g1 + v2 * g2);
-			er[a] -= pg * L.J * adv + diff * L.J * (g0 * t0 + g1 * t1 + g2 * t2);
+			const double g0 = G->gnx[k][a][0], g1 = G->gnx[k][a][1], g2 = G->gnx[k][a][2];
+			const double pg = G->N[k][a] + adiff * (v0 * g0 * ri + v1 * g1 * rs + v2 * g2);
+			er[a] -= pg * jk * adv + diff * jk * (g0 * t0 * ri + g1 * t1 * rs + g2 * t2);
 		}
 	}
 #pragma unroll
@@ -1217,24 +1247,23 @@ __global__ void k_pg_residual(Lvl L, const Geo *__restrict__ geo, const double *
 }
 
 // DTdot = (sum of element residuals at the node) / lumped mass
-__global__ void k_pg_gather(Lvl L, const double *__restrict__ Eres, double *__restrict__ DTdot)
+__global__ void k_pg_gather(Lvl L, const Geo *__restrict__ geo, const double *__restrict__ Eres, double *__restrict__ DTdot)
 {
 	pdl_begin();
 	const int n = blockIdx.x * blockDim.x + threadIdx.x;
 	if(n >= L.nno)
 		return;
 	const int z = n % L.noz, x = (n / L.noz) % L.nox, y = n / (L.noz * L.nox);
-	double s = 0.0;
-	int cnt = 0;
+	double s = 0.0, m = 0.0;
 	for(int a = 0; a < 8; ++a)
 	{
 		const int ex = x - cg_loc(a, 0), ey = y - cg_loc(a, 1), ez = z - cg_loc(a, 2);
 		if(ex < 0 || ex >= L.elx || ey < 0 || ey >= L.ely || ez < 0 || ez >= L.elz)
 			continue;
 		s += Eres[8 * (size_t)(ez + L.elz * (ex + L.elx * ey)) + a];
-		++cnt;
+		m += geo[cg_col(L, ex, ez)].tww[a];
 	}
-	DTdot[n] = s * (1.0 / ((double)cnt * L.J));
+	DTdot[n] = s * (1.0 / m);
 }
 
 // predictor (Advection_diffusion.c:352-367)
@@ -1311,7 +1340,7 @@ __global__ void k_max(int n, const double *__restrict__ T, Red red, double *out)
 }
 
 // advective part of std_timestep (Advection_diffusion.c:737-810): min over elements of 0.5/uc
-__global__ void k_adv_step(Lvl L, const double *__restrict__ V, Red red, double *out)
+__global__ void k_adv_step(Lvl L, const Geo *__restrict__ geo, const double *__restrict__ V, Red red, double *out)
 {
 	pdl_begin();
 	__shared__ double sh[RED_THREADS / 32];
@@ -1327,7 +1356,8 @@ __global__ void k_adv_step(Lvl L, const double *__restrict__ V, Red red, double 
 			for(int d = 0; d < 3; ++d)
 				uc[d] += 0.125 * V[(size_t)d * L.nno + n];
 		}
-		const double u = fabs(uc[0]) / L.h[0] + fabs(uc[1]) / L.h[1] + fabs(uc[2]) / L.h[2];
+		const Geo *G = geo + cg_col(L, ex, ez);
+		const double u = fabs(uc[0]) / G->size[0] + fabs(uc[1]) / G->size[1] + fabs(uc[2]) / G->size[2];
 		m = fmin(m, 0.5 / u);
 	}
 	for(int o = 16; o > 0; o >>= 1)
@@ -1367,6 +1397,7 @@ __global__ void k_hf_elem(Lvl L, const Geo *__restrict__ geo, const double *__re
 	if(e >= L.nel)
 		return;
 	const int ez = e % L.elz, ex = (e / L.elz) % L.elx, ey = e / (L.elz * L.elx);
+	const Geo *G = geo + cg_col(L, ex, ez);
 	double vz[8], tt[8];
 	for(int a = 0; a < 8; ++a)
 	{
@@ -1380,41 +1411,43 @@ __global__ void k_hf_elem(Lvl L, const Geo *__restrict__ geo, const double *__re
 		double u = 0, t = 0, dz = 0;
 		for(int a = 0; a < 8; ++a)
 		{
-			u += vz[a] * geo->N[k][a];
-			t += tt[a] * geo->N[k][a];
-			dz += tt[a] * geo->gnx[k][a][2];
+			u += vz[a] * G->N[k][a];
+			t += tt[a] * G->N[k][a];
+			dz += tt[a] * G->gnx[k][a][2];
 		}
-		uT += (u * t - dz) * L.J;
+		uT += (u * t - dz) * G->gda[k];
 	}
-	uTe[e] = uT / (8.0 * L.J);
+	uTe[e] = uT / G->area;
 }
 
 // step 2: nodal flux = TWW-weighted element means / lumped mass
-__global__ void k_hf_node(Lvl L, const double *__restrict__ uTe, double *__restrict__ hf)
+__global__ void k_hf_node(Lvl L, const Geo *__restrict__ geo, const double *__restrict__ uTe, double *__restrict__ hf)
 {
 	pdl_begin();
 	const int n = blockIdx.x * blockDim.x + threadIdx.x;
 	if(n >= L.nno)
 		return;
 	const int z = n % L.noz, x = (n / L.noz) % L.nox, y = n / (L.noz * L.nox);
-	double s = 0.0;
-	int cnt = 0;
+	double s = 0.0, m = 0.0;
 	for(int a = 0; a < 8; ++a)
 	{
 		const int ex = x - cg_loc(a, 0), ey = y - cg_loc(a, 1), ez = z - cg_loc(a, 2);
 		if(ex < 0 || ex >= L.elx || ey < 0 || ey >= L.ely || ez < 0 || ez >= L.elz)
 			continue;
-		s += L.J * uTe[ez + L.elz * (ex + L.elx * ey)];
-		++cnt;
+		const double w = geo[cg_col(L, ex, ez)].tww[a];
+		s += w * uTe[ez + L.elz * (ex + L.elx * ey)];
+		m += w;
 	}
-	hf[n] = s * (1.0 / ((double)cnt * L.J));
+	hf[n] = s * (1.0 / m);
 }
 
-// step 3: surface extrapolation 2 hf[s] - hf[s-1] and the element-area means; out = (Nut, Nub)
-__global__ void k_hf_surface(Lvl L, const double *__restrict__ hf, Red red, double *out)
+// step 3: surface extrapolation 2 hf[s] - hf[s-1], summed over the four nodes of
+// each surface element and weighted by the volume of the element below (top)
+// or above (bottom) it; out = (top sum, bottom sum, top weight, bottom weight)
+__global__ void k_hf_surface(Lvl L, const Geo *__restrict__ geo, const double *__restrict__ hf, Red red, double *out)
 {
 	pdl_begin();
-	double v[2] = {0.0, 0.0};
+	double v[4] = {0.0, 0.0, 0.0, 0.0};
 	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < L.elx * L.ely; i += gridDim.x * blockDim.x)
 	{
 		const int x = i % L.elx, y = i / L.elx;
@@ -1426,19 +1459,23 @@ __global__ void k_hf_surface(Lvl L, const double *__restrict__ hf, Red red, doub
 			tt += 2.0 * hf[top] - hf[top - 1];
 			tb += 2.0 * hf[bot] - hf[bot + 1];
 		}
-		v[0] += tt;
-		v[1] += tb;
+		const double at = geo[cg_col(L, x, L.elz - 1)].area, ab = geo[cg_col(L, x, 0)].area;
+		v[0] += tt * at;
+		v[1] += tb * ab;
+		v[2] += at;
+		v[3] += ab;
 	}
-	block_reduce_store<2>(v, red, out);
+	block_reduce_store<4>(v, red, out);
 }
 
 __global__ void k_vrms(Lvl L, const Geo *__restrict__ geo, const double *__restrict__ V, Red red, double *out)
 {
 	pdl_begin();
-	double v[1] = {0.0};
+	double v[2] = {0.0, 0.0};
 	for(int e = blockIdx.x * blockDim.x + threadIdx.x; e < L.nel; e += gridDim.x * blockDim.x)
 	{
 		const int ez = e % L.elz, ex = (e / L.elz) % L.elx, ey = e / (L.elz * L.elx);
+		const Geo *G = geo + cg_col(L, ex, ez);
 		double vn[8][3];
 		for(int a = 0; a < 8; ++a)
 		{
@@ -1451,14 +1488,15 @@ __global__ void k_vrms(Lvl L, const Geo *__restrict__ geo, const double *__restr
 			double u0 = 0, u1 = 0, u2 = 0;
 			for(int a = 0; a < 8; ++a)
 			{
-				u0 += geo->N[k][a] * vn[a][0];
-				u1 += geo->N[k][a] * vn[a][1];
-				u2 += geo->N[k][a] * vn[a][2];
+				u0 += G->N[k][a] * vn[a][0];
+				u1 += G->N[k][a] * vn[a][1];
+				u2 += G->N[k][a] * vn[a][2];
 			}
-			v[0] += L.J * (u0 * u0 + u1 * u1 + u2 * u2);
+			v[0] += G->gda[k] * (u0 * u0 + u1 * u1 + u2 * u2);
+			v[1] += G->gda[k];
 		}
 	}
-	block_reduce_store<1>(v, red, out);
+	block_reduce_store<2>(v, red, out);
 }
 
 } // namespace
@@ -1504,6 +1542,11 @@ static void launch_k(void (*kern)(KArgs...), dim3 grid, dim3 block, cudaStream_t
 
 void geo_fill_host(const Lvl &L, Geo *g)
 {
+	if(L.sphere)
+	{
+		geo_fill_sphere(L, g);
+		return;
+	}
 	const double beta = 0.57735026918962576451;
 	double gnx[8][8][3], gnxc[8][3];
 	for(int k = 0; k <= 8; ++k)
@@ -1545,6 +1588,23 @@ void geo_fill_host(const Lvl &L, Geo *g)
 	for(int a = 0; a < 8; ++a)
 		for(int d = 0; d < 3; ++d)
 			g->g[3 * a + d] = -gnxc[a][d] * 8.0 * L.J;
+	// box element: |J| is constant, TWW = J, the radial direction is z
+	for(int k = 0; k < 8; ++k)
+	{
+		g->gda[k] = L.J;
+		g->rinv[k] = 1.0;
+		g->rsin[k] = 1.0;
+		for(int a = 0; a < 8; ++a)
+			for(int i = 0; i < 3; ++i)
+				g->cr[k][a][i] = i == 2 ? 1.0 : 0.0;
+	}
+	for(int a = 0; a < 8; ++a)
+		g->tww[a] = L.J;
+	for(int d = 0; d < 3; ++d)
+		g->size[d] = L.h[d];
+	g->area = 8.0 * L.J;
+	for(int i = 0; i < 4; ++i)
+		g->wface[i] = L.h[0] * L.h[1] / 4.0;
 }
 
 void launch_assemble(cudaStream_t st, const Lvl &L, const Geo *geo, const double *evi, int aug, double lambda, double *K64,
@@ -1674,14 +1734,14 @@ void launch_gs_small(cudaStream_t st, const Lvl &L, const T *K, const T *BI, con
 		launch_k_smem(k_gs_small<T, 0>, g, b, gs_table_bytes(L), st, L, K, BI, F, d, cycles, zero_start);
 }
 
-template <typename T> void launch_project(cudaStream_t st, const Lvl &Lf, const Lvl &Lc, const T *AU, T *AD)
+template <typename T> void launch_project(cudaStream_t st, const Lvl &Lf, const Lvl &Lc, const Geo *gc, const T *AU, T *AD)
 {
-	launch_k(k_project<T>, nblocks(8 * (long)Lc.nno), TPB, st, Lf, Lc, AU, AD);
+	launch_k(k_project<T>, nblocks(8 * (long)Lc.nno), TPB, st, Lf, Lc, gc, AU, AD);
 }
 
-template <typename T> void launch_interp(cudaStream_t st, const Lvl &Lc, const Lvl &Lf, const T *AD, T *AU)
+template <typename T> void launch_interp(cudaStream_t st, const Lvl &Lc, const Lvl &Lf, const Geo *gf, const T *AD, T *AU)
 {
-	launch_k(k_interp<T>, nblocks(Lf.nno), TPB, st, Lc, Lf, AD, AU);
+	launch_k(k_interp<T>, nblocks(Lf.nno), TPB, st, Lc, Lf, gf, AD, AU);
 }
 
 template <typename T>
@@ -1696,8 +1756,8 @@ void launch_vel_update(cudaStream_t st, int n, T *vel, const T *del, T *res, con
 	template void launch_kmul_linesearch<T>(cudaStream_t, const Lvl &, const T *, const T *, const T *, T *, Red, double *); \
 	template void launch_gs_colour<T>(cudaStream_t, const Lvl &, const T *, const T *, const T *, T *, int);                 \
 	template void launch_gs_small<T>(cudaStream_t, const Lvl &, const T *, const T *, const T *, T *, int, int);             \
-	template void launch_project<T>(cudaStream_t, const Lvl &, const Lvl &, const T *, T *);                                 \
-	template void launch_interp<T>(cudaStream_t, const Lvl &, const Lvl &, const T *, T *);                                  \
+	template void launch_project<T>(cudaStream_t, const Lvl &, const Lvl &, const Geo *, const T *, T *);                    \
+	template void launch_interp<T>(cudaStream_t, const Lvl &, const Lvl &, const Geo *, const T *, T *);                     \
 	template void launch_vel_update<T>(cudaStream_t, int, T *, const T *, T *, const T *, const double *, int);
 INST(double)
 INST(float)
@@ -1776,19 +1836,19 @@ void launch_visc_from_T(cudaStream_t st, const Lvl &L, const Geo *geo, const Rhe
 	launch_k(k_visc_from_T, nblocks(L.nel), TPB, st, L, geo, r, T, evi);
 }
 
-void launch_project_viscosity(cudaStream_t st, const Lvl &Lf, const Lvl &Lc, const Geo *geoc, const double *evi_f, double *evi_c,
-                              double *work_f, double *work_c)
+void launch_project_viscosity(cudaStream_t st, const Lvl &Lf, const Lvl &Lc, const Geo *geof, const Geo *geoc, const double *evi_f,
+                              double *evi_c, double *work_f, double *work_c)
 {
-	launch_k(k_visc_to_nodes, nblocks(Lf.nno), TPB, st, Lf, evi_f, work_f);
-	launch_k(k_project_scalar, nblocks(Lc.nno), TPB, st, Lf, Lc, work_f, work_c);
+	launch_k(k_visc_to_nodes, nblocks(Lf.nno), TPB, st, Lf, geof, evi_f, work_f);
+	launch_k(k_project_scalar, nblocks(Lc.nno), TPB, st, Lf, Lc, geoc, work_f, work_c);
 	launch_k(k_visc_to_gint, nblocks(Lc.nel), TPB, st, Lc, geoc, work_c, evi_c);
 }
 
-void launch_buoyancy(cudaStream_t st, const Lvl &L, double Ra, const double *T, double *buoy)
+void launch_buoyancy(cudaStream_t st, const Lvl &L, const Geo *geo, double Ra, const double *T, double *buoy)
 {
 	// the layer means go into the tail of `buoy`'s companion buffer: buoy + nno (caller sizes it nno + noz)
 	double *H = buoy + L.nno;
-	launch_k(k_horiz_ave, L.noz, TPB, st, L, Ra, T, H);
+	launch_k(k_horiz_ave, L.noz, TPB, st, L, geo, Ra, T, H);
 	launch_k(k_buoyancy, nblocks(L.nno), TPB, st, L, Ra, T, H, buoy);
 }
 
@@ -1808,9 +1868,9 @@ void launch_pg_residual(cudaStream_t st, const Lvl &L, const Geo *geo, const dou
 	launch_k(k_pg_residual, nblocks(L.nel, 128), 128, st, L, geo, T, Tdot, V, Q0, Eres);
 }
 
-void launch_pg_gather(cudaStream_t st, const Lvl &L, const double *Eres, double *DTdot)
+void launch_pg_gather(cudaStream_t st, const Lvl &L, const Geo *geo, const double *Eres, double *DTdot)
 {
-	launch_k(k_pg_gather, nblocks(L.nno), TPB, st, L, Eres, DTdot);
+	launch_k(k_pg_gather, nblocks(L.nno), TPB, st, L, geo, Eres, DTdot);
 }
 
 void launch_predictor(cudaStream_t st, const Lvl &L, double *T, double *Tdot, double dt, double gamma)
@@ -1828,9 +1888,9 @@ void launch_tmax(cudaStream_t st, int n, const double *T, Red red, double *out)
 	launch_k(k_max, red_grid(n), RED_THREADS, st, n, T, red, out);
 }
 
-void launch_adv_timestep(cudaStream_t st, const Lvl &L, const double *V, Red red, double *out)
+void launch_adv_timestep(cudaStream_t st, const Lvl &L, const Geo *geo, const double *V, Red red, double *out)
 {
-	launch_k(k_adv_step, red_grid(L.nel), RED_THREADS, st, L, V, red, out);
+	launch_k(k_adv_step, red_grid(L.nel), RED_THREADS, st, L, geo, V, red, out);
 }
 
 void launch_conform_T(cudaStream_t st, const Lvl &L, double *T) { launch_k(k_conform_T, nblocks(L.nno), TPB, st, L, T); }
@@ -1839,8 +1899,8 @@ void launch_heat_flux(cudaStream_t st, const Lvl &L, const Geo *geo, const doubl
 {
 	// work holds nel element means then nno nodal fluxes
 	launch_k(k_hf_elem, nblocks(L.nel), TPB, st, L, geo, T, V, work);
-	launch_k(k_hf_node, nblocks(L.nno), TPB, st, L, work, work + L.nel);
-	launch_k(k_hf_surface, red_grid((long)L.elx * L.ely), RED_THREADS, st, L, work + L.nel, red, out);
+	launch_k(k_hf_node, nblocks(L.nno), TPB, st, L, geo, work, work + L.nel);
+	launch_k(k_hf_surface, red_grid((long)L.elx * L.ely), RED_THREADS, st, L, geo, work + L.nel, red, out);
 }
 
 void launch_vrms(cudaStream_t st, const Lvl &L, const Geo *geo, const double *V, Red red, double *out)

@@ -6,14 +6,30 @@
 
 #include "level.h"
 
-// Per-level constant geometry of a uniform box element (device resident).
+// Geometry of one element (device resident): one entry per level for the
+// box, one per (theta, r) column of elements for the sphere (cg_col).
 struct Geo
 {
-	double Mk[8][8][8][9];  // J * (dNa/dxj dNb/dxi + delta_ij grad Na . grad Nb) at Gauss point k: [k][a][b][3i+j]
-	double g[24];           // divergence operator of one element (get_elt_g, Cartesian)
-	double gnx[8][8][3];    // dN_a/dx_d at Gauss point k: [k][a][d]
+	double Mk[8][8][8][9];  // stiffness kernel at Gauss point k, [k][a][b][3i+j]: K_e = sum_k eta_k Mk[k] (get_elt_k);
+	                        // box: J (dNa/dxj dNb/dxi + delta_ij grad Na . grad Nb); sphere: |J| of the
+	                        // strain-rate form 2 (ba1 ba1 + ba2 ba2 + ba3 ba3) + ba4 ba4 + ba5 ba5 + ba6 ba6
+	double g[24];           // divergence operator of the element (get_elt_g)
+	double gnx[8][8][3];    // dN_a/dx_d at Gauss point k: [k][a][d]; sphere: d/dtheta, d/dphi, d/dr
 	double N[8][8];         // N_a at Gauss point k: [k][a]
+	double gda[8];          // |J| times the Gauss weight at Gauss point k (E->GDA)
+	double tww[8];          // integral of N_a over the element (E->TWW)
+	double size[3];         // element sizes (E->ECO.size)
+	double area;            // element volume (E->ECO.area)
+	double cr[8][8][3];     // [k][a][i]: radial unit vector at Gauss point k . basis vector i of node a (Cc(3, i, a, k));
+	                        // box: 1 for i = z, else 0
+	double rinv[8];         // 1/r at Gauss point k (box: 1)
+	double rsin[8];         // 1/(r sin theta) at Gauss point k (box: 1)
+	double wface[4];        // horizontal-average weights of the 4 nodes of the lower face (return_horiz_ave):
+	                        // integral of their bilinear shape functions over the face (box: hx hy / 4)
 };
+
+// geometry table entries of a level
+inline int geo_count(const Lvl &L) { return L.sphere ? L.elx * L.elz : 1; }
 
 // Deterministic reductions: fixed grid, per-block partials, last block sums
 // the partials in block order and writes `out[0..nv)`.
@@ -25,7 +41,9 @@ struct Red
 #define RED_MAX_BLOCKS 304
 #define RED_THREADS 256
 
+// fills the geo_count(L) entries of level L (host memory)
 void geo_fill_host(const Lvl &L, Geo *g);
+void geo_fill_sphere(const Lvl &L, Geo *g);  // geometry.cu
 
 // kernels issued by the launchers below since load (host-side count; a graph
 // capture counts its kernels once, each replay is added by the driver)
@@ -49,8 +67,10 @@ void launch_kmul_linesearch(cudaStream_t st, const Lvl &L, const T *K, const T *
 template <typename T> void launch_gs_colour(cudaStream_t st, const Lvl &L, const T *K, const T *BI, const T *F, T *d, int colour);
 template <typename T>
 void launch_gs_small(cudaStream_t st, const Lvl &L, const T *K, const T *BI, const T *F, T *d, int cycles, int zero_start);
-template <typename T> void launch_project(cudaStream_t st, const Lvl &Lf, const Lvl &Lc, const T *AU, T *AD);
-template <typename T> void launch_interp(cudaStream_t st, const Lvl &Lc, const Lvl &Lf, const T *AD, T *AU);
+// gc: geometry table of the coarse level (TWW)
+template <typename T> void launch_project(cudaStream_t st, const Lvl &Lf, const Lvl &Lc, const Geo *gc, const T *AU, T *AD);
+// gf: geometry table of the fine level (the sphere's element sizes)
+template <typename T> void launch_interp(cudaStream_t st, const Lvl &Lc, const Lvl &Lf, const Geo *gf, const T *AD, T *AU);
 template <typename T> void launch_vel_update(cudaStream_t st, int n, T *vel, const T *del, T *res, const T *AU, const double *alpha_num_den, int update_res);
 bool gs_small_fits(const Lvl &L, size_t word);
 // small FP32 levels: one CTA, vectors in shared memory, padded stencil Kt (63 float4 per node)
@@ -101,6 +121,7 @@ struct CoLevels
 	const float *BI[CO_MAX_LEV];
 	float *vec[CO_MAX_LEV][CO_NVEC];
 	int win[CO_MAX_LEV];  // ranks on either side of a node's owner that hold its neighbours
+	const Geo *geo[CO_MAX_LEV];  // geometry tables (TWW of the projection, sizes of the interpolation)
 	double *err;          // set to 1 if a wait of the cluster smoother timed out
 };
 // cluster size the device supports for the program (16 or 8); -1 if none
@@ -151,18 +172,18 @@ struct Rheo
 	double vmin, vmax;
 };
 void launch_visc_from_T(cudaStream_t st, const Lvl &L, const Geo *geo, const Rheo &r, const double *T, double *evi);
-void launch_project_viscosity(cudaStream_t st, const Lvl &Lf, const Lvl &Lc, const Geo *geoc, const double *evi_f,
-                              double *evi_c, double *work_f, double *work_c);
-void launch_buoyancy(cudaStream_t st, const Lvl &L, double Ra, const double *T, double *buoy);
+void launch_project_viscosity(cudaStream_t st, const Lvl &Lf, const Lvl &Lc, const Geo *geof, const Geo *geoc,
+                              const double *evi_f, double *evi_c, double *work_f, double *work_c);
+void launch_buoyancy(cudaStream_t st, const Lvl &L, const Geo *geo, double Ra, const double *T, double *buoy);
 void launch_forces(cudaStream_t st, const Lvl &L, const Geo *geo, const double *buoy, double *F);
 void launch_v_from_vector(cudaStream_t st, const Lvl &L, const double *U, double *V);
 void launch_pg_residual(cudaStream_t st, const Lvl &L, const Geo *geo, const double *T, const double *Tdot, const double *V,
                         double Q0, double *Eres);
-void launch_pg_gather(cudaStream_t st, const Lvl &L, const double *Eres, double *DTdot);
+void launch_pg_gather(cudaStream_t st, const Lvl &L, const Geo *geo, const double *Eres, double *DTdot);
 void launch_predictor(cudaStream_t st, const Lvl &L, double *T, double *Tdot, double dt, double gamma);
 void launch_corrector(cudaStream_t st, const Lvl &L, double *T, double *Tdot, const double *DTdot, double dt, double gamma);
 void launch_tmax(cudaStream_t st, int n, const double *T, Red red, double *out);
-void launch_adv_timestep(cudaStream_t st, const Lvl &L, const double *V, Red red, double *out_min_step);
+void launch_adv_timestep(cudaStream_t st, const Lvl &L, const Geo *geo, const double *V, Red red, double *out_min_step);
 void launch_conform_T(cudaStream_t st, const Lvl &L, double *T);
 void launch_heat_flux(cudaStream_t st, const Lvl &L, const Geo *geo, const double *T, const double *V, double *hf_work,
                       Red red, double *out_nut_nub);

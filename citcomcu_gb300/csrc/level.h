@@ -24,15 +24,24 @@ struct Lvl
 	int cnt[3][2];   // number of indices of parity p along axis (0 x, 1 y, 2 z)
 	int coff[9];     // colour offsets in colour-major order
 	int toff[9];     // first tile of each colour (tiles of CG_TILE positions, a colour's last one partial)
-	double h[3];     // element edge lengths (uniform per axis)
-	double J;        // Jacobian determinant hx*hy*hz/8
+	double h[3];     // element edge lengths (uniform per axis); in the sphere dtheta, dphi (radians), dr
+	double J;        // Jacobian determinant hx*hy*hz/8 (box only)
+	int sphere;      // 1: regional spherical shell segment, x, y, z = theta, phi, r (Geometry=Rsphere)
+	double org[3];   // coordinates of node (0, 0, 0): 0, 0, 0 in the box; theta_north, phi_west (radians), r_inner
 };
+
 
 #ifdef __CUDACC__
 #define CG_HD __host__ __device__ __forceinline__
 #else
 #define CG_HD inline
 #endif
+
+// Element geometry is the same for every element of the box, and for every
+// element of one (theta, r) column of the sphere (the segment is invariant
+// under rotation about the polar axis by multiples of dphi): index of the
+// geometry table entry of element (ex, ., ez)
+CG_HD int cg_col(const Lvl &L, int ex, int ez) { return L.sphere ? ex * L.elz + ez : 0; }
 
 CG_HD int cg_colour(int x, int y, int z) { return (z & 1) | ((x & 1) << 1) | ((y & 1) << 2); }
 

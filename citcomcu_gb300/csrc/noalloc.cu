@@ -30,9 +30,9 @@ constexpr int RED_WORDS = RED_MAX_BLOCKS * 8;
 // layout (in doubles): geometry | reduction partials | counter + result | element means | nodal fluxes
 constexpr long OFF_GEO = 0;
 constexpr long OFF_RED = ((OFF_GEO + GEO_WORDS + 31) / 32) * 32;
-constexpr long OFF_CTR = OFF_RED + RED_WORDS;  // one word for the counter, two for (Nut, Nub) sums
-constexpr long OFF_OUT = OFF_CTR + 4;
-constexpr long OFF_WORK = ((OFF_OUT + 2 + 31) / 32) * 32;
+constexpr long OFF_CTR = OFF_RED + RED_WORDS;  // one word for the counter
+constexpr long OFF_OUT = OFF_CTR + 4;           // top and bottom flux sums, top and bottom weights
+constexpr long OFF_WORK = ((OFF_OUT + 4 + 31) / 32) * 32;
 constexpr long SCRATCH_WORDS = OFF_WORK + CITCOM_GPU_NOALLOC_MAX_ELEMENTS + CITCOM_GPU_NOALLOC_MAX_NODES;
 constexpr int MAX_DEVICES = 64;
 
@@ -139,7 +139,7 @@ extern "C" int citcom_gpu_heat_flux_noalloc(int nox, int noy, int noz, const dou
 		launch_heat_flux(st, L, dgeo, dT, dV, work, red, dout);
 		e = cudaGetLastError();
 	}
-	double sums[2] = {0.0, 0.0};
+	double sums[4] = {0.0, 0.0, 0.0, 0.0};
 	if(e == cudaSuccess)
 		e = cudaMemcpyAsync(sums, dout, sizeof(sums), cudaMemcpyDeviceToHost, st);
 	if(e == cudaSuccess)
@@ -149,10 +149,9 @@ extern "C" int citcom_gpu_heat_flux_noalloc(int nox, int noy, int noz, const dou
 		fprintf(stderr, "citcom_gpu_heat_flux_noalloc: %s\n", cudaGetErrorString(e));
 		return CITCOM_GPU_ERR_CUDA;
 	}
-	const double ns = 4.0 * (double)L.elx * (double)L.ely;
 	if(nut)
-		*nut = sums[0] / ns;
+		*nut = sums[0] / (4.0 * sums[2]);
 	if(nub)
-		*nub = sums[1] / ns;
+		*nub = sums[1] / (4.0 * sums[3]);
 	return CITCOM_GPU_OK;
 }

@@ -73,6 +73,12 @@ typedef struct citcom_gpu_config
 	double finetunedt, fixed_timestep;
 	/* CITCOM_GPU_FP64 or CITCOM_GPU_MIXED */
 	int precision;
+	/* Geometry=Rsphere (control.Rsphere): a regional spherical shell segment
+	 * with x, y, z = theta, phi, r; theta_north/south and fi_west/east in
+	 * degrees, radius_inner/outer (sphere.ti, to, fi, fo, ri, ro); dimen is
+	 * then unused.  0: the Cartesian box (Geometry=cart3d). */
+	int sphere;
+	double theta[2], fi[2], radius[2];
 } citcom_gpu_config;
 
 /* Time-step bookkeeping that PG_timestep updates in E->advection / E->monitor. */

@@ -53,6 +53,10 @@ class Case:
     finetunedt: float = 0.75
     fixed_timestep: float = 0.0
     maxstep: int = 10
+    # regional spherical shell segment (Geometry=Rsphere): theta_north,
+    # theta_south, fi_west, fi_east in degrees, radius_inner, radius_outer;
+    # None is the Cartesian box.  x, y, z of the mesh are then theta, phi, r.
+    sphere: Optional[tuple] = None
 
     @property
     def nox(self):
@@ -98,11 +102,7 @@ def make_deck(c: Case, datafile: str) -> str:
         f"nodex={c.nox} nodez={c.noz} nodey={c.noy}",
         f"mgunitx={c.mgunit[0]}", f"mgunitz={c.mgunit[2]}", f"mgunity={c.mgunit[1]}",
         f"levels={c.levels}",
-        "Geometry=cart3d",
-        f"dimenx={c.dimen[0]!r}", f"dimenz={c.dimen[2]!r}", f"dimeny={c.dimen[1]!r}",
-        "z_grid_layers=2", f"zz=0.0,{c.dimen[2]!r}", f"nz=1,{c.noz}",
-        "x_grid_layers=2", f"xx=0.0,{c.dimen[0]!r}", f"nx=1,{c.nox}",
-        "y_grid_layers=2", f"yy=0.0,{c.dimen[1]!r}", f"ny=1,{c.noy}",
+    ] + (_geometry_cart(c) if c.sphere is None else _geometry_sphere(c)) + [
         "z_lmantle=0.76655052", "z_410=0.857143", "z_lith=0.9651568",
         "rheol=3",
         f"TDEPV={'on' if c.tdepv else 'off'}",
@@ -140,11 +140,32 @@ def make_deck(c: Case, datafile: str) -> str:
         "ll_max=20", "nlong=180", "nlati=90",
         "DESCRIBE=off", "BEGINNER=off", "VERBOSE=off", "verbose=off", "see_convergence=1",
     ]
-    # Viscosity_structures.c:120-135 wants num_mat values of z_layer (material
-    # l+1 where the element centroid z >= z_layer[l], scanned top down)
+    # Viscosity_structures.c:120-135 wants num_mat values of z_layer (r_layer
+    # in the sphere): material l+1 where the element centroid z (r) >=
+    # z_layer[l], scanned top down
     zl = list(c.z_layer) + [0.0] * (nm - len(c.z_layer))
-    lines.append(f"z_layer={_vec(zl)}")
+    lines.append(f"{'z' if c.sphere is None else 'r'}_layer={_vec(zl)}")
     return "\n".join(lines) + "\n"
+
+
+def _geometry_cart(c: Case) -> List[str]:
+    return ["Geometry=cart3d",
+            f"dimenx={c.dimen[0]!r}", f"dimenz={c.dimen[2]!r}", f"dimeny={c.dimen[1]!r}",
+            "z_grid_layers=2", f"zz=0.0,{c.dimen[2]!r}", f"nz=1,{c.noz}",
+            "x_grid_layers=2", f"xx=0.0,{c.dimen[0]!r}", f"nx=1,{c.nox}",
+            "y_grid_layers=2", f"yy=0.0,{c.dimen[1]!r}", f"ny=1,{c.noy}"]
+
+
+def _geometry_sphere(c: Case) -> List[str]:
+    # Instructions.c:1018-1029 (corners), Nodal_mesh.c:87-133 (t/f/r grid layers)
+    tn, ts, fw, fe, ri, ro = c.sphere
+    return ["Geometry=Rsphere",
+            f"theta_north={tn!r}", f"theta_south={ts!r}", f"fi_west={fw!r}", f"fi_east={fe!r}",
+            f"radius_inner={ri!r}", f"radius_outer={ro!r}",
+            "r_grid_layers=2", f"rr={ri!r},{ro!r}", f"nr=1,{c.noz}",
+            "t_grid_layers=2", f"tt={tn!r},{ts!r}", f"nt=1,{c.nox}",
+            "f_grid_layers=2", f"ff={fw!r},{fe!r}", f"nf=1,{c.noy}",
+            "r_lmantle=0.7", "r_410=0.9", "r_lith=0.98"]
 
 
 def conductive_T0(c: Case, amp: float = 0.01, seed: int = 0):

@@ -12,6 +12,11 @@ Fixtures
   cfg1_16.npz      16^3 elements, 3 levels, isoviscous, Ra 1e4, the deck's own
                    sinusoidal IC, accuracy 1e-6, 5 steps (FP64-promoted build;
                    per-step scalars from the stock float build alongside).
+  sphere_tdep.npz  Geometry=Rsphere: theta 45-135 deg, phi 0-90 deg, r 0.55-1.0,
+                   9x13x9 nodes (mgunit 2,3,2; 3 levels), eta = exp(ln(100)
+                   (0 - T)), Ra 1e4, seeded T0 (1 - (r - ri)/(ro - ri) plus
+                   noise), accuracy 1e-8.  Operator probes on every level plus
+                   3 time steps (FP64-promoted build).
 """
 from __future__ import annotations
 
@@ -33,6 +38,12 @@ def small_case() -> Case:
     return Case(name="small_tdep", mgunit=(2, 3, 2), levels=3, dimen=(1.0, 1.5, 1.0),
                 rayleigh=1e4, tdepv=True, visc0=(1.0,), viscE=(4.605170185988092,), viscT=(0.0,),
                 accuracy=1e-8, maxstep=3)
+
+
+def sphere_case() -> Case:
+    return Case(name="sphere_tdep", mgunit=(2, 3, 2), levels=3, rayleigh=1e4, tdepv=True, visc0=(1.0,),
+                viscE=(4.605170185988092,), viscT=(0.0,), accuracy=1e-8, maxstep=3,
+                sphere=(45.0, 135.0, 0.0, 90.0, 0.55, 1.0))
 
 
 def cfg1_case() -> Case:
@@ -64,6 +75,15 @@ def main():
         keep["T0_input"] = T0
         np.savez_compressed(os.path.join(HERE, "small_tdep.npz"), **keep)
 
+        c = sphere_case()
+        T0 = conductive_T0(c, amp=0.01, seed=0)
+        R = run_reference(c, os.path.join(tmp, "sphere"), nsteps=3, T0=T0, probe=True)
+        keep = {k: v for k, v in R.items() if not k.startswith("s") and not k.startswith("gs")}
+        keep.update(_steps(R, 3))
+        keep["s0_F"] = R["s0_F"]
+        keep["T0_input"] = T0
+        np.savez_compressed(os.path.join(HERE, "sphere_tdep.npz"), **keep)
+
         c = cfg1_case()
         R = run_reference(c, os.path.join(tmp, "cfg1"), nsteps=5)
         R32 = run_reference(c, os.path.join(tmp, "cfg1_32"), nsteps=5, precision="f32")
@@ -74,7 +94,7 @@ def main():
         for k in ("T", "V1", "V2", "V3", "P"):
             keep[f"s5_{k}"] = R[f"s5_{k}"]
         np.savez_compressed(os.path.join(HERE, "cfg1_16.npz"), **keep)
-    for f in ("small_tdep.npz", "cfg1_16.npz"):
+    for f in ("small_tdep.npz", "cfg1_16.npz", "sphere_tdep.npz"):
         print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")
 
 
