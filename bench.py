@@ -59,6 +59,30 @@ def workload(size: int):
                   viscE=(math.log(1e3),), viscT=(0.0,), accuracy=1e-6, piterations=375)
 
 
+def sphere_workload():
+    """Regional spherical shell segment: colatitude 45-135 deg, longitude
+    0-90 deg, radius 0.55-1.0, 192 x 192 x 96 elements, 6 multigrid levels,
+    eta = exp(-ln(1e5) T) times 30 below r = 0.9, Ra 1e7."""
+    from citcomcu_gb300 import Config
+    return Config(mgunit=(6, 6, 3), levels=6, rayleigh=1e7, tdepv=True, visc0=(1.0, 30.0),
+                  viscE=(math.log(1e5), math.log(1e5)), viscT=(0.0, 0.0), z_layer=(0.9,), accuracy=1e-6,
+                  piterations=375, sphere=(45.0, 135.0, 0.0, 90.0, 0.55, 1.0))
+
+
+def seeded_T0_sphere(case, seed: int = 0):
+    """Conductive shell profile T = (1/r - 1/ro) / (1/ri - 1/ro) plus seeded
+    uniform noise of +-0.01 on the interior (numpy PCG64)."""
+    ri, ro = case.sphere[4], case.sphere[5]
+    rng = np.random.Generator(np.random.PCG64(seed))
+    r = np.linspace(ri, ro, case.noz)
+    T = np.empty((case.noy, case.nox, case.noz))
+    T[:] = (1.0 / r - 1.0 / ro) / (1.0 / ri - 1.0 / ro)
+    T += rng.uniform(-0.01, 0.01, size=T.shape)
+    T[:, :, 0] = 1.0
+    T[:, :, -1] = 0.0
+    return T.reshape(-1)
+
+
 def seeded_T0(case, seed: int = 0):
     rng = np.random.Generator(np.random.PCG64(seed))
     z = np.linspace(0.0, case.dimen[2], case.noz)
@@ -303,6 +327,46 @@ def reference_arm(args):
     return 0
 
 
+def sphere_arm(args):
+    """The regional spherical segment (not the headline): cold solves of the
+    seeded state with the FP32 multigrid + FP64 refinement path."""
+    import torch
+    import citcomcu_gb300 as cg
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    cg.build()
+    case = sphere_workload()
+    case.piterations = args.piterations
+    T0 = seeded_T0_sphere(case)
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        recs, launches, res, nu, vr, energy_ms = run_mode(cg, case, cg.MIXED, T0, args.steps, args.warmup)
+    ms = float(np.mean([r["stokes_ms"] for r in recs]))
+    sweeps = sum(r["smoother_sweeps"] for r in recs)
+    sm_ms = sum(r["smoother_ms"] for r in recs)
+    per_launch_s = sm_ms * 1e-3 / max(8 * sweeps, 1)
+    per_launch_bytes = bytes_per_sweep(case.nno, 4) / 8.0
+    peak, peak_kind = peaks()
+    achieved = per_launch_bytes / per_launch_s / 1e9 if per_launch_s > 0 else None
+    line = {"metric": METRIC, "value": ms, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms + float(energy_ms), "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": "regional spherical shell segment, colatitude 45-135 deg, longitude 0-90 deg, r 0.55-1.0, "
+                                   f"{case.nox - 1}x{case.noy - 1}x{case.noz - 1} Q1 elements, {case.levels} multigrid levels, "
+                                   "eta=exp(-ln(1e5) T) x30 below r=0.9, Ra=1e7, conductive T0 + U(-0.01,0.01) seed 0, "
+                                   f"accuracy 1e-6, piterations {case.piterations}",
+                       "mode": "FP32 multigrid + FP64 refinement",
+                       "step": "cold Stokes solve of the seeded initial state (general_stokes_solver)"},
+            "uzawa_iterations": [r["uzawa"] for r in recs], "mg_passes": [r["mg_passes"] for r in recs],
+            "ms_per_mg_pass": ms / max(np.mean([r["mg_passes"] for r in recs]), 1),
+            "residuals_final": res, "nu_top": nu[0], "nu_bot": nu[1], "vrms": vr, "energy_ms": energy_ms,
+            "roofline": {"bound": "hbm", "kernel": "k_tile<float, 0> (finest-level Gauss-Seidel colour)",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": (achieved / peak) if achieved else None, "traffic": None, "peak_kind": peak_kind,
+                         "bytes_per_launch": per_launch_bytes, "launch_us": per_launch_s * 1e6},
+            "clocks": clk.summary(), "gpu_launches": int(launches)}
+    print(json.dumps(line))
+    return 0
+
+
 def workload_name(case):
     return (f"{case.nox - 1}^3 Q1 elements, {case.levels} multigrid levels, eta=exp(-ln(1e3) T), Ra=1e5, free slip, "
             f"T0=1-z+U(-0.01,0.01) seed 0, accuracy 1e-6, piterations 375")
@@ -324,11 +388,15 @@ def main():
     ap.add_argument("--learn-seeds", type=int, default=10)
     ap.add_argument("--learn-steps", type=int, default=4, help="time steps recorded after each seed's cold solve")
     ap.add_argument("--learn-adam", type=int, default=1000, help="Adam steps of the online training")
+    ap.add_argument("--workload", default="cube", choices=["cube", "sphere"],
+                    help="sphere: the 192x192x96 regional spherical segment instead of the headline box")
     ap.add_argument("--piterations", type=int, default=375,
                     help="Uzawa iteration cap; lower values only for short profiling runs")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
+    if args.workload == "sphere":
+        return sphere_arm(args)
 
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))
