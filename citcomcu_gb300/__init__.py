@@ -66,6 +66,15 @@ class Config:
     # (radius_inner, radius_outer); x, y, z of the mesh are then theta, phi, r
     # and dimen is unused.  None: the Cartesian box.
     sphere: Optional[tuple] = None
+    # stress-dependent viscosity (SDEPV) and the viscosity iteration of
+    # general_stokes_solver; sdepv_expt / sdepv_trns per material
+    sdepv: bool = False
+    sdepv_rheology: int = 2
+    sdepv_expt: tuple = (3.0,)
+    sdepv_trns: tuple = (1.0,)
+    sdepv_misfit: float = 0.001
+    max_sdep_visc_iter: int = 50
+    sdepv_iter_damp: float = 1.0
 
     @property
     def nox(self):
@@ -126,6 +135,13 @@ class _CConfig(ctypes.Structure):
         ("theta", ctypes.c_double * 2),
         ("fi", ctypes.c_double * 2),
         ("radius", ctypes.c_double * 2),
+        ("sdepv", ctypes.c_int),
+        ("sdepv_rheology", ctypes.c_int),
+        ("sdepv_expt", ctypes.c_double * 8),
+        ("sdepv_trns", ctypes.c_double * 8),
+        ("sdepv_misfit", ctypes.c_double),
+        ("sdepv_iter_damp", ctypes.c_double),
+        ("max_sdep_visc_iter", ctypes.c_int),
     ]
 
 
@@ -138,7 +154,8 @@ class _CStats(ctypes.Structure):
     _fields_ = [("uzawa_iterations", ctypes.c_int), ("del2_calls", ctypes.c_int), ("mg_passes", ctypes.c_int),
                 ("initial_residual", ctypes.c_double), ("stokes_ms", ctypes.c_double), ("energy_ms", ctypes.c_double),
                 ("smoother_ms", ctypes.c_double), ("smoother_sweeps", ctypes.c_int),
-                ("kernel_launches", ctypes.c_ulonglong), ("warm_start", ctypes.c_int),
+                ("kernel_launches", ctypes.c_ulonglong), ("visc_iterations", ctypes.c_int),
+                ("visc_misfit", ctypes.c_double), ("warm_start", ctypes.c_int),
                 ("warm_residual", ctypes.c_double), ("base_residual", ctypes.c_double)]
 
 
@@ -289,6 +306,14 @@ class Solver:
         c.finetunedt = cfg.finetunedt
         c.fixed_timestep = cfg.fixed_timestep
         c.precision = cfg.precision
+        c.sdepv = int(cfg.sdepv)
+        c.sdepv_rheology = cfg.sdepv_rheology
+        for i in range(8):
+            c.sdepv_expt[i] = cfg.sdepv_expt[min(i, len(cfg.sdepv_expt) - 1)]
+            c.sdepv_trns[i] = cfg.sdepv_trns[min(i, len(cfg.sdepv_trns) - 1)]
+        c.sdepv_misfit = cfg.sdepv_misfit
+        c.sdepv_iter_damp = cfg.sdepv_iter_damp
+        c.max_sdep_visc_iter = cfg.max_sdep_visc_iter
         if cfg.sphere is not None:
             tn, ts, fw, fe, ri, ro = cfg.sphere
             c.sphere = 1
@@ -334,7 +359,8 @@ class Solver:
         return dict(uzawa=s.uzawa_iterations, del2_calls=s.del2_calls, mg_passes=s.mg_passes,
                     initial_residual=s.initial_residual, stokes_ms=s.stokes_ms, energy_ms=s.energy_ms,
                     smoother_ms=s.smoother_ms, smoother_sweeps=s.smoother_sweeps, kernel_launches=s.kernel_launches,
-                    warm_start=s.warm_start, warm_residual=s.warm_residual, base_residual=s.base_residual)
+                    warm_start=s.warm_start, warm_residual=s.warm_residual, base_residual=s.base_residual,
+                    visc_iterations=s.visc_iterations, visc_misfit=s.visc_misfit)
 
     def stokes_residuals(self):
         """(|F - K U - G P| / |F|, |div U| / (|U| sqrt(npno/neq))) of the resident solution."""

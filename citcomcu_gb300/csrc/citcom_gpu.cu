@@ -102,6 +102,9 @@ struct citcom_gpu
 	std::vector<void *> allocs;
 	citcom_nn *warm;   // warm-start network attached to the Stokes solve (not owned), or null
 	double diff_ts;    // diffusive time-step limit of the finest level
+	double *oldU;      // the previous viscosity iteration's U (general_stokes_solver's oldU, kept across solves)
+	double *edot;      // strain-rate invariant per fine element
+	int sdepv_visits;  // calls of visc_from_S so far (the first one takes a unit strain rate)
 	char err[512];
 };
 
@@ -235,6 +238,13 @@ Rheo rheo_of(const citcom_gpu_config &c)
 	r.vmax_on = c.vmax_on;
 	r.vmin = c.vmin;
 	r.vmax = c.vmax;
+	r.sdepv = c.sdepv;
+	r.sdepv_rheology = c.sdepv_rheology;
+	for(int i = 0; i < 8; ++i)
+	{
+		r.sdepv_expt[i] = c.sdepv_expt[i];
+		r.sdepv_trns[i] = c.sdepv_trns[i];
+	}
 	return r;
 }
 
@@ -706,10 +716,26 @@ int project_viscosity(citcom_gpu *h)
 	return CITCOM_GPU_OK;
 }
 
+// get_system_viscosity (Viscosity_structures.c:369-455) on the resident T
+// (and, with stress dependence, the resident V), then project_viscosity
 int viscosity_from_device_T(citcom_gpu *h)
 {
 	const int lmax = h->L - 1;
-	launch_visc_from_T(h->st, h->lv[lmax], h->geo[lmax], rheo_of(h->cfg), h->T, h->evi[lmax]);
+	const Lvl &Lf = h->lv[lmax];
+	const Rheo r = rheo_of(h->cfg);
+	launch_visc_from_T(h->st, Lf, h->geo[lmax], r, h->T, h->evi[lmax]);
+	if(h->cfg.sdepv)
+	{
+		// the first call of visc_from_S takes a unit strain rate (:787-790)
+		const double *ed = nullptr;
+		if(h->sdepv_visits > 0)
+		{
+			launch_strain_rate(h->st, Lf, h->geo[lmax], h->V, h->edot);
+			ed = h->edot;
+		}
+		launch_visc_from_S(h->st, Lf, h->geo[lmax], r, h->T, ed, h->evi[lmax]);
+		h->sdepv_visits++;
+	}
 	return project_viscosity(h);
 }
 
@@ -734,14 +760,42 @@ int stokes_resident(citcom_gpu *h)
 	h->stats.smoother_sweeps = 0;
 	launch_strip(h->st, Lf, h->U);  // velocities_conform_bcs with VB = 0
 	TRY(forces_from_device_T(h));
-	if(h->cfg.tdepv || !h->visc_ready)
-		TRY(viscosity_from_device_T(h));
-	if(h->cfg.tdepv || !h->stiffness_ready)
-		TRY(construct_stiffness(h));
-	int steps = h->cfg.piterations;
-	double r0;
-	TRY(uzawa(h, h->U, h->P, h->F, h->cfg.accuracy, &steps, &r0));
-	launch_v_from_vector(h->st, Lf, h->U, h->V);
+	// the viscosity iteration of stress-dependent rheologies (Drive_solvers.c:
+	// 120-159): viscosity from T and the last V, operator, solve, damped
+	// update, until |dU| / |U| <= sdepv_misfit or max_sdep_visc_iter
+	const bool iterate = h->cfg.sdepv != 0;
+	const bool update = h->cfg.tdepv || iterate;
+	int vcount = 0, uzawa_total = 0;
+	double misfit = 0.0;
+	do
+	{
+		if(update || !h->visc_ready)
+			TRY(viscosity_from_device_T(h));
+		if(update || !h->stiffness_ready)
+			TRY(construct_stiffness(h));
+		int steps = h->cfg.piterations;
+		double r0;
+		TRY(uzawa(h, h->U, h->P, h->F, h->cfg.accuracy, &steps, &r0));
+		uzawa_total += steps;
+		launch_v_from_vector(h->st, Lf, h->U, h->V);
+		++vcount;
+		if(iterate)
+		{
+			const double alpha = h->cfg.sdepv_iter_damp;
+			if(std::fabs(alpha - 1.0) > 1e-7)
+				launch_lin2(h->st, Lf.neq, h->U, alpha, h->U, 1.0 - alpha, h->oldU);
+			launch_lin2(h->st, Lf.neq, h->r64, 1.0, h->U, -1.0, h->oldU);  // delta_U
+			CK(cudaMemcpyAsync(h->oldU, h->U, sizeof(double) * Lf.neq, cudaMemcpyDeviceToDevice, h->st));
+			launch_dots4(h->st, Lf.neq, h->U, h->U, h->r64, h->r64, nullptr, nullptr, nullptr, nullptr, red_of(h),
+			             h->dscal + S_DOT);
+			TRY(readback(h, S_DOT, 2));
+			const double uu = std::sqrt(h->hscal[S_DOT]), dd = std::sqrt(h->hscal[S_DOT + 1]);
+			misfit = uu != 0.0 ? dd / uu : dd;
+		}
+	} while(iterate && misfit > h->cfg.sdepv_misfit && vcount < h->cfg.max_sdep_visc_iter);
+	h->stats.uzawa_iterations = uzawa_total;
+	h->stats.visc_iterations = vcount;
+	h->stats.visc_misfit = misfit;
 	CK(cudaEventRecord(h->ev1, h->st));
 	CK(cudaEventSynchronize(h->ev1));
 	float ms = 0.f;
@@ -1033,6 +1087,8 @@ int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 		TRYC(dalloc(h, &h->Ah, Lf.neq + 2));
 		TRYC(dalloc(h, &h->u1, Lf.neq + 2));
 		TRYC(dalloc(h, &h->r64, Lf.neq + 2));
+		TRYC(dalloc(h, &h->oldU, Lf.neq + 2));
+		TRYC(dalloc(h, &h->edot, Lf.nel));
 		TRYC(dalloc(h, &h->Eres, (size_t)8 * Lf.nel));
 		TRYC(dalloc(h, &h->DTdot, Lf.nno));
 		TRYC(dalloc(h, &h->T1, Lf.nno));

@@ -217,6 +217,11 @@ void fill_column(const Lvl &L, int ex, int ez, Geo *G)
 		point(X, SA, xi, P);
 		const double temp = 8.0 * P.jac;
 		const double ra = P.rinv, si = 1.0 / sin(P.theta), ct = cos(P.theta) * si;
+		G->rinvc = P.rinv;
+		G->thetac = P.theta;
+		for(int a = 0; a < 8; ++a)
+			for(int d = 0; d < 3; ++d)
+				G->gnxc[a][d] = P.gnx[a][d];
 		for(int a = 0; a < 8; ++a)
 		{
 			const double n = shp(a, xi);

@@ -973,6 +973,125 @@ __global__ void k_visc_from_T(Lvl L, const Geo *__restrict__ geo, Rheo r, const 
 		}
 		else
 			v = r.visc0[m];
+		if(!r.sdepv)
+		{
+			if(r.vmax_on && v > r.vmax)
+				v = r.vmax;
+			if(r.vmin_on && v < r.vmin)
+				v = r.vmin;
+		}
+		evi[8 * e + k] = v;
+	}
+}
+
+// strain_rate_2_inv (Viscosity_structures.c:979-1086) at the element centre,
+// SQRT form: sqrt(0.5 sum of e_ij e_ij).  The spherical branch forms its
+// tensor from the velocity gradient in (theta, phi, r) as the reference does
+// (diagonal 2 d_ii, off-diagonal d_ij + d_ji).
+__global__ void k_strain_rate(Lvl L, const Geo *__restrict__ geo, const double *__restrict__ V, double *__restrict__ edot)
+{
+	pdl_begin();
+	const int e = blockIdx.x * blockDim.x + threadIdx.x;
+	if(e >= L.nel)
+		return;
+	const int ez = e % L.elz, ex = (e / L.elz) % L.elx, ey = e / (L.elz * L.elx);
+	const Geo *G = geo + cg_col(L, ex, ez);
+	double vv[8][3];
+	for(int a = 0; a < 8; ++a)
+	{
+		const int n = cg_node(L, ex + cg_loc(a, 0), ey + cg_loc(a, 1), ez + cg_loc(a, 2));
+		for(int d = 0; d < 3; ++d)
+			vv[a][d] = V[(size_t)d * L.nno + n];
+	}
+	double e11, e22, e33, e12, e13, e23;
+	if(!L.sphere)
+	{
+		double du[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+		for(int a = 0; a < 8; ++a)
+			for(int p = 0; p < 3; ++p)
+				for(int q = 0; q < 3; ++q)
+					du[p][q] += vv[a][p] * G->gnxc[a][q];
+		e11 = du[0][0];
+		e22 = du[1][1];
+		e33 = du[2][2];
+		e12 = 0.5 * (du[0][1] + du[1][0]);
+		e13 = 0.5 * (du[0][2] + du[2][0]);
+		e23 = 0.5 * (du[1][2] + du[2][1]);
+	}
+	else
+	{
+		const double ra = G->rinvc, st = sin(G->thetac), ct = cos(G->thetac), n = 0.125;
+		double x1 = 0, x2 = 0, x3 = 0, x4 = 0, x5 = 0, x6 = 0;
+		for(int a = 0; a < 8; ++a)
+		{
+			const double v1 = vv[a][0], v2 = vv[a][1], v3 = vv[a][2];
+			const double g0 = G->gnxc[a][0], g1 = G->gnxc[a][1], g2 = G->gnxc[a][2];
+			x1 += (v1 * g0 + v3 * n) * ra;
+			x2 += ((v2 * g1 + v1 * n * ct) / st + v3 * n) * ra;
+			x3 += v3 * g2;
+			x4 += ((v1 * g1 - v2 * n * ct) / st + v2 * g0) * ra;
+			x5 += v1 * g2 + ra * (v3 * g0 - v1 * n);
+			x6 += v2 * g2 + ra * (v3 * g1 / st - v2 * n);
+		}
+		e11 = 2.0 * x1;
+		e22 = 2.0 * x2;
+		e33 = 2.0 * x3;
+		e12 = x4;
+		e13 = x5;
+		e23 = x6;
+	}
+	const double s = e11 * e11 + e12 * e12 * 2.0 + e22 * e22 + e23 * e23 * 2.0 + e33 * e33 + e13 * e13 * 2.0;
+	edot[e] = sqrt(0.5 * s);
+}
+
+// visc_from_S (Viscosity_structures.c:744-846), rheology 1 (eta <- 2 eta /
+// (1 + s eta^(1-1/n))) or 2 (eta <- eta / (1 + s eta^(1-1/n)) below the
+// transition temperature; without composition), s = (2 edot / trns)^(1-1/n)
+// of the element's material; then VMAX/VMIN (:414-427).  edot null: 1.
+__global__ void k_visc_from_S(Lvl L, const Geo *__restrict__ geo, Rheo r, const double *__restrict__ T,
+                              const double *__restrict__ edot, double *__restrict__ evi)
+{
+	pdl_begin();
+	const int e = blockIdx.x * blockDim.x + threadIdx.x;
+	if(e >= L.nel)
+		return;
+	const int ez = e % L.elz, ex = (e / L.elz) % L.elx, ey = e / (L.elz * L.elx);
+	const Geo *G = geo + cg_col(L, ex, ez);
+	const double zc = L.org[2] + ((double)ez + 0.5) * L.h[2];
+	int layer = 0;
+	for(int i = 0; i < r.num_mat - 1; ++i)
+		if(zc >= r.z_layer[i])
+		{
+			layer = i + 1;
+			break;
+		}
+	if(!layer)
+		layer = r.num_mat;
+	const int m = layer - 1;
+	const double ed = edot ? edot[e] : 1.0;
+	const double e1 = 1.0 - 1.0 / r.sdepv_expt[m];
+	const double scale = pow(2.0 * ed / r.sdepv_trns[m], e1);
+	double TT[8];
+	for(int a = 0; a < 8; ++a)
+	{
+		const double t = T[cg_node(L, ex + cg_loc(a, 0), ey + cg_loc(a, 1), ez + cg_loc(a, 2))];
+		TT[a] = t > 0.0 ? t : 0.0;
+	}
+	for(int k = 0; k < 8; ++k)
+	{
+		double v = evi[8 * e + k];
+		if(r.sdepv_rheology == 1)
+			v = 2.0 * v / (1.0 + scale * pow(v, e1));
+		else
+		{
+			double t = 0.0;
+			for(int a = 0; a < 8; ++a)
+				t += TT[a] * G->N[k][a];
+			// the transition temperature (3000) and composition (2) of the
+			// reference's defaults: the non-dimensional T and C = 0 are below
+			if(t < 3000.0)
+				v = v / (1.0 + scale * pow(v, e1));
+		}
 		if(r.vmax_on && v > r.vmax)
 			v = r.vmax;
 		if(r.vmin_on && v < r.vmin)
@@ -1605,6 +1724,11 @@ void geo_fill_host(const Lvl &L, Geo *g)
 	g->area = 8.0 * L.J;
 	for(int i = 0; i < 4; ++i)
 		g->wface[i] = L.h[0] * L.h[1] / 4.0;
+	for(int a = 0; a < 8; ++a)
+		for(int d = 0; d < 3; ++d)
+			g->gnxc[a][d] = gnxc[a][d];
+	g->rinvc = 1.0;
+	g->thetac = 0.0;
 }
 
 void launch_assemble(cudaStream_t st, const Lvl &L, const Geo *geo, const double *evi, int aug, double lambda, double *K64,
@@ -1834,6 +1958,17 @@ void launch_residual64(cudaStream_t st, const Lvl &L, const double *K, const dou
 void launch_visc_from_T(cudaStream_t st, const Lvl &L, const Geo *geo, const Rheo &r, const double *T, double *evi)
 {
 	launch_k(k_visc_from_T, nblocks(L.nel), TPB, st, L, geo, r, T, evi);
+}
+
+void launch_strain_rate(cudaStream_t st, const Lvl &L, const Geo *geo, const double *V, double *edot)
+{
+	launch_k(k_strain_rate, nblocks(L.nel), TPB, st, L, geo, V, edot);
+}
+
+void launch_visc_from_S(cudaStream_t st, const Lvl &L, const Geo *geo, const Rheo &r, const double *T, const double *edot,
+                        double *evi)
+{
+	launch_k(k_visc_from_S, nblocks(L.nel), TPB, st, L, geo, r, T, edot, evi);
 }
 
 void launch_project_viscosity(cudaStream_t st, const Lvl &Lf, const Lvl &Lc, const Geo *geof, const Geo *geoc, const double *evi_f,

@@ -26,6 +26,8 @@ struct Geo
 	double rsin[8];         // 1/(r sin theta) at Gauss point k (box: 1)
 	double wface[4];        // horizontal-average weights of the 4 nodes of the lower face (return_horiz_ave):
 	                        // integral of their bilinear shape functions over the face (box: hx hy / 4)
+	double gnxc[8][3];      // dN_a/dx_d at the element centre (the pressure point)
+	double rinvc, thetac;   // 1/r and theta at the element centre (sphere)
 };
 
 // geometry table entries of a level
@@ -170,8 +172,15 @@ struct Rheo
 	double visc0[8], viscE[8], viscT[8], z_layer[8];
 	int vmin_on, vmax_on;
 	double vmin, vmax;
+	int sdepv, sdepv_rheology;      // with sdepv the VMIN/VMAX clamps follow visc_from_S
+	double sdepv_expt[8], sdepv_trns[8];
 };
 void launch_visc_from_T(cudaStream_t st, const Lvl &L, const Geo *geo, const Rheo &r, const double *T, double *evi);
+// strain_rate_2_inv (Viscosity_structures.c:979-1086), SQRT form, at the element centres
+void launch_strain_rate(cudaStream_t st, const Lvl &L, const Geo *geo, const double *V, double *edot);
+// visc_from_S, rheology 1 or 2 (Viscosity_structures.c:744-846), then VMAX/VMIN; edot null: 1 everywhere
+void launch_visc_from_S(cudaStream_t st, const Lvl &L, const Geo *geo, const Rheo &r, const double *T, const double *edot,
+                        double *evi);
 void launch_project_viscosity(cudaStream_t st, const Lvl &Lf, const Lvl &Lc, const Geo *geof, const Geo *geoc,
                               const double *evi_f, double *evi_c, double *work_f, double *work_c);
 void launch_buoyancy(cudaStream_t st, const Lvl &L, const Geo *geo, double Ra, const double *T, double *buoy);

@@ -79,6 +79,14 @@ typedef struct citcom_gpu_config
 	 * then unused.  0: the Cartesian box (Geometry=cart3d). */
 	int sphere;
 	double theta[2], fi[2], radius[2];
+	/* stress-dependent viscosity (viscosity.SDEPV, Viscosity_structures.c:
+	 * 155-162, 286-307): rheology 1 or 2 of visc_from_S, power-law exponent
+	 * and transition strain rate per material, the outer iteration's misfit,
+	 * iteration cap and damping of general_stokes_solver (Drive_solvers.c:45-165) */
+	int sdepv, sdepv_rheology;
+	double sdepv_expt[8], sdepv_trns[8];
+	double sdepv_misfit, sdepv_iter_damp;
+	int max_sdep_visc_iter;
 } citcom_gpu_config;
 
 /* Time-step bookkeeping that PG_timestep updates in E->advection / E->monitor. */
@@ -102,6 +110,8 @@ typedef struct citcom_gpu_stats
 	double smoother_ms;         /* device time of the finest-level Gauss-Seidel calls */
 	int smoother_sweeps;        /* finest-level sweeps (8 colour launches each) in smoother_ms */
 	unsigned long long kernel_launches;  /* kernels launched by the library since it was loaded */
+	int visc_iterations;        /* viscosity iterations of general_stokes_solver (1 unless SDEPV) */
+	double visc_misfit;         /* |dU| / |U| of the last stress-dependent iteration */
 	int warm_start;             /* 1: the attached network's guess started the Uzawa solve */
 	double warm_residual;       /* |F - K U - G P| / |F| of the network's guess */
 	double base_residual;       /* the same of the resident U, P it was compared with */

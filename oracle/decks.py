@@ -57,6 +57,14 @@ class Case:
     # theta_south, fi_west, fi_east in degrees, radius_inner, radius_outer;
     # None is the Cartesian box.  x, y, z of the mesh are then theta, phi, r.
     sphere: Optional[tuple] = None
+    # stress-dependent viscosity (Viscosity_structures.c:155-162, 286, 303-307)
+    sdepv: bool = False
+    sdepv_rheology: int = 2
+    sdepv_expt: tuple = (3.0,)
+    sdepv_trns: tuple = (1.0,)
+    sdepv_misfit: float = 0.001
+    max_sdep_visc_iter: int = 50
+    sdepv_iter_damp: float = 1.0
 
     @property
     def nox(self):
@@ -106,13 +114,15 @@ def make_deck(c: Case, datafile: str) -> str:
         "z_lmantle=0.76655052", "z_410=0.857143", "z_lith=0.9651568",
         "rheol=3",
         f"TDEPV={'on' if c.tdepv else 'off'}",
-        f"VISC_UPDATE={'on' if c.tdepv else 'off'}",
+        f"VISC_UPDATE={'on' if (c.tdepv or c.sdepv) else 'off'}",
         "update_every_steps=1",
         f"num_mat={nm}",
         f"visc0={_vec(c.visc0)}", f"viscE={_vec(c.viscE)}", f"viscT={_vec(c.viscT)}",
         f"viscZ={_vec([0.0] * nm)}",
-        "SDEPV=off", "sdepv_misfit=0.010",
-        f"sdepv_expt={_vec([1.0] * nm)}", f"sdepv_trns={_vec([1.0] * nm)}",
+        f"SDEPV={'on' if c.sdepv else 'off'}", f"sdepv_rheology={c.sdepv_rheology}",
+        f"sdepv_misfit={c.sdepv_misfit!r}", f"max_sdep_visc_iter={c.max_sdep_visc_iter}",
+        f"sdepv_iter_damp={c.sdepv_iter_damp!r}",
+        f"sdepv_expt={_vec((list(c.sdepv_expt) * nm)[:nm])}", f"sdepv_trns={_vec((list(c.sdepv_trns) * nm)[:nm])}",
         f"VMIN={'on' if c.vmin is not None else 'off'} visc_min={c.vmin if c.vmin is not None else 1e-3!r}",
         f"VMAX={'on' if c.vmax is not None else 'off'} visc_max={c.vmax if c.vmax is not None else 1e3!r}",
         "visc_smooth_cycles=1", "Viscosity=system",

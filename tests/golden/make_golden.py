@@ -12,6 +12,11 @@ Fixtures
   cfg1_16.npz      16^3 elements, 3 levels, isoviscous, Ra 1e4, the deck's own
                    sinusoidal IC, accuracy 1e-6, 5 steps (FP64-promoted build;
                    per-step scalars from the stock float build alongside).
+  sdepv_box.npz    stress-dependent viscosity (SDEPV, rheology 2, n = 3,
+                   transition strain rate 300) on a T-dependent base viscosity
+                   exp(ln(100) (0 - T)), 9^3 nodes (3 levels), Ra 1e4, seeded T0
+                   with +-0.05 noise, accuracy 1e-8, 3 time steps (FP64-promoted
+                   build; the viscosity iteration of general_stokes_solver).
   sphere_tdep.npz  Geometry=Rsphere: theta 45-135 deg, phi 0-90 deg, r 0.55-1.0,
                    9x13x9 nodes (mgunit 2,3,2; 3 levels), eta = exp(ln(100)
                    (0 - T)), Ra 1e4, seeded T0 (1 - (r - ri)/(ro - ri) plus
@@ -46,6 +51,12 @@ def sphere_case() -> Case:
                 sphere=(45.0, 135.0, 0.0, 90.0, 0.55, 1.0))
 
 
+def sdepv_case() -> Case:
+    return Case(name="sdepv_box", mgunit=(2, 2, 2), levels=3, rayleigh=1e4, tdepv=True, visc0=(1.0,),
+                viscE=(4.605170185988092,), viscT=(0.0,), accuracy=1e-8, maxstep=3, sdepv=True,
+                sdepv_rheology=2, sdepv_expt=(3.0,), sdepv_trns=(300.0,))
+
+
 def cfg1_case() -> Case:
     return Case(name="cfg1_16", mgunit=(4, 4, 4), levels=3, rayleigh=1e4, accuracy=1e-6,
                 perturbmag=0.01, perturbk=1.0, maxstep=5)
@@ -75,6 +86,13 @@ def main():
         keep["T0_input"] = T0
         np.savez_compressed(os.path.join(HERE, "small_tdep.npz"), **keep)
 
+        c = sdepv_case()
+        T0 = conductive_T0(c, amp=0.05, seed=1)
+        R = run_reference(c, os.path.join(tmp, "sdepv"), nsteps=3, T0=T0)
+        keep = {"dims": R["dims"], "T0": R["T0"], "T0_input": T0}
+        keep.update(_steps(R, 3))
+        np.savez_compressed(os.path.join(HERE, "sdepv_box.npz"), **keep)
+
         c = sphere_case()
         T0 = conductive_T0(c, amp=0.01, seed=0)
         R = run_reference(c, os.path.join(tmp, "sphere"), nsteps=3, T0=T0, probe=True)
@@ -94,7 +112,7 @@ def main():
         for k in ("T", "V1", "V2", "V3", "P"):
             keep[f"s5_{k}"] = R[f"s5_{k}"]
         np.savez_compressed(os.path.join(HERE, "cfg1_16.npz"), **keep)
-    for f in ("small_tdep.npz", "cfg1_16.npz", "sphere_tdep.npz"):
+    for f in ("small_tdep.npz", "cfg1_16.npz", "sphere_tdep.npz", "sdepv_box.npz"):
         print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")
 
 

@@ -18,7 +18,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 LOC = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]])
 FIELDS = [("Mk", (8, 8, 8, 9)), ("g", (24,)), ("gnx", (8, 8, 3)), ("N", (8, 8)), ("gda", (8,)), ("tww", (8,)),
-          ("size", (3,)), ("area", ()), ("cr", (8, 8, 3)), ("rinv", (8,)), ("rsin", (8,)), ("wface", (4,))]
+          ("size", (3,)), ("area", ()), ("cr", (8, 8, 3)), ("rinv", (8,)), ("rsin", (8,)), ("wface", (4,)),
+          ("gnxc", (8, 3)), ("rinvc", ()), ("thetac", ())]
 MGUNIT = (2, 3, 2)
 SPHERE = (45.0, 135.0, 0.0, 90.0, 0.55, 1.0)
 
