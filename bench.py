@@ -274,6 +274,25 @@ def e2e_mode(cg, s, T0, steps, warmup):
     return float(np.mean(ms)), h2d, d2h
 
 
+def output_step(s, reps: int = 10):
+    """One output step of the solved state (heat_flux and averages fields
+    computed on the device: the six .ave layer profiles, heatflux,
+    heatflux_adv, surface fluxes, Nu, Vrms; plus T, V, P) copied to pinned
+    host buffers: wall time of output_async + output_wait."""
+    bufs = s.output_buffers(pinned=True)
+    for _ in range(3):
+        s.output_async(bufs)
+        s.output_wait()
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        s.output_async(bufs)
+        s.output_wait()
+        ts.append(1e3 * (time.perf_counter() - t0))
+    return {"ms": float(np.median(ts)), "d2h_bytes": 8 * sum(s.output_sizes().values()),
+            "fields": "T, V, P, heatflux, heatflux_adv, Have (T, vrms, Vi, Rho, F, f), shflux, bhflux, Nut, Nub, Vrms"}
+
+
 # --------------------------------------------------------------- CPU side
 def cpu_sample(case, T0, uzawa_sample: int = 3, full_passes=None):
     """The oracle port (FP64, lexicographic smoother = the reference's
@@ -506,6 +525,7 @@ def main():
         e2e_ms, h2d, d2h = e2e_mode(cg, es, T0, min(args.steps, 3), 1)
         line["e2e"] = {"value": e2e_ms, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                        "mode": mode}
+        line["output_step"] = output_step(es)
     if learned:
         ln.close()
         ls.close()

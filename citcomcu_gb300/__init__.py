@@ -163,6 +163,16 @@ class _CStats(ctypes.Structure):
 _D = ctypes.POINTER(ctypes.c_double)
 _I = ctypes.POINTER(ctypes.c_int)
 _H = ctypes.c_void_p
+
+# fields of an output step, in the order of citcom_gpu_output; count per field
+# in units of (nno, nel, noz, nsf)
+OUTPUT_FIELDS = (("T", (1, 0, 0, 0)), ("V", (3, 0, 0, 0)), ("P", (0, 1, 0, 0)), ("heatflux", (1, 0, 0, 0)),
+                 ("heatflux_adv", (1, 0, 0, 0)), ("Have", (0, 0, 6, 0)), ("surf", (0, 0, 0, 2)), ("scalars", None))
+HAVE_COLUMNS = ("T", "vrms", "Vi", "Rho", "F", "f")
+
+
+class _COutput(ctypes.Structure):
+    _fields_ = [(name, _D) for name, _ in OUTPUT_FIELDS]
 _F = ctypes.POINTER(ctypes.c_float)
 _SIGNATURES = {
     "citcom_gpu_create": (ctypes.c_int, [ctypes.POINTER(_CConfig), ctypes.POINTER(ctypes.c_void_p)]),
@@ -188,6 +198,8 @@ _SIGNATURES = {
     "citcom_gpu_step_resident": (ctypes.c_int, [_H, ctypes.POINTER(_CAdvection)]),
     "citcom_gpu_last_stats": (ctypes.c_int, [_H, ctypes.POINTER(_CStats)]),
     "citcom_gpu_stokes_residuals": (ctypes.c_int, [_H, _D]),
+    "citcom_gpu_output_async": (ctypes.c_int, [_H, ctypes.POINTER(_COutput)]),
+    "citcom_gpu_output_wait": (ctypes.c_int, [_H]),
     "citcom_gpu_op_kmul": (ctypes.c_int, [_H, ctypes.c_int, _D, _D]),
     "citcom_gpu_op_gauss_seidel": (ctypes.c_int, [_H, ctypes.c_int, _D, _D, _D, ctypes.c_int, ctypes.c_int]),
     "citcom_gpu_op_project": (ctypes.c_int, [_H, ctypes.c_int, _D, _D]),
@@ -462,6 +474,63 @@ class Solver:
         adv.elapsed_time = elapsed_time
         self._check(self.lib.citcom_gpu_step_resident(self.h, ctypes.byref(adv)))
         return dict(timestep=adv.timestep, elapsed_time=adv.elapsed_time, T_interior=adv.T_interior)
+
+    # ---------------------------------------------------------- output step
+    def output_sizes(self) -> dict:
+        f = self.fine
+        nsf = f["nox"] * f["noy"]
+        out = {}
+        for name, k in OUTPUT_FIELDS:
+            out[name] = 3 if k is None else k[0] * f["nno"] + k[1] * f["nel"] + k[2] * f["noz"] + k[3] * nsf
+        return out
+
+    def output_buffers(self, pinned: bool = True) -> dict:
+        """Host buffers for output_async, page-locked when torch is available
+        (the copy to the host then overlaps the next step)."""
+        out = {}
+        for name, n in self.output_sizes().items():
+            if pinned:
+                try:
+                    import torch
+                    out[name] = torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+                    continue
+                except Exception:  # noqa: BLE001 - plain memory still works, only without the overlap
+                    pass
+            out[name] = np.empty(n)
+        return out
+
+    def output_async(self, bufs: dict):
+        """Start an output step into `bufs` (name -> float64 array, any subset
+        of OUTPUT_FIELDS); the arrays are complete after output_wait()."""
+        sizes = self.output_sizes()
+        o = _COutput()
+        for name, n in sizes.items():
+            a = bufs.get(name)
+            if a is None:
+                continue
+            if a.dtype != np.float64 or not a.flags.c_contiguous or a.size < n:
+                raise CitcomGPUError(f"output buffer {name}: need {n} contiguous float64")
+            setattr(o, name, _dp(a))
+        self._out_bufs = bufs  # kept alive until the copies complete
+        self._check(self.lib.citcom_gpu_output_async(self.h, ctypes.byref(o)))
+
+    def output_wait(self):
+        self._check(self.lib.citcom_gpu_output_wait(self.h))
+        self._out_bufs = None
+
+    def output(self) -> dict:
+        """One output step, synchronously: the fields as a dict of arrays,
+        Have split into its six layer profiles."""
+        bufs = self.output_buffers(pinned=False)
+        self.output_async(bufs)
+        self.output_wait()
+        noz, nsf = self.fine["noz"], self.fine["nox"] * self.fine["noy"]
+        out = {k: bufs[k] for k in ("T", "V", "P", "heatflux", "heatflux_adv")}
+        for i, c in enumerate(HAVE_COLUMNS):
+            out["Have_" + c] = bufs["Have"][i * noz:(i + 1) * noz]
+        out["shflux"], out["bhflux"] = bufs["surf"][:nsf], bufs["surf"][nsf:]
+        out["Nut"], out["Nub"], out["vrms"] = (float(x) for x in bufs["scalars"])
+        return out
 
     # ---------------------------------------------------- single operators
     def op_kmul(self, lev, u):

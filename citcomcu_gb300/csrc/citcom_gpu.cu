@@ -105,6 +105,13 @@ struct citcom_gpu
 	double *oldU;      // the previous viscosity iteration's U (general_stokes_solver's oldU, kept across solves)
 	double *edot;      // strain-rate invariant per fine element
 	int sdepv_visits;  // calls of visc_from_S so far (the first one takes a unit strain rate)
+	// output steps: device staging of the fields (allocated on first use), the
+	// stream of their host copies, the event that orders it after the compute
+	// stream and the event of its completion
+	double *snap;
+	cudaStream_t st_out;
+	cudaEvent_t ev_snap, ev_out;
+	bool snap_pending;
 	char err[512];
 };
 
@@ -1131,6 +1138,15 @@ void citcom_gpu_destroy(citcom_gpu *h)
 			        h->lt_sweeps[l] ? 1e3 * h->lt_ms[l] / h->lt_sweeps[l] : 0.0);
 	if(h->st)
 		cudaStreamSynchronize(h->st);
+	if(h->st_out)
+	{
+		cudaStreamSynchronize(h->st_out);
+		cudaStreamDestroy(h->st_out);
+	}
+	if(h->ev_snap)
+		cudaEventDestroy(h->ev_snap);
+	if(h->ev_out)
+		cudaEventDestroy(h->ev_out);
 	if(h->mg_exec)
 		cudaGraphExecDestroy(h->mg_exec);
 	for(void *p : h->allocs)
@@ -1367,6 +1383,61 @@ int citcom_gpu_step_resident(citcom_gpu *h, citcom_gpu_advection *adv)
 	float ms = 0.f;
 	CK(cudaEventElapsedTime(&ms, a, b));
 	h->stats.energy_ms = ms;
+	return CITCOM_GPU_OK;
+}
+
+int citcom_gpu_output_async(citcom_gpu *h, const citcom_gpu_output *o)
+{
+	TRY(check_handle(h));
+	if(!o)
+		return fail(h, CITCOM_GPU_ERR_ARG, "null output descriptor");
+	const int lmax = h->L - 1;
+	const Lvl &Lf = h->lv[lmax];
+	const size_t nno = Lf.nno, nel = Lf.nel, noz = Lf.noz, nsf = (size_t)Lf.nox * Lf.noy;
+	if(!h->snap)
+	{
+		TRY(dalloc(h, &h->snap, 8 * nno + 4 * nel + 6 * noz + 2 * nsf + 9));
+		if(cudaStreamCreateWithFlags(&h->st_out, cudaStreamNonBlocking) != cudaSuccess ||
+		   cudaEventCreateWithFlags(&h->ev_snap, cudaEventDisableTiming) != cudaSuccess ||
+		   cudaEventCreateWithFlags(&h->ev_out, cudaEventDisableTiming) != cudaSuccess)
+			return fail(h, CITCOM_GPU_ERR_CUDA, "output stream/event creation failed");
+	}
+	double *sT = h->snap, *sV = sT + nno, *sP = sV + 3 * nno, *f = sP + nel, *scratch = f + 3 * nno, *ue = scratch + nno;
+	double *H = ue + 3 * nel, *surf = H + 6 * noz, *sums = surf + 2 * nsf, *scal = sums + 6;
+	// the staging must not change under a host copy still in flight
+	if(h->snap_pending)
+		CK(cudaStreamWaitEvent(h->st, h->ev_out, 0));
+	if(o->T)
+		CK(cudaMemcpyAsync(sT, h->T, sizeof(double) * nno, cudaMemcpyDeviceToDevice, h->st));
+	if(o->V)
+		CK(cudaMemcpyAsync(sV, h->V, sizeof(double) * 3 * nno, cudaMemcpyDeviceToDevice, h->st));
+	if(o->P)
+		CK(cudaMemcpyAsync(sP, h->P, sizeof(double) * nel, cudaMemcpyDeviceToDevice, h->st));
+	if(o->heatflux || o->heatflux_adv || o->Have || o->surf || o->scalars)
+		launch_output_fields(h->st, Lf, h->geo[lmax], h->T, h->V, h->evi[lmax], red_of(h), f, scratch, ue, H, surf, sums, scal);
+	CK(cudaEventRecord(h->ev_snap, h->st));
+	CK(cudaStreamWaitEvent(h->st_out, h->ev_snap, 0));
+	struct
+	{
+		double *dst;
+		const double *src;
+		size_t n;
+	} cp[8] = {{o->T, sT, nno},           {o->V, sV, 3 * nno},         {o->P, sP, nel},   {o->heatflux, f + 2 * nno, nno},
+	           {o->heatflux_adv, f + nno, nno}, {o->Have, H, 6 * noz}, {o->surf, surf, 2 * nsf}, {o->scalars, scal, 3}};
+	for(int i = 0; i < 8; ++i)
+		if(cp[i].dst)
+			CK(cudaMemcpyAsync(cp[i].dst, cp[i].src, sizeof(double) * cp[i].n, cudaMemcpyDeviceToHost, h->st_out));
+	CK(cudaEventRecord(h->ev_out, h->st_out));
+	h->snap_pending = true;
+	return CITCOM_GPU_OK;
+}
+
+int citcom_gpu_output_wait(citcom_gpu *h)
+{
+	TRY(check_handle(h));
+	if(h->snap_pending)
+		CK(cudaEventSynchronize(h->ev_out));
+	h->snap_pending = false;
 	return CITCOM_GPU_OK;
 }
 

@@ -1587,6 +1587,119 @@ __global__ void k_hf_surface(Lvl L, const Geo *__restrict__ geo, const double *_
 	block_reduce_store<4>(v, red, out);
 }
 
+// Output fields of heat_flux (Process_buoyancy.c:103-136), per element: the
+// Gauss integrals over the element / its area of u_z T - dT/dz, u_z T' and
+// u_z |T'|, T' = T - <T> (HT: the layer means of T); ue = 3 x nel
+__global__ void k_out_elem(Lvl L, const Geo *__restrict__ geo, const double *__restrict__ T, const double *__restrict__ V,
+                           const double *__restrict__ HT, double *__restrict__ ue)
+{
+	pdl_begin();
+	const int e = blockIdx.x * blockDim.x + threadIdx.x;
+	if(e >= L.nel)
+		return;
+	const int ez = e % L.elz, ex = (e / L.elz) % L.elx, ey = e / (L.elz * L.elx);
+	const Geo *G = geo + cg_col(L, ex, ez);
+	double vz[8], tt[8], ta[8];
+	for(int a = 0; a < 8; ++a)
+	{
+		const int n = cg_node(L, ex + cg_loc(a, 0), ey + cg_loc(a, 1), ez + cg_loc(a, 2));
+		vz[a] = V[2 * (size_t)L.nno + n];
+		tt[a] = T[n];
+		ta[a] = T[n] - HT[ez + cg_loc(a, 2)];
+	}
+	double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+	for(int k = 0; k < 8; ++k)
+	{
+		double u = 0, t = 0, t1 = 0, dz = 0;
+		for(int a = 0; a < 8; ++a)
+		{
+			u += vz[a] * G->N[k][a];
+			t += tt[a] * G->N[k][a];
+			t1 += ta[a] * G->N[k][a];
+			dz += tt[a] * G->gnx[k][a][2];
+		}
+		s0 += (u * t - dz) * G->gda[k];
+		s1 += u * t1 * G->gda[k];
+		s2 += u * fabs(t1) * G->gda[k];
+	}
+	ue[e] = s0 / G->area;
+	ue[L.nel + e] = s1 / G->area;
+	ue[2 * L.nel + e] = s2 / G->area;
+}
+
+// nodal fields from the element means, TWW-weighted / lumped mass: f = 3 x nno
+// (heatflux, heatflux_adv, flux of Process_buoyancy.c:138-152)
+__global__ void k_out_node(Lvl L, const Geo *__restrict__ geo, const double *__restrict__ ue, double *__restrict__ f)
+{
+	pdl_begin();
+	const int n = blockIdx.x * blockDim.x + threadIdx.x;
+	if(n >= L.nno)
+		return;
+	const int z = n % L.noz, x = (n / L.noz) % L.nox, y = n / (L.noz * L.nox);
+	double s0 = 0.0, s1 = 0.0, s2 = 0.0, m = 0.0;
+	for(int a = 0; a < 8; ++a)
+	{
+		const int ex = x - cg_loc(a, 0), ey = y - cg_loc(a, 1), ez = z - cg_loc(a, 2);
+		if(ex < 0 || ex >= L.elx || ey < 0 || ey >= L.ely || ez < 0 || ez >= L.elz)
+			continue;
+		const double w = geo[cg_col(L, ex, ez)].tww[a];
+		const int e = ez + L.elz * (ex + L.elx * ey);
+		s0 += w * ue[e];
+		s1 += w * ue[L.nel + e];
+		s2 += w * ue[2 * L.nel + e];
+		m += w;
+	}
+	const double im = 1.0 / m;
+	f[n] = s0 * im;
+	f[L.nno + n] = s1 * im;
+	f[2 * (size_t)L.nno + n] = s2 * im;
+}
+
+// surface heat flux by linear extrapolation of the two outermost nodes of each
+// column (Process_buoyancy.c:154-161): surf = (shflux, bhflux), nsf each, and
+// the extrapolated values replace the surface nodes of hf
+__global__ void k_out_surface(Lvl L, double *__restrict__ hf, double *__restrict__ surf)
+{
+	pdl_begin();
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	const int nsf = L.nox * L.noy;
+	if(i >= nsf)
+		return;
+	const int top = i * L.noz + L.noz - 1, bot = i * L.noz;
+	const double s = 2.0 * hf[top] - hf[top - 1], b = 2.0 * hf[bot] - hf[bot + 1];
+	surf[i] = s;
+	surf[nsf + i] = b;
+	hf[top] = s;
+	hf[bot] = b;
+}
+
+// |V|^2 per node (averages, Process_velocity.c:198-209)
+__global__ void k_out_speed2(Lvl L, const double *__restrict__ V, double *__restrict__ v2)
+{
+	pdl_begin();
+	const int n = blockIdx.x * blockDim.x + threadIdx.x;
+	if(n >= L.nno)
+		return;
+	const double a = V[n], b = V[L.nno + n], c = V[2 * (size_t)L.nno + n];
+	v2[n] = a * a + b * b + c * c;
+}
+
+// sums = (Nu top sum, bottom sum, top weight, bottom weight, vrms sum, volume)
+// -> scal = (Nut, Nub, Vrms); H[noz .. 2 noz) = sqrt of the layer means of |V|^2
+__global__ void k_out_final(Lvl L, const double *__restrict__ sums, double *__restrict__ scal, double *__restrict__ H)
+{
+	pdl_begin();
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i < L.noz)
+		H[L.noz + i] = sqrt(H[L.noz + i]);
+	if(i == 0)
+	{
+		scal[0] = sums[0] / (4.0 * sums[2]);
+		scal[1] = sums[1] / (4.0 * sums[3]);
+		scal[2] = sqrt(sums[4] / sums[5]);
+	}
+}
+
 __global__ void k_vrms(Lvl L, const Geo *__restrict__ geo, const double *__restrict__ V, Red red, double *out)
 {
 	pdl_begin();
@@ -1987,6 +2100,11 @@ void launch_buoyancy(cudaStream_t st, const Lvl &L, const Geo *geo, double Ra, c
 	launch_k(k_buoyancy, nblocks(L.nno), TPB, st, L, Ra, T, H, buoy);
 }
 
+void launch_horiz_ave(cudaStream_t st, const Lvl &L, const Geo *geo, const double *T, double *H)
+{
+	launch_k(k_horiz_ave, L.noz, TPB, st, L, geo, 1.0, T, H);
+}
+
 void launch_forces(cudaStream_t st, const Lvl &L, const Geo *geo, const double *buoy, double *F)
 {
 	launch_k(k_forces, nblocks(L.nno), TPB, st, L, geo, buoy, F);
@@ -2041,4 +2159,28 @@ void launch_heat_flux(cudaStream_t st, const Lvl &L, const Geo *geo, const doubl
 void launch_vrms(cudaStream_t st, const Lvl &L, const Geo *geo, const double *V, Red red, double *out)
 {
 	launch_k(k_vrms, red_grid(L.nel), RED_THREADS, st, L, geo, V, red, out);
+}
+
+void launch_output_fields(cudaStream_t st, const Lvl &L, const Geo *geo, const double *T, const double *V, const double *evi, Red red,
+                          double *f, double *scratch, double *ue, double *H, double *surf, double *sums, double *scal)
+{
+	const int noz = L.noz;
+	// heat_flux: Have.T first (the element integrals need it), then the three
+	// nodal fields, Nu from the unreplaced heatflux, the surface replacement and
+	// the layer means Have.Rho / F / f
+	launch_k(k_horiz_ave, noz, TPB, st, L, geo, 1.0, T, H);
+	launch_k(k_out_elem, nblocks(L.nel), TPB, st, L, geo, T, V, (const double *)H, ue);
+	launch_k(k_out_node, nblocks(L.nno), TPB, st, L, geo, (const double *)ue, f);
+	launch_k(k_hf_surface, red_grid((long)L.elx * L.ely), RED_THREADS, st, L, geo, (const double *)f, red, sums);
+	launch_k(k_out_surface, nblocks(L.nox * L.noy), TPB, st, L, f, surf);
+	launch_k(k_horiz_ave, noz, TPB, st, L, geo, 1.0, (const double *)f, H + 3 * noz);
+	launch_k(k_horiz_ave, noz, TPB, st, L, geo, 1.0, (const double *)(f + L.nno), H + 4 * noz);
+	launch_k(k_horiz_ave, noz, TPB, st, L, geo, 1.0, (const double *)(f + 2 * (size_t)L.nno), H + 5 * noz);
+	// averages: Have.vrms and Have.Vi, and the global Vrms
+	launch_k(k_out_speed2, nblocks(L.nno), TPB, st, L, V, scratch);
+	launch_k(k_horiz_ave, noz, TPB, st, L, geo, 1.0, (const double *)scratch, H + noz);
+	launch_k(k_visc_to_nodes, nblocks(L.nno), TPB, st, L, geo, evi, scratch);
+	launch_k(k_horiz_ave, noz, TPB, st, L, geo, 1.0, (const double *)scratch, H + 2 * noz);
+	launch_k(k_vrms, red_grid(L.nel), RED_THREADS, st, L, geo, V, red, sums + 4);
+	launch_k(k_out_final, nblocks(noz), TPB, st, L, (const double *)sums, scal, H);
 }

@@ -184,6 +184,8 @@ void launch_visc_from_S(cudaStream_t st, const Lvl &L, const Geo *geo, const Rhe
 void launch_project_viscosity(cudaStream_t st, const Lvl &Lf, const Lvl &Lc, const Geo *geof, const Geo *geoc,
                               const double *evi_f, double *evi_c, double *work_f, double *work_c);
 void launch_buoyancy(cudaStream_t st, const Lvl &L, const Geo *geo, double Ra, const double *T, double *buoy);
+// H[z] = horizontal average of T on node layer z (return_horiz_ave)
+void launch_horiz_ave(cudaStream_t st, const Lvl &L, const Geo *geo, const double *T, double *H);
 void launch_forces(cudaStream_t st, const Lvl &L, const Geo *geo, const double *buoy, double *F);
 void launch_v_from_vector(cudaStream_t st, const Lvl &L, const double *U, double *V);
 void launch_pg_residual(cudaStream_t st, const Lvl &L, const Geo *geo, const double *T, const double *Tdot, const double *V,
@@ -197,3 +199,10 @@ void launch_conform_T(cudaStream_t st, const Lvl &L, double *T);
 void launch_heat_flux(cudaStream_t st, const Lvl &L, const Geo *geo, const double *T, const double *V, double *hf_work,
                       Red red, double *out_nut_nub);
 void launch_vrms(cudaStream_t st, const Lvl &L, const Geo *geo, const double *V, Red red, double *out);
+// The fields of an output step (heat_flux, Process_buoyancy.c:63-203, and
+// averages, Process_velocity.c:179-224) from the resident T, V and viscosity:
+// f (3 nno): heatflux with the surface nodes replaced, heatflux_adv, flux;
+// H (6 noz): layer means T, vrms, Vi, Rho, F, f; surf (2 nsf): shflux, bhflux;
+// scal (3): Nut, Nub, Vrms.  scratch: nno, ue: 3 nel, sums: 6 words.
+void launch_output_fields(cudaStream_t st, const Lvl &L, const Geo *geo, const double *T, const double *V, const double *evi, Red red,
+                          double *f, double *scratch, double *ue, double *H, double *surf, double *sums, double *scal);

@@ -174,6 +174,32 @@ int citcom_gpu_store_state(citcom_gpu *h, double *T, double *Tdot, double *U, do
 int citcom_gpu_stokes_resident(citcom_gpu *h);
 int citcom_gpu_step_resident(citcom_gpu *h, citcom_gpu_advection *adv);
 int citcom_gpu_last_stats(const citcom_gpu *h, citcom_gpu_stats *s);
+/* Output step.  The reference computes the fields of an output step on the
+ * host (heat_flux, Process_buoyancy.c:63-203; averages,
+ * Process_velocity.c:179-224) and writes them as ASCII (output_velo_related,
+ * Output.c:54-170).  citcom_gpu_output_async computes them on the device from
+ * the resident state (T, V, P, viscosity), copies them into device staging on
+ * the handle's stream, and from there to the caller's host buffers on a second
+ * stream, so that the copy to the host overlaps the work queued after it (the
+ * next time step).  Host buffers should be pinned for the overlap; any pointer
+ * may be null.  They are complete once citcom_gpu_output_wait returns; a
+ * second call first waits for the previous one's copies.  The staging
+ * (8 nno + 4 nel doubles) is allocated on the first call.  Composition
+ * (Have.C), the adiabat (Have.Tadi) and topography (slice.tpg) are not
+ * computed. */
+typedef struct
+{
+	double *T;            /* nno */
+	double *V;            /* 3 x nno (V[1], V[2], V[3]) */
+	double *P;            /* nel */
+	double *heatflux;     /* nno: E->heatflux as heat_flux leaves it (u_z |T - <T>|) */
+	double *heatflux_adv; /* nno: E->heatflux_adv (u_z (T - <T>)) */
+	double *Have;         /* 6 x noz: Have.T, vrms, Vi, Rho, F, f (.ave columns 1-6) */
+	double *surf;         /* 2 x nox noy: slice.shflux, slice.bhflux */
+	double *scalars;      /* 3: slice.Nut, slice.Nub, Vrms */
+} citcom_gpu_output;
+int citcom_gpu_output_async(citcom_gpu *h, const citcom_gpu_output *out);
+int citcom_gpu_output_wait(citcom_gpu *h);
 /* Residuals of the resident solution, in FP64: out[0] = |F - K U - G P| / |F|
  * (momentum), out[1] = |div U| / (|U| sqrt(npno/neq)) (continuity).  No
  * counterpart in the reference, which stops on the relative increments

@@ -214,6 +214,55 @@ static double vrms_of(struct All_variables *E)
 	return sqrt(s / vol);
 }
 
+/* The output-step fields after heat_flux: the layer profiles that
+ * output_velo_related writes to the .ave file (Have.T, Rho, F, f from heat_flux;
+ * Have.vrms and Have.Vi computed here as averages, Process_velocity.c:179-224,
+ * does, through the same reference routines, without its composition part),
+ * the nodal heatflux / heatflux_adv and the surface fluxes of the .th_t/.th_b
+ * files. */
+static void dump_output_fields(struct All_variables *E, int step)
+{
+	char nm[64];
+	const int nno = E->lmesh.nno, noz = E->lmesh.noz, nsf = E->lmesh.nsf;
+	const int lev = E->mesh.levmax;
+	float *temp = (float *)malloc((size_t)(nno + 1) * sizeof(float));
+	double *have = (double *)malloc((size_t)6 * noz * sizeof(double));
+	double *surf = (double *)malloc((size_t)2 * nsf * sizeof(double));
+	int i;
+	visc_from_gint_to_nodes(E, E->EVI[lev], temp, lev);
+	return_horiz_ave(E, temp, E->Have.Vi);
+	for(i = 1; i <= nno; i++)
+		temp[i] = E->V[1][i] * E->V[1][i] + E->V[2][i] * E->V[2][i] + E->V[3][i] * E->V[3][i];
+	return_horiz_ave(E, temp, E->Have.vrms);
+	for(i = 1; i <= noz; i++)
+		E->Have.vrms[i] = sqrt(E->Have.vrms[i]);
+	for(i = 0; i < noz; i++)
+	{
+		have[i] = E->Have.T[i + 1];
+		have[noz + i] = E->Have.vrms[i + 1];
+		have[2 * noz + i] = E->Have.Vi[i + 1];
+		have[3 * noz + i] = E->Have.Rho[i + 1];
+		have[4 * noz + i] = E->Have.F[i + 1];
+		have[5 * noz + i] = E->Have.f[i + 1];
+	}
+	for(i = 0; i < nsf; i++)
+	{
+		surf[i] = E->slice.shflux[i + 1];
+		surf[nsf + i] = E->slice.bhflux[i + 1];
+	}
+	snprintf(nm, sizeof nm, "s%d_Have", step);
+	rec_d(nm, have, 6L * noz);
+	snprintf(nm, sizeof nm, "s%d_surf", step);
+	rec_d(nm, surf, 2L * nsf);
+	snprintf(nm, sizeof nm, "s%d_heatflux", step);
+	rec_f(nm, E->heatflux + 1, nno);
+	snprintf(nm, sizeof nm, "s%d_heatflux_adv", step);
+	rec_f(nm, E->heatflux_adv + 1, nno);
+	free(temp);
+	free(have);
+	free(surf);
+}
+
 static void dump_state(struct All_variables *E, int step, double stokes_s, int uzawa_calls, int mg_cycles)
 {
 	char nm[64];
@@ -249,6 +298,7 @@ static void dump_state(struct All_variables *E, int step, double stokes_s, int u
 		snprintf(nm, sizeof nm, "s%d_scalars", step);
 		rec_d(nm, sc, 10);
 	}
+	dump_output_fields(E, step);
 }
 
 static void timed_stokes(struct All_variables *E, double *secs, int *calls, int *cycles)

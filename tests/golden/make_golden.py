@@ -22,6 +22,9 @@ Fixtures
                    (0 - T)), Ra 1e4, seeded T0 (1 - (r - ri)/(ro - ri) plus
                    noise), accuracy 1e-8.  Operator probes on every level plus
                    3 time steps (FP64-promoted build).
+small_tdep, sdepv_box and sphere_tdep also hold, per step, the fields of an
+output step after heat_flux (s<k>_Have: the six .ave layer profiles T, vrms,
+Vi, Rho, F, f; s<k>_surf: shflux, bhflux; s<k>_heatflux, s<k>_heatflux_adv).
 """
 from __future__ import annotations
 
@@ -62,7 +65,10 @@ def cfg1_case() -> Case:
                 perturbmag=0.01, perturbk=1.0, maxstep=5)
 
 
-def _steps(R, n, keys=("T", "V1", "V2", "V3", "U", "P", "Tdot")):
+OUTPUT_KEYS = ("Have", "surf", "heatflux", "heatflux_adv")
+
+
+def _steps(R, n, keys=("T", "V1", "V2", "V3", "U", "P", "Tdot") + OUTPUT_KEYS):
     out = {}
     for s in range(n + 1):
         for k in keys:
