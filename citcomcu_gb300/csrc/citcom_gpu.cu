@@ -93,6 +93,10 @@ struct citcom_gpu
 	int co_cluster;
 	size_t co_smem;
 	bool co_local[CITCOM_MAX_LEVELS];
+	// the zero-start smoothing of level 0 as one dense product d = N f
+	// (CITCOM_GPU_NO_DENSE keeps the sweeps): N and its build scratch
+	float *co_dense;
+	float *co_dense_work;
 	CoLevels co_lv;
 	CoProg co_prog;
 	double lt_ms[CITCOM_MAX_LEVELS];
@@ -303,6 +307,8 @@ void co_push(citcom_gpu *h, int type, int lev, int a, int b, int c, int cycles =
 	op.c = (unsigned char)c;
 	op.zero = (unsigned char)zero;
 	op.local = (unsigned char)(type == CO_GS && h->co_local[lev]);
+	if(type == CO_GS && lev == 0 && zero && h->co_dense && cycles == h->cfg.vlowstep)
+		op.type = CO_DENSE;
 	op.pad = 0;
 	op.cycles = (unsigned short)cycles;
 }
@@ -706,6 +712,9 @@ int construct_stiffness(citcom_gpu *h)
 		                need32 ? h->K32[l] : nullptr, need64 ? h->BI64[l] : nullptr, need32 ? h->BI32[l] : nullptr);
 		if(h->Kt32[l])
 			launch_tiny_stencil(h->st, h->lv[l], h->K32[l], h->Kt32[l]);
+		if(l == 0 && h->co_dense)
+			launch_coarse_dense_build(h->st, h->lv[0], h->Kt32[0], h->BI32[0], c.vlowstep, h->co_dense_work, h->co_dense,
+			                          h->dscal + S_ERR);
 	}
 	launch_bpi(h->st, h->lv[lmax], h->geo[lmax], h->BI64[lmax], h->BPI, c.precond);
 	CK(cudaGetLastError());
@@ -1074,6 +1083,19 @@ int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 			for(int v = 0; v < CO_NVEC; ++v)
 				h->co_lv.vec[l][v] = mg_vec(h->mg32, l, v);
 		}
+		h->co_dense = nullptr;
+		h->co_dense_work = nullptr;
+		if(h->co_LC >= 0 && h->co_local[0] && h->lv[0].neq <= CO_DENSE_MAX_EQ)
+		{
+			const char *nd = getenv("CITCOM_GPU_NO_DENSE");
+			if(!(nd && nd[0] && nd[0] != '0'))
+			{
+				const size_t n = (size_t)h->lv[0].neq;
+				TRYC(dalloc(h, &h->co_dense, n * n));
+				TRYC(dalloc(h, &h->co_dense_work, 2 * n * n));
+			}
+		}
+		h->co_lv.dense = h->co_dense;
 		TRYC(dalloc(h, &h->BPI, Lf.nel));
 		TRYC(dalloc(h, &h->visc_work[0], Lf.nno));
 		TRYC(dalloc(h, &h->visc_work[1], Lf.nno));

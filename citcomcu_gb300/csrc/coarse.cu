@@ -591,6 +591,32 @@ __global__ void __launch_bounds__(CO_THREADS) k_coarse(const __grid_constant__ C
 				halo_lev = -1;
 			break;
 		}
+		case CO_DENSE:
+		{
+			// vec a = N vec b: this CTA's rows, one warp per row, the
+			// right-hand side staged in shared memory
+			float *sv = reinterpret_cast<float *>(arena);
+			const int n = L.neq;
+			co_stage(D.vec[l][op.b], n, sv);
+			int lo, cnt;
+			co_chunk(n, rank, ncta, lo, cnt);
+			const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+			float *out = D.vec[l][op.a];
+			for(int i = lo + warp; i < lo + cnt; i += CO_WARPS)
+			{
+				const float *row = D.dense + (size_t)i * n;
+				float s = 0.f;
+				for(int k = lane; k < n; k += 32)
+					s += __ldg(row + k) * sv[k];
+#pragma unroll
+				for(int o = 16; o > 0; o >>= 1)
+					s += __shfl_xor_sync(0xffffffffu, s, o);
+				if(lane == 0)
+					out[i] = s;
+			}
+			halo_lev = -1;
+			break;
+		}
 		case CO_UPD:
 		{
 			// vec a += alpha vec b (the level's line-search step)
@@ -648,12 +674,43 @@ size_t co_gs_bytes(const Lvl &L, bool local)
 	return 16 * (hn + 16 * CO_NODES) + 8 * 8 * CO_NODES + (local ? (size_t)16 * 63 * L.nno : 0);
 }
 
+// column j of the coarsest smoother's matrix: the one-CTA smoother of the
+// cluster program run from d = 0 against f = e_j (work[j n ..] holds e_j,
+// work[n^2 + j n ..] receives the column)
+__global__ void __launch_bounds__(CO_THREADS) k_co_dense_build(Lvl L, const float4 *Kt, const float *BI, int cycles, float *work, double *err)
+{
+	pdl_begin();
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	__shared__ __align__(8) unsigned long long bars[2];
+	const int n = L.neq, j = blockIdx.x;
+	float *f = work + (size_t)j * n;
+	float *d = work + (size_t)n * n + (size_t)j * n;
+	for(int i = threadIdx.x; i < n; i += blockDim.x)
+		f[i] = (i == j) ? 1.f : 0.f;
+	__threadfence();
+	__syncthreads();
+	cgp::cluster_group cl = cgp::this_cluster();
+	co_gs<true>(cl, L, Kt, BI, d, f, cycles, true, 0, reinterpret_cast<float4 *>(smem_raw), bars, err);
+}
+
+// N[i][j] = column j, entry i
+__global__ void k_co_dense_t(int n, const float *cols, float *N)
+{
+	pdl_begin();
+	const int t = blockIdx.x * blockDim.x + threadIdx.x;
+	if(t >= n * n)
+		return;
+	const int i = t / n, j = t - i * n;
+	N[t] = cols[(size_t)j * n + i];
+}
+
 } // namespace
 
 int coarse_init(int *cluster_size)
 {
 	*cluster_size = 0;
-	if(cudaFuncSetAttribute(k_coarse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CO_SMEM_MAX) != cudaSuccess)
+	if(cudaFuncSetAttribute(k_coarse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CO_SMEM_MAX) != cudaSuccess ||
+	   cudaFuncSetAttribute(k_co_dense_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CO_SMEM_MAX) != cudaSuccess)
 		return -1;
 	cudaFuncSetAttribute(k_coarse, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
 	for(int cs = CO_MAX_CLUSTER; cs >= 8; cs /= 2)
@@ -696,6 +753,15 @@ bool coarse_level_ok(const Lvl &L, int level, int cluster, bool *local)
 size_t coarse_smem(const Lvl &L, bool local) { return co_gs_bytes(L, local); }
 
 int coarse_window(const Lvl &L, int cluster) { return cg_owner_window(L, cluster); }
+
+void launch_coarse_dense_build(cudaStream_t st, const Lvl &L, const float4 *Kt, const float *BI, int cycles, float *work, float *N,
+                               double *err)
+{
+	const int n = L.neq;
+	k_co_dense_build<<<n, CO_THREADS, co_gs_bytes(L, true), st>>>(L, Kt, BI, cycles, work, err);
+	k_co_dense_t<<<(n * n + 255) / 256, 256, 0, st>>>(n, work + (size_t)n * n, N);
+	g_kernel_launches += 2;
+}
 
 void launch_coarse(cudaStream_t st, const CoLevels &D, const CoProg &P, int cluster, size_t smem)
 {

@@ -100,7 +100,8 @@ enum CoOpType
 	CO_PROJ,    // vec b (level lev-1) = projection of vec a (level lev), stripped
 	CO_INTERP,  // vec b (level lev) = interpolation of vec a (level lev-1), stripped
 	CO_KDOT,    // vec c = K vec a; alpha = (c . vec b) / (c . c), FP64; if `zero`: then vel += alpha vec a
-	CO_UPD      // vec a += alpha vec b
+	CO_UPD,     // vec a += alpha vec b
+	CO_DENSE    // vec a = N vec b: `cycles` zero-start sweeps of level 0 as one dense product
 };
 #define CO_MAX_LEV 6
 #define CO_MAX_OPS 96
@@ -125,6 +126,7 @@ struct CoLevels
 	int win[CO_MAX_LEV];  // ranks on either side of a node's owner that hold its neighbours
 	const Geo *geo[CO_MAX_LEV];  // geometry tables (TWW of the projection, sizes of the interpolation)
 	double *err;          // set to 1 if a wait of the cluster smoother timed out
+	const float *dense;   // N (neq x neq, row-major) of the level-0 smoother, or null
 };
 // cluster size the device supports for the program (16 or 8); -1 if none
 int coarse_init(int *cluster_size);
@@ -134,6 +136,14 @@ bool coarse_level_ok(const Lvl &L, int level, int cluster, bool *local);
 int coarse_window(const Lvl &L, int cluster);
 size_t coarse_smem(const Lvl &L, bool local);
 void launch_coarse(cudaStream_t st, const CoLevels &D, const CoProg &P, int cluster, size_t smem);
+// The coarsest smoother as a matrix.  With a zero start, `cycles` Gauss-Seidel
+// sweeps of level 0 are linear in the right-hand side: d = N f.  Column j of N
+// is the smoother (the cluster program's own one-CTA smoother, same colour
+// order and arithmetic) applied to the unit vector e_j, one CTA per column.
+// work: 2 neq^2 floats; N: neq^2 floats, row-major.
+#define CO_DENSE_MAX_EQ 2048
+void launch_coarse_dense_build(cudaStream_t st, const Lvl &L, const float4 *Kt, const float *BI, int cycles, float *work, float *N,
+                               double *err);
 
 // Stencil kernels of the tiled (large) levels, tile.cu: persistent CTAs
 // streaming tiles through shared memory with bulk copies
