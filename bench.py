@@ -483,6 +483,7 @@ def main():
 
     def summary(recs, res, nu, vr):
         return {"stokes_ms_per_step": float(np.mean([r["stokes_ms"] for r in recs])),
+                "multigrid_ms_per_step": float(np.mean([r["pass_ms"] for r in recs])),
                 "uzawa_iterations": [r["uzawa"] for r in recs], "mg_passes": [r["mg_passes"] for r in recs],
                 "residuals_final": res, "nu_top": nu[0], "vrms": vr,
                 "nu_rel_err_vs_fp64": abs(nu[0] - nu_fp64[0]) / abs(nu_fp64[0]),

@@ -156,7 +156,8 @@ class _CStats(ctypes.Structure):
                 ("smoother_ms", ctypes.c_double), ("smoother_sweeps", ctypes.c_int),
                 ("kernel_launches", ctypes.c_ulonglong), ("visc_iterations", ctypes.c_int),
                 ("visc_misfit", ctypes.c_double), ("warm_start", ctypes.c_int),
-                ("warm_residual", ctypes.c_double), ("base_residual", ctypes.c_double)]
+                ("warm_residual", ctypes.c_double), ("base_residual", ctypes.c_double),
+                ("pass_ms", ctypes.c_double)]
 
 
 # every symbol of include/citcom_gb300.h with its argument types
@@ -372,7 +373,7 @@ class Solver:
                     initial_residual=s.initial_residual, stokes_ms=s.stokes_ms, energy_ms=s.energy_ms,
                     smoother_ms=s.smoother_ms, smoother_sweeps=s.smoother_sweeps, kernel_launches=s.kernel_launches,
                     warm_start=s.warm_start, warm_residual=s.warm_residual, base_residual=s.base_residual,
-                    visc_iterations=s.visc_iterations, visc_misfit=s.visc_misfit)
+                    visc_iterations=s.visc_iterations, visc_misfit=s.visc_misfit, pass_ms=s.pass_ms)
 
     def stokes_residuals(self):
         """(|F - K U - G P| / |F|, |div U| / (|U| sqrt(npno/neq))) of the resident solution."""

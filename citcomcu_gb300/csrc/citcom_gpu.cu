@@ -75,6 +75,7 @@ struct citcom_gpu
 	Red red;
 	cudaStream_t st;
 	cudaEvent_t ev0, ev1;
+	cudaEvent_t ev_pass[2];  // brackets each multigrid pass
 	cudaEvent_t ev_gs[8];   // brackets the finest-level smoother calls inside a multigrid pass
 	int n_gs_pairs;         // pairs recorded by the captured pass
 	cudaGraphExec_t mg_exec;
@@ -552,7 +553,9 @@ int solve_del2_u(citcom_gpu *h, double acc, int *valid)
 		if(count >= 1000)
 			return fail(h, CITCOM_GPU_ERR_NOCONV, "solve_del2_u: no convergence after %d multigrid passes (residual %g > %g)",
 			            count, residual, acc);
+		CK(cudaEventRecord(h->ev_pass[0], h->st));
 		TRY(run_pass(h));
+		CK(cudaEventRecord(h->ev_pass[1], h->st));
 		if(tile_error_async(h->hscal + S_TERR, h->st) != 0)
 			return fail(h, CITCOM_GPU_ERR_CUDA, "solve_del2_u: reading the tile kernels' error word failed");
 		TRY(readback(h, S_RES, 2));
@@ -561,6 +564,13 @@ int solve_del2_u(citcom_gpu *h, double acc, int *valid)
 		if(h->hscal[S_TERR] != 0.0)
 			return fail(h, CITCOM_GPU_ERR_CUDA, "solve_del2_u: a stencil tile copy did not arrive");
 		residual = std::sqrt(h->hscal[S_RES] / neq);
+		{
+			float ms = 0.f;
+			if(cudaEventElapsedTime(&ms, h->ev_pass[0], h->ev_pass[1]) == cudaSuccess)
+				h->stats.pass_ms += ms;
+			else
+				cudaGetLastError();
+		}
 		for(int k = 0; k < h->n_gs_pairs; ++k)
 		{
 			float ms = 0.f;
@@ -774,6 +784,7 @@ int stokes_resident(citcom_gpu *h)
 	h->stats.mg_passes = 0;
 	h->stats.smoother_ms = 0.0;
 	h->stats.smoother_sweeps = 0;
+	h->stats.pass_ms = 0.0;
 	launch_strip(h->st, Lf, h->U);  // velocities_conform_bcs with VB = 0
 	TRY(forces_from_device_T(h));
 	// the viscosity iteration of stress-dependent rheologies (Drive_solvers.c:
@@ -989,6 +1000,8 @@ int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 		bool ev_ok = true;
 		for(int k = 0; k < 8; ++k)
 			ev_ok = ev_ok && cudaEventCreate(&h->ev_gs[k]) == cudaSuccess;
+		for(int k = 0; k < 2; ++k)
+			ev_ok = ev_ok && cudaEventCreate(&h->ev_pass[k]) == cudaSuccess;
 		if(!ev_ok || cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess ||
 		   cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess)
 		{
@@ -1182,6 +1195,9 @@ void citcom_gpu_destroy(citcom_gpu *h)
 	for(int k = 0; k < 8; ++k)
 		if(h->ev_gs[k])
 			cudaEventDestroy(h->ev_gs[k]);
+	for(int k = 0; k < 2; ++k)
+		if(h->ev_pass[k])
+			cudaEventDestroy(h->ev_pass[k]);
 	if(h->st)
 		cudaStreamDestroy(h->st);
 	delete h;
@@ -1257,6 +1273,7 @@ int citcom_gpu_solve_Ahat_p_fhat_device(citcom_gpu *h, double *dV, double *dP, c
 	h->stats.mg_passes = 0;
 	h->stats.smoother_ms = 0.0;
 	h->stats.smoother_sweeps = 0;
+	h->stats.pass_ms = 0.0;
 	CK(cudaEventRecord(h->ev0, h->st));
 	TRY(uzawa(h, dV, dP, dF, imp, steps_max, initial_residual));
 	CK(cudaEventRecord(h->ev1, h->st));

@@ -115,6 +115,7 @@ typedef struct citcom_gpu_stats
 	int warm_start;             /* 1: the attached network's guess started the Uzawa solve */
 	double warm_residual;       /* |F - K U - G P| / |F| of the network's guess */
 	double base_residual;       /* the same of the resident U, P it was compared with */
+	double pass_ms;             /* device time of the multigrid passes (multi_grid calls) */
 } citcom_gpu_stats;
 
 /* Allocates every device buffer the solver will use (on the current
