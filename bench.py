@@ -59,6 +59,16 @@ def workload(size: int):
                   viscE=(math.log(1e3),), viscT=(0.0,), accuracy=1e-6, piterations=375)
 
 
+def cfg2_workload():
+    """The 2 x 2 x 1 box of 128 x 128 x 64 elements, 6 multigrid levels,
+    eta = exp(-ln(1e4) T) times 30 below z = 0.8, Ra 1e6, internal heating
+    Q0 = 1."""
+    from citcomcu_gb300 import Config
+    return Config(mgunit=(4, 4, 2), levels=6, dimen=(2.0, 2.0, 1.0), rayleigh=1e6, Q0=1.0, tdepv=True,
+                  visc0=(1.0, 30.0), viscE=(math.log(1e4), math.log(1e4)), viscT=(0.0, 0.0), z_layer=(0.8,),
+                  accuracy=1e-6, piterations=375)
+
+
 def sphere_workload():
     """Regional spherical shell segment: colatitude 45-135 deg, longitude
     0-90 deg, radius 0.55-1.0, 192 x 192 x 96 elements, 6 multigrid levels,
@@ -387,6 +397,10 @@ def sphere_arm(args):
 
 
 def workload_name(case):
+    if case.dimen[0] == 2.0:
+        return (f"2x2x1 box, {case.nox - 1}x{case.noy - 1}x{case.noz - 1} Q1 elements, {case.levels} multigrid levels, "
+                "eta=exp(-ln(1e4) T) x30 below z=0.8, Ra=1e6, Q0=1, free slip, T0=1-z+U(-0.01,0.01) seed 0, "
+                "accuracy 1e-6, piterations 375")
     return (f"{case.nox - 1}^3 Q1 elements, {case.levels} multigrid levels, eta=exp(-ln(1e3) T), Ra=1e5, free slip, "
             f"T0=1-z+U(-0.01,0.01) seed 0, accuracy 1e-6, piterations 375")
 
@@ -407,8 +421,9 @@ def main():
     ap.add_argument("--learn-seeds", type=int, default=10)
     ap.add_argument("--learn-steps", type=int, default=4, help="time steps recorded after each seed's cold solve")
     ap.add_argument("--learn-adam", type=int, default=1000, help="Adam steps of the online training")
-    ap.add_argument("--workload", default="cube", choices=["cube", "sphere"],
-                    help="sphere: the 192x192x96 regional spherical segment instead of the headline box")
+    ap.add_argument("--workload", default="cube", choices=["cube", "sphere", "cfg2"],
+                    help="sphere: the 192x192x96 regional spherical segment; cfg2: the 128x128x64 box with a 10^4 "
+                         "contrast, instead of the headline 64^3 box")
     ap.add_argument("--piterations", type=int, default=375,
                     help="Uzawa iteration cap; lower values only for short profiling runs")
     args = ap.parse_args()
@@ -428,7 +443,7 @@ def main():
 
     import citcomcu_gb300 as cg
     cg.build()
-    case = workload(args.size)
+    case = cfg2_workload() if args.workload == "cfg2" else workload(args.size)
     case.piterations = args.piterations
     T0 = seeded_T0(case)
 
@@ -506,7 +521,9 @@ def main():
         "roofline": {"bound": "hbm", "kernel": "k_tile<float, 0> (finest-level Gauss-Seidel colour)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None,
-                     "traffic": TRAFFIC_PER_LAUNCH_64 if args.size == 64 else None,
+                     # the ncu capture at 64^3 scaled by the nodes of one colour launch (the
+                     # kernel's DRAM bytes per node do not depend on the level's size)
+                     "traffic": TRAFFIC_PER_LAUNCH_64 * nno / 274625 if nno >= 274625 else None,
                      "peak_kind": peak_kind, "bytes_per_launch": per_launch_bytes,
                      "launch_us": per_launch_s * 1e6},
         "clocks": clk.summary(),
@@ -531,7 +548,11 @@ def main():
         ln.close()
         ls.close()
     if not args.no_cpu:
-        line["cpu_baseline"] = cpu_sample(case, T0)
+        # full-solve pass count: the oracle's own count where it was measured,
+        # else the FP64 GPU path's (the same algorithm in 8 colours)
+        full = REF_FULL_SOLVE_PASSES.get(case.nox - 1) if args.workload == "cube" else int(np.mean(
+            [r["mg_passes"] for r in fp64]))
+        line["cpu_baseline"] = cpu_sample(case, T0, full_passes=full)
     print(json.dumps(line))
     return 0
 
