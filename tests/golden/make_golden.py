@@ -10,13 +10,21 @@ Fixtures
                    seeded conductive T0, accuracy 1e-8.  Operator probes on
                    every level plus 3 time steps (FP64-promoted build).
   cfg1_16.npz      16^3 elements, 3 levels, isoviscous, Ra 1e4, the deck's own
-                   sinusoidal IC, accuracy 1e-6, 5 steps (FP64-promoted build;
-                   per-step scalars from the stock float build alongside).
+                   sinusoidal IC, accuracy 1e-6, 50 steps (FP64-promoted build;
+                   per-step scalars from the stock float build alongside; the
+                   fields after steps 5 and 50).
   sdepv_box.npz    stress-dependent viscosity (SDEPV, rheology 2, n = 3,
                    transition strain rate 300) on a T-dependent base viscosity
                    exp(ln(100) (0 - T)), 9^3 nodes (3 levels), Ra 1e4, seeded T0
                    with +-0.05 noise, accuracy 1e-8, 3 time steps (FP64-promoted
                    build; the viscosity iteration of general_stokes_solver).
+  knobs_box.npz    the solver options away from their defaults: no augmented
+                   Lagrangian, no Uzawa preconditioner, mg_cycle 2 (W-like
+                   cycles), down_heavy 2, up_heavy 4, vlowstep 10, vhighstep
+                   2; two viscosity layers (x10 below z = 0.7) of
+                   exp(ln(100) (0 - T)) clamped to [0.05, 5]; 17^3 nodes (4
+                   levels), Ra 1e4, seeded T0, accuracy 1e-8, 3 time steps
+                   (FP64-promoted build).
   sphere_tdep.npz  Geometry=Rsphere: theta 45-135 deg, phi 0-90 deg, r 0.55-1.0,
                    9x13x9 nodes (mgunit 2,3,2; 3 levels), eta = exp(ln(100)
                    (0 - T)), Ra 1e4, seeded T0 (1 - (r - ri)/(ro - ri) plus
@@ -60,9 +68,16 @@ def sdepv_case() -> Case:
                 sdepv_rheology=2, sdepv_expt=(3.0,), sdepv_trns=(300.0,))
 
 
+def knobs_case() -> Case:
+    return Case(name="knobs_box", mgunit=(2, 2, 2), levels=4, rayleigh=1e4, tdepv=True, visc0=(1.0, 10.0),
+                viscE=(4.605170185988092, 4.605170185988092), viscT=(0.0, 0.0), z_layer=(0.7,), vmin=0.05,
+                vmax=5.0, aug_lagr=False, precond=False, mg_cycle=2, down_heavy=2, up_heavy=4, vlowstep=10,
+                vhighstep=2, accuracy=1e-8, maxstep=3)
+
+
 def cfg1_case() -> Case:
     return Case(name="cfg1_16", mgunit=(4, 4, 4), levels=3, rayleigh=1e4, accuracy=1e-6,
-                perturbmag=0.01, perturbk=1.0, maxstep=5)
+                perturbmag=0.01, perturbk=1.0, maxstep=50)
 
 
 OUTPUT_KEYS = ("Have", "surf", "heatflux", "heatflux_adv")
@@ -99,6 +114,13 @@ def main():
         keep.update(_steps(R, 3))
         np.savez_compressed(os.path.join(HERE, "sdepv_box.npz"), **keep)
 
+        c = knobs_case()
+        T0 = conductive_T0(c, amp=0.01, seed=2)
+        R = run_reference(c, os.path.join(tmp, "knobs"), nsteps=3, T0=T0)
+        keep = {"dims": R["dims"], "T0": R["T0"], "T0_input": T0}
+        keep.update(_steps(R, 3, keys=("T", "V1", "V2", "V3", "P")))
+        np.savez_compressed(os.path.join(HERE, "knobs_box.npz"), **keep)
+
         c = sphere_case()
         T0 = conductive_T0(c, amp=0.01, seed=0)
         R = run_reference(c, os.path.join(tmp, "sphere"), nsteps=3, T0=T0, probe=True)
@@ -109,16 +131,17 @@ def main():
         np.savez_compressed(os.path.join(HERE, "sphere_tdep.npz"), **keep)
 
         c = cfg1_case()
-        R = run_reference(c, os.path.join(tmp, "cfg1"), nsteps=5)
-        R32 = run_reference(c, os.path.join(tmp, "cfg1_32"), nsteps=5, precision="f32")
+        R = run_reference(c, os.path.join(tmp, "cfg1"), nsteps=50)
+        R32 = run_reference(c, os.path.join(tmp, "cfg1_32"), nsteps=50, precision="f32")
         keep = {"dims": R["dims"], "T0": R["T0"]}
-        for s in range(6):
+        for s in range(51):
             keep[f"s{s}_scalars"] = R[f"s{s}_scalars"]
             keep[f"s{s}_scalars_f32"] = R32[f"s{s}_scalars"]
-        for k in ("T", "V1", "V2", "V3", "P"):
-            keep[f"s5_{k}"] = R[f"s5_{k}"]
+        for st in (5, 50):
+            for k in ("T", "V1", "V2", "V3", "P"):
+                keep[f"s{st}_{k}"] = R[f"s{st}_{k}"]
         np.savez_compressed(os.path.join(HERE, "cfg1_16.npz"), **keep)
-    for f in ("small_tdep.npz", "cfg1_16.npz", "sphere_tdep.npz", "sdepv_box.npz"):
+    for f in ("small_tdep.npz", "cfg1_16.npz", "sphere_tdep.npz", "sdepv_box.npz", "knobs_box.npz"):
         print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")
 
 

@@ -223,24 +223,41 @@ def test_time_steps_match_reference_order_at_tight_tolerance(cg, olib):
 
 
 def test_cfg1_against_reference_fixture(cg):
-    """16^3 isoviscous Ra 1e4 at the reference's accuracy 1e-6: per-step Nu and
-    Vrms of the FP64 GPU path against the reference's own run (fixture)."""
+    """The CPU-runnable configuration (16^3 isoviscous, Ra 1e4, accuracy 1e-6)
+    over its 50 time steps: per-step Nu and Vrms of the FP64 GPU path against
+    the reference's own run (fixture), and T after steps 5 and 50.
+
+    The GPU relaxes in 8 colours, the reference lexicographically; both stop
+    at the same 1e-6 tolerance, so each step's solution differs at that level
+    and the difference is carried forward.  The oracle run in the GPU's
+    colour order drifts from the reference by at most 3.8e-6 (Nu), 2.5e-6
+    (Vrms) and 4.5e-6 (T after step 50); the bounds below are 2.5x those."""
     G = dict(np.load(os.path.join(GOLD, "cfg1_16.npz")))
     case = cfg1_case()
     s = cg.Solver(cg.Config.like(case))
     f = s.fine
     U, P, Tdot = np.zeros(f["neq"]), np.zeros(f["nel"]), np.zeros(f["nno"])
     T = G["T0"].copy()
-    for step in range(6):
+    worst = [0.0, 0.0]
+    for step in range(51):
         if step:
             s.PG_timestep(T, Tdot, V)
         V = s.general_stokes_solver(T, U, P)
         nut, _ = s.heat_flux(T, V)
+        vr = s.vrms(V)
         sc = G[f"s{step}_scalars"]
-        print(step, nut, sc[0], s.vrms(V), sc[2], s.stats()["uzawa"], sc[6] - 1)
-        assert abs(nut - sc[0]) < 2e-6 * abs(sc[0])
-        assert abs(s.vrms(V) - sc[2]) < 2e-5 * sc[2]
-    assert float(np.max(np.abs(T - G["s5_T"]))) < 1e-5
+        e_nu, e_vr = abs(nut - sc[0]) / abs(sc[0]), abs(vr - sc[2]) / sc[2]
+        worst = [max(worst[0], e_nu), max(worst[1], e_vr)]
+        if step in (0, 1, 5, 10, 25, 50):
+            print(f"step {step}: Nu {nut:.9f} ({sc[0]:.9f}) rel {e_nu:.1e}, Vrms {vr:.7f} ({sc[2]:.7f}) rel {e_vr:.1e}, "
+                  f"uzawa {s.stats()['uzawa']} ({int(sc[6]) - 1})")
+        assert e_nu < 1e-5 and e_vr < 1e-5, (step, e_nu, e_vr)
+        if step in (5, 50):
+            dT = float(np.max(np.abs(T - G[f"s{step}_T"])))
+            print(f"step {step}: max |dT| {dT:.1e}")
+            assert dT < (1e-5 if step == 5 else 1.2e-5)
+    print(f"drift over 50 steps: Nu {worst[0]:.1e}, Vrms {worst[1]:.1e}")
+    s.close()
 
 
 def test_mixed_precision_matches_fp64(cg):
