@@ -24,6 +24,12 @@ host buffers (pinned), the copies included.
 
   python bench.py [--steps K] [--warmup W] [--gpus N] [--impl reference]
                   [--size 64|32] [--no-cpu] [--no-learned]
+                  [--workload cube|cfg2|sphere]
+
+--workload cfg2 is the 2x2x1 box of 128x128x64 elements (10^4 contrast,
+Ra 1e6, Q0 1); --workload sphere the 192x192x96 regional spherical segment
+(10^5 contrast x30 below r 0.9, Ra 1e7; no CPU baseline: the oracle has no
+spherical geometry).  Both report the same fields as the headline.
 """
 from __future__ import annotations
 
@@ -356,47 +362,12 @@ def reference_arm(args):
     return 0
 
 
-def sphere_arm(args):
-    """The regional spherical segment (not the headline): cold solves of the
-    seeded state with the FP32 multigrid + FP64 refinement path."""
-    import torch
-    import citcomcu_gb300 as cg
-    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    cg.build()
-    case = sphere_workload()
-    case.piterations = args.piterations
-    T0 = seeded_T0_sphere(case)
-    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
-        recs, launches, res, nu, vr, energy_ms = run_mode(cg, case, cg.MIXED, T0, args.steps, args.warmup)
-    ms = float(np.mean([r["stokes_ms"] for r in recs]))
-    sweeps = sum(r["smoother_sweeps"] for r in recs)
-    sm_ms = sum(r["smoother_ms"] for r in recs)
-    per_launch_s = sm_ms * 1e-3 / max(8 * sweeps, 1)
-    per_launch_bytes = bytes_per_sweep(case.nno, 4) / 8.0
-    peak, peak_kind = peaks()
-    achieved = per_launch_bytes / per_launch_s / 1e9 if per_launch_s > 0 else None
-    line = {"metric": METRIC, "value": ms, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": ms + float(energy_ms), "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32+f64", "data": "synthetic",
-            "config": {"workload": "regional spherical shell segment, colatitude 45-135 deg, longitude 0-90 deg, r 0.55-1.0, "
-                                   f"{case.nox - 1}x{case.noy - 1}x{case.noz - 1} Q1 elements, {case.levels} multigrid levels, "
-                                   "eta=exp(-ln(1e5) T) x30 below r=0.9, Ra=1e7, conductive T0 + U(-0.01,0.01) seed 0, "
-                                   f"accuracy 1e-6, piterations {case.piterations}",
-                       "mode": "FP32 multigrid + FP64 refinement",
-                       "step": "cold Stokes solve of the seeded initial state (general_stokes_solver)"},
-            "uzawa_iterations": [r["uzawa"] for r in recs], "mg_passes": [r["mg_passes"] for r in recs],
-            "ms_per_mg_pass": ms / max(np.mean([r["mg_passes"] for r in recs]), 1),
-            "residuals_final": res, "nu_top": nu[0], "nu_bot": nu[1], "vrms": vr, "energy_ms": energy_ms,
-            "roofline": {"bound": "hbm", "kernel": "k_tile<float, 0> (finest-level Gauss-Seidel colour)",
-                         "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": (achieved / peak) if achieved else None, "traffic": None, "peak_kind": peak_kind,
-                         "bytes_per_launch": per_launch_bytes, "launch_us": per_launch_s * 1e6},
-            "clocks": clk.summary(), "gpu_launches": int(launches)}
-    print(json.dumps(line))
-    return 0
-
-
 def workload_name(case):
+    if case.sphere is not None:
+        return ("regional spherical shell segment, colatitude 45-135 deg, longitude 0-90 deg, r 0.55-1.0, "
+                f"{case.nox - 1}x{case.noy - 1}x{case.noz - 1} Q1 elements, {case.levels} multigrid levels, "
+                "eta=exp(-ln(1e5) T) x30 below r=0.9, Ra=1e7, conductive T0 + U(-0.01,0.01) seed 0, "
+                f"accuracy 1e-6, piterations {case.piterations}")
     if case.dimen[0] == 2.0:
         return (f"2x2x1 box, {case.nox - 1}x{case.noy - 1}x{case.noz - 1} Q1 elements, {case.levels} multigrid levels, "
                 "eta=exp(-ln(1e4) T) x30 below z=0.8, Ra=1e6, Q0=1, free slip, T0=1-z+U(-0.01,0.01) seed 0, "
@@ -429,8 +400,6 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
-    if args.workload == "sphere":
-        return sphere_arm(args)
 
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -443,9 +412,14 @@ def main():
 
     import citcomcu_gb300 as cg
     cg.build()
-    case = cfg2_workload() if args.workload == "cfg2" else workload(args.size)
+    if args.workload == "sphere":
+        case = sphere_workload()
+        T0_of = lambda sd: seeded_T0_sphere(case, sd)  # noqa: E731
+    else:
+        case = cfg2_workload() if args.workload == "cfg2" else workload(args.size)
+        T0_of = lambda sd: seeded_T0(case, sd)  # noqa: E731
     case.piterations = args.piterations
-    T0 = seeded_T0(case)
+    T0 = T0_of(0)
 
     def barrier():
         torch.cuda.synchronize()
@@ -464,7 +438,7 @@ def main():
         else:
             fp64, res_fp64, nu_fp64, vr_fp64 = mixed, res_mixed, nu_mixed, vr_mixed
         if not args.no_learned:
-            ls, ln, train_info = train_warm_start(cg, case, lambda sd: seeded_T0(case, sd), args.learn_seeds,
+            ls, ln, train_info = train_warm_start(cg, case, T0_of, args.learn_seeds,
                                                   args.learn_steps, args.learn_adam)
             t2 = time.perf_counter()
             lrecs, llaunches, res_l, nu_l, vr_l = run_learned(cg, case, T0, args.steps, args.warmup, ls, ln)
@@ -511,7 +485,8 @@ def main():
         "dtype": "f32+f64", "data": "synthetic",
         "config": {"workload": workload_name(case), "mode": mode + " (headline)",
                    "step": "cold Stokes solve of the seeded initial state (general_stokes_solver)",
-                   "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (FP32 stencils 267 MB, FP64 fine 535 MB)",
+                   "parallelism": f"replicas{world}", "l2": f"inputs larger than L2 (finest FP32 stencil {case.nno * 972 / 1e6:.0f} MB, FP64 "
+                         f"{case.nno * 1944 / 1e6:.0f} MB)",
                    "timing": "CUDA events around each Stokes solve inside the library, mean over timed steps"},
         "fp64_plain": {"stokes_ms_per_step": stokes_ms_fp64,
                        "uzawa_iterations": [r["uzawa"] for r in fp64], "mg_passes": [r["mg_passes"] for r in fp64],
@@ -547,7 +522,7 @@ def main():
     if learned:
         ln.close()
         ls.close()
-    if not args.no_cpu:
+    if not args.no_cpu and case.sphere is None:  # the oracle has no spherical geometry
         # full-solve pass count: the oracle's own count where it was measured,
         # else the FP64 GPU path's (the same algorithm in 8 colours)
         full = REF_FULL_SOLVE_PASSES.get(case.nox - 1) if args.workload == "cube" else int(np.mean(
