@@ -344,11 +344,18 @@ def reference_arm(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
-    case = workload(args.size)
+    if args.workload == "sphere":
+        print(json.dumps({"impl": "reference", "unavailable": "the spherical segment has no CPU port of the path "
+                                                               "(the oracle is Cartesian)"}))
+        return 0
+    case = cfg2_workload() if args.workload == "cfg2" else workload(args.size)
     T0 = seeded_T0(case)
+    # full-solve pass count of the 128x128x64 box: the FP64 GPU path's 788
+    # (the same algorithm in 8 colours; the oracle's own count is not measured)
+    full = 788 if args.workload == "cfg2" else None
     vals = []
     for i in range(args.warmup + args.steps):
-        r = cpu_sample(case, T0, uzawa_sample=2)
+        r = cpu_sample(case, T0, uzawa_sample=2, full_passes=full)
         if i >= args.warmup:
             vals.append(r["value"])
     v = float(np.mean(vals))
