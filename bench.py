@@ -19,7 +19,9 @@ seeds (1..10: each seed's cold solve and the 4 time steps after it, 50
 snapshots, 1000 Adam steps); the training time is reported, not timed into
 `value`.  The same solve without the network and the FP64 plain path are
 timed the same way and reported beside it; `ms_per_step` adds one SUPG time
-step (PG_timestep).  `e2e` times the headline solve through the C ABI with
+step (PG_timestep).  `time_loop` reports the reference's own loop as well:
+after one cold solve, PG_timestep and a Stokes solve warm from the previous
+step's U, P per step (mixed and FP64 plain, --loop-steps timed steps).  `e2e` times the headline solve through the C ABI with
 host buffers (pinned), the copies included.
 
   python bench.py [--steps K] [--warmup W] [--gpus N] [--impl reference]
@@ -257,6 +259,33 @@ def run_learned(cg, case, T0, steps, warmup, solver, net):
     return recs, launches, res, nu, vr
 
 
+def time_loop(cg, case, T0, precision, steps, warmup):
+    """The reference's time loop on resident state: one cold solve of the
+    seeded state, then per step PG_timestep and general_stokes_solver warm
+    from the previous step's U, P (step_resident).  Device time per step
+    (CUDA events inside the library), after `warmup` untimed steps."""
+    s = cg.Solver(cg.Config.like(case, precision=precision))
+    f = s.fine
+    s.load_state(T=T0, Tdot=np.zeros(f["nno"]), U=np.zeros(f["neq"]), P=np.zeros(f["nel"]))
+    s.stokes_resident()
+    t = 0.0
+    recs = []
+    for i in range(warmup + steps):
+        adv = s.step_resident(t)
+        t = adv["elapsed_time"]
+        if i >= warmup:
+            st = s.stats()
+            recs.append((st["stokes_ms"], st["energy_ms"], st["uzawa"], st["mg_passes"]))
+    nu = s.heat_flux()
+    vr = s.vrms()
+    s.close()
+    return {"steps": steps, "warmup": warmup,
+            "stokes_ms_per_step": float(np.mean([r[0] for r in recs])),
+            "ms_per_step": float(np.mean([r[0] + r[1] for r in recs])),
+            "uzawa_iterations": [r[2] for r in recs], "mg_passes": [r[3] for r in recs],
+            "nu_top": nu[0], "vrms": vr, "elapsed_time": t}
+
+
 def bytes_per_sweep(nno: int, word: int) -> int:
     """Algorithmic bytes of one Gauss-Seidel sweep (8 colour launches) on a
     level with stored 27-block stencils: the 243 coefficients and 3 inverse
@@ -402,6 +431,9 @@ def main():
     ap.add_argument("--workload", default="cube", choices=["cube", "sphere", "cfg2"],
                     help="sphere: the 192x192x96 regional spherical segment; cfg2: the 128x128x64 box with a 10^4 "
                          "contrast, instead of the headline 64^3 box")
+    ap.add_argument("--loop-steps", type=int, default=10,
+                    help="timed steps of the time-loop measurement (0: skip it)")
+    ap.add_argument("--loop-warmup", type=int, default=3)
     ap.add_argument("--piterations", type=int, default=375,
                     help="Uzawa iteration cap; lower values only for short profiling runs")
     args = ap.parse_args()
@@ -529,6 +561,16 @@ def main():
     if learned:
         ln.close()
         ls.close()
+    if args.loop_steps > 0:
+        # per time step as the reference's loop runs it: warm solves from the
+        # previous step (mixed path, and FP64 plain for comparison)
+        tl = {"mixed": time_loop(cg, case, T0, cg.MIXED, args.loop_steps, args.loop_warmup)}
+        if args.modes == "both":
+            tl["fp64_plain"] = time_loop(cg, case, T0, cg.FP64, args.loop_steps, args.loop_warmup)
+            tl["speedup_vs_fp64"] = tl["fp64_plain"]["ms_per_step"] / tl["mixed"]["ms_per_step"]
+            tl["nu_rel_err_vs_fp64"] = abs(tl["mixed"]["nu_top"] - tl["fp64_plain"]["nu_top"]) / abs(
+                tl["fp64_plain"]["nu_top"])
+        line["time_loop"] = tl
     if not args.no_cpu and case.sphere is None:  # the oracle has no spherical geometry
         # full-solve pass count: the oracle's own count where it was measured,
         # else the FP64 GPU path's (the same algorithm in 8 colours)

@@ -76,6 +76,7 @@ struct citcom_gpu
 	cudaStream_t st;
 	cudaEvent_t ev0, ev1;
 	cudaEvent_t ev_pass[2];  // brackets each multigrid pass
+	cudaEvent_t ev_energy[2];  // brackets the PG_timestep of step_resident
 	cudaEvent_t ev_gs[8];   // brackets the finest-level smoother calls inside a multigrid pass
 	int n_gs_pairs;         // pairs recorded by the captured pass
 	cudaGraphExec_t mg_exec;
@@ -1001,7 +1002,7 @@ int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 		for(int k = 0; k < 8; ++k)
 			ev_ok = ev_ok && cudaEventCreate(&h->ev_gs[k]) == cudaSuccess;
 		for(int k = 0; k < 2; ++k)
-			ev_ok = ev_ok && cudaEventCreate(&h->ev_pass[k]) == cudaSuccess;
+			ev_ok = ev_ok && cudaEventCreate(&h->ev_pass[k]) == cudaSuccess && cudaEventCreate(&h->ev_energy[k]) == cudaSuccess;
 		if(!ev_ok || cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess ||
 		   cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess)
 		{
@@ -1196,8 +1197,12 @@ void citcom_gpu_destroy(citcom_gpu *h)
 		if(h->ev_gs[k])
 			cudaEventDestroy(h->ev_gs[k]);
 	for(int k = 0; k < 2; ++k)
+	{
 		if(h->ev_pass[k])
 			cudaEventDestroy(h->ev_pass[k]);
+		if(h->ev_energy[k])
+			cudaEventDestroy(h->ev_energy[k]);
+	}
 	if(h->st)
 		cudaStreamDestroy(h->st);
 	delete h;
@@ -1413,7 +1418,9 @@ int citcom_gpu_stokes_resident(citcom_gpu *h)
 int citcom_gpu_step_resident(citcom_gpu *h, citcom_gpu_advection *adv)
 {
 	TRY(check_handle(h));
-	cudaEvent_t a = h->ev_gs[6], b = h->ev_gs[7];
+	// events of their own: the multigrid graph re-records the smoother and pass
+	// events during the solve that follows
+	cudaEvent_t a = h->ev_energy[0], b = h->ev_energy[1];
 	CK(cudaEventRecord(a, h->st));
 	TRY(pg_timestep(h, adv));
 	CK(cudaEventRecord(b, h->st));
