@@ -167,6 +167,24 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def max_over_ranks(values, world: int, device: str = "cuda"):
+    """The per-rank times reduced to their maximum over the replicas (a
+    replica run is as slow as its slowest rank); identity for one rank."""
+    if world <= 1:
+        return [float(v) for v in values]
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v) for v in values], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t.tolist()]
+
+
+def whole_job_value(ms_per_step_max: float, world: int) -> float:
+    """Whole-job ms per step of N replicas that each ran the same steps in
+    the same wall time: N steps complete per step time."""
+    return ms_per_step_max / max(world, 1)
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -490,12 +508,8 @@ def main():
     head = learned[0] if learned else mixed
     stokes_ms = float(np.mean([r["stokes_ms"] for r in head]))
     step_ms = stokes_ms + float(energy_ms)
-    if world > 1:
-        t = torch.tensor([stokes_ms, step_ms], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        stokes_ms, step_ms = float(t[0]), float(t[1])
-    # whole job: N replicas each ran `steps` steps in the same wall time
-    value = stokes_ms / world
+    stokes_ms, step_ms = max_over_ranks([stokes_ms, step_ms], world)
+    value = whole_job_value(stokes_ms, world)
 
     # dominant kernel: finest-level FP32 Gauss-Seidel colour launches, timed live
     nno = case.nno
