@@ -1440,14 +1440,25 @@ int citcom_gpu_output_async(citcom_gpu *h, const citcom_gpu_output *o)
 	const int lmax = h->L - 1;
 	const Lvl &Lf = h->lv[lmax];
 	const size_t nno = Lf.nno, nel = Lf.nel, noz = Lf.noz, nsf = (size_t)Lf.nox * Lf.noy;
-	if(!h->snap)
+	// created on first use, each on its own so that a failed call leaves
+	// nothing half made
+	if(!h->st_out && cudaStreamCreateWithFlags(&h->st_out, cudaStreamNonBlocking) != cudaSuccess)
 	{
-		TRY(dalloc(h, &h->snap, 8 * nno + 4 * nel + 6 * noz + 2 * nsf + 9));
-		if(cudaStreamCreateWithFlags(&h->st_out, cudaStreamNonBlocking) != cudaSuccess ||
-		   cudaEventCreateWithFlags(&h->ev_snap, cudaEventDisableTiming) != cudaSuccess ||
-		   cudaEventCreateWithFlags(&h->ev_out, cudaEventDisableTiming) != cudaSuccess)
-			return fail(h, CITCOM_GPU_ERR_CUDA, "output stream/event creation failed");
+		h->st_out = nullptr;
+		return fail(h, CITCOM_GPU_ERR_CUDA, "output stream creation failed");
 	}
+	if(!h->ev_snap && cudaEventCreateWithFlags(&h->ev_snap, cudaEventDisableTiming) != cudaSuccess)
+	{
+		h->ev_snap = nullptr;
+		return fail(h, CITCOM_GPU_ERR_CUDA, "output event creation failed");
+	}
+	if(!h->ev_out && cudaEventCreateWithFlags(&h->ev_out, cudaEventDisableTiming) != cudaSuccess)
+	{
+		h->ev_out = nullptr;
+		return fail(h, CITCOM_GPU_ERR_CUDA, "output event creation failed");
+	}
+	if(!h->snap)
+		TRY(dalloc(h, &h->snap, 8 * nno + 4 * nel + 6 * noz + 2 * nsf + 9));
 	double *sT = h->snap, *sV = sT + nno, *sP = sV + 3 * nno, *f = sP + nel, *scratch = f + 3 * nno, *ue = scratch + nno;
 	double *H = ue + 3 * nel, *surf = H + 6 * noz, *sums = surf + 2 * nsf, *scal = sums + 6;
 	// the staging must not change under a host copy still in flight
