@@ -69,3 +69,29 @@ def test_config_like_copies_case_fields():
     k = cg.Config.like(c, precision=cg.MIXED)
     assert k.mgunit == (2, 3, 2) and k.levels == 4 and k.rayleigh == 1e5 and k.tdepv
     assert k.visc0 == (1.0, 30.0) and k.z_layer == (0.8,) and k.precision == cg.MIXED
+
+
+def test_header_is_plain_c_and_links(lib, tmp_path):
+    """CitcomCU is C: a C99 translation unit that includes the header, takes
+    the address of every entry point and calls the ones that need no device
+    (argument checks) compiles with gcc -std=c99 -Wall -Werror, links against
+    the library and runs."""
+    import citcomcu_gb300 as cg
+    syms = header_symbols()
+    src = ["#include <stdio.h>", '#include "citcom_gb300.h"', "int main(void)", "{",
+           "\tconst void *p[] = {" + ", ".join(f"(const void *){s}" for s in syms) + "};",
+           "\tcitcom_gpu_config c = {0};", "\tcitcom_gpu *h = 0;",
+           "\tint rc = citcom_gpu_create(&c, &h);  /* levels = 0: rejected before any device call */",
+           "\tif(rc != CITCOM_GPU_ERR_ARG || h) return 1;",
+           "\tif(citcom_gpu_output_async(0, 0) != CITCOM_GPU_ERR_ARG) return 2;",
+           "\tprintf(\"ok %d\\n\", (int)(sizeof(p) / sizeof(p[0])));", "\treturn 0;", "}"]
+    c_file = tmp_path / "abi_check.c"
+    c_file.write_text("\n".join(src) + "\n")
+    exe = tmp_path / "abi_check"
+    libdir = os.path.dirname(cg.LIB_PATH)
+    name = os.path.basename(cg.LIB_PATH)[3:-3]
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), str(c_file), "-o", str(exe),
+                    f"-L{libdir}", f"-l{name}", f"-Wl,-rpath,{libdir}"], check=True, capture_output=True, text=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0, (out.returncode, out.stdout, out.stderr)
+    assert out.stdout.strip() == f"ok {len(syms)}"
