@@ -63,10 +63,14 @@ def build(quiet: bool = True) -> str:
     return LIB_PATH
 
 
+# the unchanged reference's sources, where they exist (the build container)
+REF_SRC = "/root/reference/src"
+
+
 def build_reference(quiet: bool = True) -> bool:
     """Compile the unchanged reference into oracle/_ref when its sources are
     present (this container); returns False where they are absent."""
-    if not os.path.isdir("/root/reference/src"):
+    if not os.path.isdir(REF_SRC):
         return False
     subprocess.run(["make", "-s", "-j8", "-C", os.path.join(HERE, "ref")], check=True,
                    stdout=subprocess.DEVNULL if quiet else None,
