@@ -948,17 +948,29 @@ template <typename T> int alloc_mg(citcom_gpu *h, MG<T> &B)
 
 extern "C" {
 
+// why the last citcom_gpu_create of the process failed (no handle to hold it)
+static char g_create_err[256];
+
+static int create_failed(int r, const char *msg)
+{
+	snprintf(g_create_err, sizeof(g_create_err), "%s", msg);
+	return r;
+}
+
 int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 {
 	if(!cfg || !out)
-		return CITCOM_GPU_ERR_ARG;
+		return create_failed(CITCOM_GPU_ERR_ARG, "null argument");
 	*out = nullptr;
 	if(cfg->levels < 1 || cfg->levels > CITCOM_MAX_LEVELS || cfg->mgunit[0] < 1 || cfg->mgunit[1] < 1 || cfg->mgunit[2] < 1 ||
 	   cfg->precision < CITCOM_GPU_FP64 || cfg->precision > CITCOM_GPU_MIXED || cfg->num_mat < 1 || cfg->num_mat > 8)
-		return CITCOM_GPU_ERR_ARG;
+		return create_failed(CITCOM_GPU_ERR_ARG, "invalid configuration (levels, mgunit, precision or num_mat)");
 	int ndev = 0;
 	if(cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1)
-		return CITCOM_GPU_ERR_CUDA;
+	{
+		cudaGetLastError();
+		return create_failed(CITCOM_GPU_ERR_CUDA, "no usable CUDA device (there is no CPU fallback)");
+	}
 	citcom_gpu *h = new citcom_gpu();
 	memset(h->err, 0, sizeof(h->err));
 	h->cfg = *cfg;
@@ -1156,6 +1168,7 @@ int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 	*out = h;
 	return CITCOM_GPU_OK;
 failed:
+	create_failed(r, h->err);
 	citcom_gpu_destroy(h);
 	return r;
 }
@@ -1208,7 +1221,12 @@ void citcom_gpu_destroy(citcom_gpu *h)
 	delete h;
 }
 
-const char *citcom_gpu_error_string(const citcom_gpu *h) { return h ? h->err : "null handle"; }
+const char *citcom_gpu_error_string(const citcom_gpu *h)
+{
+	if(h)
+		return h->err;
+	return g_create_err[0] ? g_create_err : "null handle";
+}
 
 int citcom_gpu_level_dims(const citcom_gpu *h, int lev, int dims[6])
 {

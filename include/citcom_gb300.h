@@ -16,7 +16,8 @@
  * *_device variants take device pointers and do no host traffic.
  *
  * Every function returns CITCOM_GPU_OK (0) or a negative error code; the
- * message is available from citcom_gpu_error_string().  Setting the
+ * message is available from citcom_gpu_error_string() (with a null handle:
+ * the reason the last citcom_gpu_create of the process failed).  Setting the
  * environment variable CITCOM_GPU_VERBOSE=1 prints one line per Uzawa
  * iteration in the spirit of the reference's generate_log_message;
  * CITCOM_GPU_NO_GRAPH=1 launches the multigrid pass kernel by kernel instead
@@ -26,7 +27,8 @@
  * the handle is destroyed.  There is no CPU
  * fallback: without a usable CUDA device citcom_gpu_create fails.
  *
- * Scope: Cartesian box, uniform spacing per axis on every multigrid level,
+ * Scope: the Cartesian box with uniform spacing per axis on every multigrid
+ * level, or the regional spherical shell segment (Geometry=Rsphere);
  * free-slip walls (the reference's default reflecting sides), T fixed at the
  * top (0) and bottom (1), insulating sides, one device.
  */
