@@ -61,6 +61,11 @@ struct oracle
 	/* solve_Ahat_p_fhat work (Stokes_flow_Incomp.c:323-336) */
 	double *r0, *r1, *r2, *z0, *z1, *s1, *s2, *Ah, *u1;
 	double *gs_tmp;
+	/* stress-dependent viscosity: the previous solution of the viscosity
+	   iteration (static oldU of general_stokes_solver), the element strain
+	   rates, and how often visc_from_S ran (its static `visits`) */
+	double *oldU, *edot;
+	int sdepv_visits;
 };
 
 static void *xcalloc(size_t n, size_t s)
@@ -277,6 +282,8 @@ oracle *oracle_create(const oracle_params *p)
 		o->Ah = (double *)xcalloc(f->neq + 2, sizeof(double));
 		o->u1 = (double *)xcalloc(f->neq + 2, sizeof(double));
 		o->gs_tmp = (double *)xcalloc(f->neq + 2, sizeof(double));
+		o->oldU = (double *)xcalloc(f->neq + 2, sizeof(double));
+		o->edot = (double *)xcalloc(f->nel + 1, sizeof(double));
 	}
 	setup_geometry(o);
 	setup_flags(o);
@@ -339,6 +346,8 @@ void oracle_destroy(oracle *o)
 	free(o->Ah);
 	free(o->u1);
 	free(o->gs_tmp);
+	free(o->oldU);
+	free(o->edot);
 	free(o);
 }
 
@@ -451,8 +460,74 @@ void oracle_assemble_forces(oracle *o)
 
 /* ------------------------------------------------------------- viscosity */
 
+/* strain_rate_2_inv (Viscosity_structures.c:979-1086), Cartesian branch
+ * (:1042-1075) with SQRT: per element the symmetric velocity gradient at the
+ * centre from V, edot = sqrt(0.5 (e11^2 + e22^2 + e33^2 + 2 e12^2 + 2 e13^2
+ * + 2 e23^2)) */
+static void strain_rate(oracle *o, double *edot)
+{
+	const level *f = &o->lv[o->L - 1];
+	int e, a, p, q, n[8];
+	for(e = 0; e < f->nel; e++)
+	{
+		double du[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, ed[3][3];
+		elem_nodes(f, e, n);
+		for(a = 0; a < 8; a++)
+			for(p = 0; p < 3; p++)
+				for(q = 0; q < 3; q++)
+					du[p][q] += o->V[p][n[a]] * f->gnxc[a][q];
+		for(p = 0; p < 3; p++)
+			for(q = 0; q < 3; q++)
+				ed[p][q] = 0.5 * (du[p][q] + du[q][p]);
+		edot[e] = sqrt(0.5 * (ed[0][0] * ed[0][0] + ed[0][1] * ed[0][1] * 2.0 + ed[1][1] * ed[1][1] +
+		                      ed[1][2] * ed[1][2] * 2.0 + ed[2][2] * ed[2][2] + ed[0][2] * ed[0][2] * 2.0));
+	}
+}
+
+/* visc_from_S (Viscosity_structures.c:744-846), rheologies 1 and 2: with
+ * s = (2 edot / trns)^(1 - 1/n) of the element's material, eta <- 2 eta /
+ * (1 + s eta^(1-1/n)) (1) or eta <- eta / (1 + s eta^(1-1/n)) where the
+ * Gauss-point temperature is below the transition temperature (2; the
+ * reference's default transition values 3000 for T and 2 for the absent
+ * composition are always above).  The first visit without a restart uses a
+ * unit strain rate (:787-790). */
+static void visc_from_S(oracle *o)
+{
+	level *f = &o->lv[o->L - 1];
+	int e, k, a, n[8];
+	if(o->sdepv_visits == 0)
+		for(e = 0; e < f->nel; e++)
+			o->edot[e] = 1.0;
+	else
+		strain_rate(o, o->edot);
+	for(e = 0; e < f->nel; e++)
+	{
+		const int m = o->mat[e];
+		const double e1 = 1.0 - 1.0 / o->p.sdepv_expt[m];
+		const double scale = pow(2.0 * o->edot[e] / o->p.sdepv_trns[m], e1);
+		elem_nodes(f, e, n);
+		for(k = 0; k < 8; k++)
+		{
+			double v = f->evi[8 * e + k];
+			if(o->p.sdepv_rheology == 1)
+				v = 2.0 * v / (1.0 + scale * pow(v, e1));
+			else
+			{
+				double t = 0.0;
+				for(a = 0; a < 8; a++)
+					t += (o->T[n[a]] > 0.0 ? o->T[n[a]] : 0.0) * o->Nv[k][a];
+				if(t < 3000.0)
+					v = v / (1.0 + scale * pow(v, e1));
+			}
+			f->evi[8 * e + k] = v;
+		}
+	}
+	o->sdepv_visits++;
+}
+
 /* get_system_viscosity (Viscosity_structures.c:369-455): visc_from_T rheol 3
- * (:617-646) when TDEPV, else visc_from_mat (:477-489); then VMAX/VMIN */
+ * (:617-646) when TDEPV, else visc_from_mat (:477-489); visc_from_S when
+ * SDEPV; then VMAX/VMIN (:414-427) */
 void oracle_get_system_viscosity(oracle *o)
 {
 	level *f = &o->lv[o->L - 1];
@@ -473,12 +548,17 @@ void oracle_get_system_viscosity(oracle *o)
 			}
 			else
 				v = o->p.visc0[m];
-			if(o->p.vmax_on && v > o->p.vmax)
-				v = o->p.vmax;
-			if(o->p.vmin_on && v < o->p.vmin)
-				v = o->p.vmin;
 			f->evi[8 * e + k] = v;
 		}
+	}
+	if(o->p.sdepv)
+		visc_from_S(o);
+	for(e = 0; e < 8 * f->nel; e++)
+	{
+		if(o->p.vmax_on && f->evi[e] > o->p.vmax)
+			f->evi[e] = o->p.vmax;
+		if(o->p.vmin_on && f->evi[e] < o->p.vmin)
+			f->evi[e] = o->p.vmin;
 	}
 }
 
@@ -1104,28 +1184,59 @@ double oracle_solve_Ahat_p_fhat(oracle *o, double *V, double *P, const double *F
 	return residual;
 }
 
-/* general_stokes_solver (Drive_solvers.c:45-165) for a Newtonian rheology,
- * with construct_stiffness_B_matrix (Construct_arrays.c:834-889) and
- * solve_constrained_flow_iterative / v_from_vector (Stokes_flow_Incomp.c:50-90, 530-553) */
+/* general_stokes_solver (Drive_solvers.c:45-165), with
+ * construct_stiffness_B_matrix (Construct_arrays.c:834-889) and
+ * solve_constrained_flow_iterative / v_from_vector (Stokes_flow_Incomp.c:50-90,
+ * 530-553).  With SDEPV the viscosity, operator and solve repeat
+ * (:120-159): after each solve U <- a U + (1 - a) oldU (damping a =
+ * sdepv_iter_damp, when it is not 1), then |U - oldU| / |U| is the misfit and
+ * oldU <- U, until the misfit is at most sdepv_misfit or max_sdep_visc_iter
+ * solves ran.  *steps, *del2_calls and *mg_calls add up over the solves. */
 double oracle_stokes(oracle *o, int *steps, int *del2_calls, int *mg_calls)
 {
 	const level *f = &o->lv[o->L - 1];
-	double r;
-	int n, d;
+	const int iterate = o->p.sdepv != 0;
+	double r = 0.0, misfit = 0.0;
+	int n, d, i, count = 0, total_steps = 0, total_del2 = 0, total_mg = 0;
 	for(n = 0; n < f->nno; n++)
 		for(d = 0; d < 3; d++)
 			if(f->vflag[n] & (1u << d))
 				o->U[3 * n + d] = 0.0;
 	oracle_assemble_forces(o);
-	if(o->p.tdepv)
-		oracle_get_system_viscosity(o);
-	oracle_project_viscosity(o);
-	oracle_construct_stiffness(o);
-	*steps = o->p.piterations;
-	r = oracle_solve_Ahat_p_fhat(o, o->U, o->P, o->F, o->p.accuracy, steps, del2_calls, mg_calls);
-	for(n = 0; n < f->nno; n++)
-		for(d = 0; d < 3; d++)
-			o->V[d][n] = (f->vflag[n] & (1u << d)) ? 0.0 : o->U[3 * n + d];
+	do
+	{
+		int st = o->p.piterations, dc = 0, mc = 0;
+		if(o->p.tdepv || o->p.sdepv)
+			oracle_get_system_viscosity(o);
+		oracle_project_viscosity(o);
+		oracle_construct_stiffness(o);
+		r = oracle_solve_Ahat_p_fhat(o, o->U, o->P, o->F, o->p.accuracy, &st, &dc, &mc);
+		total_steps += st;
+		total_del2 += dc;
+		total_mg += mc;
+		for(n = 0; n < f->nno; n++)
+			for(d = 0; d < 3; d++)
+				o->V[d][n] = (f->vflag[n] & (1u << d)) ? 0.0 : o->U[3 * n + d];
+		count++;
+		if(iterate)
+		{
+			const double a = o->p.sdepv_iter_damp;
+			double uu = 0.0, dd = 0.0;
+			for(i = 0; i < f->neq; i++)
+			{
+				if(fabs(a - 1.0) > 1e-7)
+					o->U[i] = a * o->U[i] + (1.0 - a) * o->oldU[i];
+				const double du = o->U[i] - o->oldU[i];
+				o->oldU[i] = o->U[i];
+				uu += o->U[i] * o->U[i];
+				dd += du * du;
+			}
+			misfit = uu != 0.0 ? sqrt(dd) / sqrt(uu) : sqrt(dd);
+		}
+	} while(iterate && misfit > o->p.sdepv_misfit && count < o->p.max_sdep_visc_iter);
+	*steps = total_steps;
+	*del2_calls = total_del2;
+	*mg_calls = total_mg;
 	return r;
 }
 

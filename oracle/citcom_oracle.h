@@ -43,6 +43,12 @@ typedef struct oracle_params
 	int adv_sub_iterations;
 	double finetunedt, fixed_timestep;
 	int gs_colored;        /* 0: lexicographic (reference order); 1: 8-colour */
+	/* stress-dependent viscosity (SDEPV, Viscosity_structures.c:744-846) and
+	   the viscosity iteration of general_stokes_solver (Drive_solvers.c:120-159) */
+	int sdepv, sdepv_rheology;
+	double sdepv_expt[ORACLE_MAX_MAT], sdepv_trns[ORACLE_MAX_MAT];
+	double sdepv_misfit, sdepv_iter_damp;
+	int max_sdep_visc_iter;
 } oracle_params;
 
 typedef struct oracle oracle;

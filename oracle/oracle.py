@@ -53,6 +53,13 @@ class _Params(ctypes.Structure):
         ("finetunedt", ctypes.c_double),
         ("fixed_timestep", ctypes.c_double),
         ("gs_colored", ctypes.c_int),
+        ("sdepv", ctypes.c_int),
+        ("sdepv_rheology", ctypes.c_int),
+        ("sdepv_expt", ctypes.c_double * MAXM),
+        ("sdepv_trns", ctypes.c_double * MAXM),
+        ("sdepv_misfit", ctypes.c_double),
+        ("sdepv_iter_damp", ctypes.c_double),
+        ("max_sdep_visc_iter", ctypes.c_int),
     ]
 
 
@@ -173,6 +180,17 @@ def params_from_case(case, gs_colored: bool = False) -> _Params:
     p.finetunedt = case.finetunedt
     p.fixed_timestep = case.fixed_timestep
     p.gs_colored = int(gs_colored)
+    p.sdepv = int(getattr(case, "sdepv", False))
+    if p.sdepv:
+        p.sdepv_rheology = case.sdepv_rheology
+        ex = (list(case.sdepv_expt) * p.num_mat)[:p.num_mat]
+        tr = (list(case.sdepv_trns) * p.num_mat)[:p.num_mat]
+        for i in range(p.num_mat):
+            p.sdepv_expt[i] = ex[i]
+            p.sdepv_trns[i] = tr[i]
+        p.sdepv_misfit = case.sdepv_misfit
+        p.sdepv_iter_damp = case.sdepv_iter_damp
+        p.max_sdep_visc_iter = case.max_sdep_visc_iter
     return p
 
 

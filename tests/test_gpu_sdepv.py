@@ -47,3 +47,36 @@ def test_sdepv_time_steps_against_reference():
         assert abs(nut - sc[0]) < 1e-6 * abs(sc[0]) and abs(nub - sc[1]) < 1e-6 * abs(sc[1])
         assert abs(vr - sc[2]) < 1e-6 * sc[2]
     s.close()
+
+
+def test_sdepv_against_the_coloured_oracle():
+    """The same run against the oracle in the GPU's own 8-colour order (the
+    same arithmetic, summation order aside): per step the same total Uzawa
+    count, U to 1e-8 and Nu to 1e-9."""
+    import citcomcu_gb300 as cg
+    from oracle.oracle import Oracle
+    cg.build()
+    G = dict(np.load(os.path.join(GOLD, "sdepv_box.npz")))
+    case = sdepv_case()
+    s = cg.Solver(cg.Config.like(case))
+    f = s.fine
+    s.get_system_viscosity(G["T0"])
+    o = Oracle(case, gs_colored=True)
+    o.set_T(G["T0_input"])
+    o.thermal_buoyancy()
+    o.viscosity()
+    U, P, Tdot = np.zeros(f["neq"]), np.zeros(f["nel"]), np.zeros(f["nno"])
+    T = G["T0"].copy()
+    for step in range(4):
+        if step:
+            s.PG_timestep(T, Tdot, V)
+            o.pg_timestep()
+        V = s.general_stokes_solver(T, U, P)
+        info = o.stokes()
+        nut, _ = s.heat_flux(T, V)
+        onut, _ = o.heat_flux()
+        eU = rel(U, o.U()[: f["neq"]])
+        print(step, s.stats()["uzawa"], info["uzawa"], f"U {eU:.2e} Nu {abs(nut - onut):.2e}")
+        assert s.stats()["uzawa"] == info["uzawa"]
+        assert eU < 1e-8 and abs(nut - onut) < 1e-9 * abs(onut)
+    s.close()

@@ -150,3 +150,30 @@ def test_solver_options_run(oracle_lib):
         assert abs(nut - sc[0]) < 1e-12 * abs(sc[0])
         assert abs(o.vrms() - sc[2]) < 1e-12 * sc[2]
         assert float(np.max(np.abs(o.T() - G[f"s{s}_T"]))) < 1e-13
+
+
+def test_sdepv_run(oracle_lib):
+    """Stress-dependent viscosity (rheology 2, n = 3, transition strain rate
+    300) with the viscosity iteration of general_stokes_solver, 3 time steps
+    (tests/golden/sdepv_box.npz): the oracle in the reference's order against
+    the reference's run, to rounding.  As in the reference driver, the
+    viscosity is computed once from T0 before the first solve; that call is
+    visc_from_S's first visit (unit strain rate), so the first solve already
+    uses the strain rate of V = 0."""
+    from tests.golden.make_golden import sdepv_case
+    G = dict(np.load(os.path.join(GOLD, "sdepv_box.npz")))
+    o = oracle_lib.Oracle(sdepv_case())
+    o.set_T(G["T0_input"])
+    o.thermal_buoyancy()
+    o.viscosity()
+    for s in range(4):
+        if s:
+            o.pg_timestep()
+        info = o.stokes()
+        nut, _ = o.heat_flux()
+        sc = G[f"s{s}_scalars"]
+        assert info["del2_calls"] == int(sc[6]), (s, info)
+        assert abs(nut - sc[0]) < 1e-12 * abs(sc[0])
+        assert abs(o.vrms() - sc[2]) < 1e-12 * sc[2]
+        assert rel(o.U()[: len(G[f"s{s}_U"])], G[f"s{s}_U"]) < 1e-12
+        assert float(np.max(np.abs(o.T() - G[f"s{s}_T"]))) < 1e-13
