@@ -656,7 +656,10 @@ __global__ void __launch_bounds__(CO_THREADS) k_coarse(const __grid_constant__ C
 			int lo, cnt;
 			co_chunk(L.nno, rank, ncta, lo, cnt);
 			for(int n = lo + threadIdx.x; n < lo + cnt; n += blockDim.x)
-				interp_node<false, float>(D.L[l - 1], L, D.geo[l], sv, D.vec[l][op.b], n);
+				if(L.sphere)
+					interp_node<false, true, float>(D.L[l - 1], L, D.geo[l], sv, D.vec[l][op.b], n);
+				else
+					interp_node<false, false, float>(D.L[l - 1], L, D.geo[l], sv, D.vec[l][op.b], n);
 			halo_lev = -1;
 			break;
 		}

@@ -151,17 +151,19 @@ __device__ __forceinline__ void project_lanes(const Lvl &Lf, const Lvl &Lc, cons
 // fill weights are x2 / (x1 + x2), x1 / (x1 + x2) with x1, x2 the sizes (along
 // the fill) of the first elements of the two neighbours (element index order:
 // corner (max(X-1, 0), ., max(Z-1, 0))): 1/2 on the box; in the sphere the
-// theta and r sizes of an element depend on its column.
+// theta and r sizes of an element depend on its column.  SPH selects the
+// spherical weights at compile time (the box variant then holds no geometry
+// reads: 65 instead of 92 registers).
 template <bool CG, typename T> __device__ __forceinline__ T coarse_at(const Lvl &Lc, const T *AD, int x, int y, int z, int d)
 {
 	return ldv<CG>(AD + 3 * cg_node(Lc, x >> 1, y >> 1, z >> 1) + d);
 }
-template <bool CG, typename T>
+template <bool CG, bool SPH, typename T>
 __device__ __forceinline__ T fill_x(const Lvl &Lc, const Lvl &Lf, const Geo *gf, const T *AD, int x, int y, int z, int d)
 {
 	if(x & 1)
 	{
-		if(Lf.sphere)
+		if(SPH)
 		{
 			const int ez = z > 0 ? z - 1 : 0;
 			const double x1 = gf[cg_col(Lf, x >= 2 ? x - 2 : 0, ez)].size[0], x2 = gf[cg_col(Lf, x, ez)].size[0];
@@ -172,24 +174,24 @@ __device__ __forceinline__ T fill_x(const Lvl &Lc, const Lvl &Lf, const Geo *gf,
 	}
 	return coarse_at<CG>(Lc, AD, x, y, z, d);
 }
-template <bool CG, typename T>
+template <bool CG, bool SPH, typename T>
 __device__ __forceinline__ T fill_z(const Lvl &Lc, const Lvl &Lf, const Geo *gf, const T *AD, int x, int y, int z, int d)
 {
 	if(z & 1)
 	{
-		if(Lf.sphere)
+		if(SPH)
 		{
 			const int ex = x > 0 ? x - 1 : 0;
 			const double x1 = gf[cg_col(Lf, ex, z >= 2 ? z - 2 : 0)].size[2], x2 = gf[cg_col(Lf, ex, z)].size[2];
-			return (T)(x2 / (x1 + x2)) * fill_x<CG>(Lc, Lf, gf, AD, x, y, z - 1, d) +
-			       (T)(x1 / (x1 + x2)) * fill_x<CG>(Lc, Lf, gf, AD, x, y, z + 1, d);
+			return (T)(x2 / (x1 + x2)) * fill_x<CG, SPH>(Lc, Lf, gf, AD, x, y, z - 1, d) +
+			       (T)(x1 / (x1 + x2)) * fill_x<CG, SPH>(Lc, Lf, gf, AD, x, y, z + 1, d);
 		}
-		return (T)0.5 * fill_x<CG>(Lc, Lf, gf, AD, x, y, z - 1, d) + (T)0.5 * fill_x<CG>(Lc, Lf, gf, AD, x, y, z + 1, d);
+		return (T)0.5 * fill_x<CG, SPH>(Lc, Lf, gf, AD, x, y, z - 1, d) + (T)0.5 * fill_x<CG, SPH>(Lc, Lf, gf, AD, x, y, z + 1, d);
 	}
-	return fill_x<CG>(Lc, Lf, gf, AD, x, y, z, d);
+	return fill_x<CG, SPH>(Lc, Lf, gf, AD, x, y, z, d);
 }
 // the y fill's two neighbours share their first element's (x, z) column: 1/2
-template <bool CG, typename T>
+template <bool CG, bool SPH, typename T>
 __device__ __forceinline__ void interp_node(const Lvl &Lc, const Lvl &Lf, const Geo *gf, const T *AD, T *AU, int n)
 {
 	const int z = n % Lf.noz, x = (n / Lf.noz) % Lf.nox, y = n / (Lf.noz * Lf.nox);
@@ -199,9 +201,9 @@ __device__ __forceinline__ void interp_node(const Lvl &Lc, const Lvl &Lf, const 
 	{
 		T v;
 		if(y & 1)
-			v = (T)0.5 * fill_z<CG>(Lc, Lf, gf, AD, x, y - 1, z, d) + (T)0.5 * fill_z<CG>(Lc, Lf, gf, AD, x, y + 1, z, d);
+			v = (T)0.5 * fill_z<CG, SPH>(Lc, Lf, gf, AD, x, y - 1, z, d) + (T)0.5 * fill_z<CG, SPH>(Lc, Lf, gf, AD, x, y + 1, z, d);
 		else
-			v = fill_z<CG>(Lc, Lf, gf, AD, x, y, z, d);
+			v = fill_z<CG, SPH>(Lc, Lf, gf, AD, x, y, z, d);
 		AU[3 * n + d] = ((f >> d) & 1u) ? (T)0 : v;
 	}
 }

@@ -705,13 +705,13 @@ __global__ void k_project(Lvl Lf, Lvl Lc, const Geo *__restrict__ gc, const T *_
 	project_lanes<false, T, T>(Lf, Lc, gc, AU, AD, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
-template <typename T>
+template <typename T, bool SPH>
 __global__ void k_interp(Lvl Lc, Lvl Lf, const Geo *__restrict__ gf, const T *__restrict__ AD, T *__restrict__ AU)
 {
 	pdl_begin();
 	const int n = blockIdx.x * blockDim.x + threadIdx.x;
 	if(n < Lf.nno)
-		interp_node<false, T>(Lc, Lf, gf, AD, AU, n);
+		interp_node<false, SPH, T>(Lc, Lf, gf, AD, AU, n);
 }
 
 // ---------------------------------------------------------------- div / grad
@@ -1978,7 +1978,10 @@ template <typename T> void launch_project(cudaStream_t st, const Lvl &Lf, const 
 
 template <typename T> void launch_interp(cudaStream_t st, const Lvl &Lc, const Lvl &Lf, const Geo *gf, const T *AD, T *AU)
 {
-	launch_k(k_interp<T>, nblocks(Lf.nno), TPB, st, Lc, Lf, gf, AD, AU);
+	if(Lf.sphere)
+		launch_k(k_interp<T, true>, nblocks(Lf.nno), TPB, st, Lc, Lf, gf, AD, AU);
+	else
+		launch_k(k_interp<T, false>, nblocks(Lf.nno), TPB, st, Lc, Lf, gf, AD, AU);
 }
 
 template <typename T>
