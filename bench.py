@@ -1,37 +1,39 @@
-"""Benchmark: Stokes ms per time step to a 1e-6 tolerance on one GB300.
+"""Benchmark: Stokes ms per time step to a 1e-6 residual on one GB300.
 
-Workload (default): 64^3 Q1 elements, 5 multigrid levels (4^3 .. 64^3), unit
-box, eta = exp(-ln(1e3) T) (a 10^3 contrast), Ra = 1e5, free-slip walls, seeded
-initial T = 1 - z + U(-0.01, 0.01) (numpy PCG64 seed 0), Uzawa accuracy 1e-6
-with the reference's own stopping rule (dv/v and dp/p below accuracy, at most
-piterations = 375), multigrid knobs of the reference's example deck.
+Workload (default, --workload cfg2): the 2 x 2 x 1 box of 128 x 128 x 64 Q1
+elements, 6 multigrid levels (4 x 4 x 2 .. 128 x 128 x 64), eta =
+exp(-ln(1e4) T) times 30 below z = 0.8, Ra 1e6, internal heating Q0 = 1,
+free-slip walls, seeded initial T = 1 - z + U(-0.01, 0.01) (numpy PCG64 seed
+0), multigrid knobs of the reference's example deck.  --workload cube is the
+64^3 unit box (eta = exp(-ln(1e3) T), Ra 1e5), --workload sphere the
+192 x 192 x 96 regional spherical segment.
 
-A step is one Stokes solve of the seeded initial state from a cold start
-(U = P = 0): general_stokes_solver as the reference runs it before its time
-loop (forces, viscosity, operator assembly, Uzawa/multigrid solve, V), on
-state resident in HBM.  Every step therefore does the same work, and the CPU
-baseline (the same solve by the reference's algorithm) is directly
-comparable.  `value` is the mean device time per solve in the headline
-configuration: FP32 multigrid inside FP64 refinement, started from the learned
-warm start (the network's guess when its Uzawa initial residual beats the zero
-start).  The network is trained online first, on converged solves of other
-seeds (1..10: each seed's cold solve and the 4 time steps after it, 50
-snapshots, 1000 Adam steps); the training time is reported, not timed into
-`value`.  The same solve without the network and the FP64 plain path are
-timed the same way and reported beside it; `ms_per_step` adds one SUPG time
-step (PG_timestep).  `time_loop` reports the reference's own loop as well:
-after one cold solve, PG_timestep and a Stokes solve warm from the previous
-step's U, P per step (mixed and FP64 plain, --loop-steps timed steps).  `e2e` times the headline solve through the C ABI with
-host buffers (pinned), the copies included.
+Stopping: the residual rule.  Every Stokes solve runs until both FP64
+residuals of its solution are at most 1e-6: |F - K U - G P| / |F| and
+|B U| / (|U| sqrt(npno/neq)) (Uzawa iterations capped at 1000).  The
+reference's own rule (dv/v and dp/p below 1e-6, at most 375 iterations) is
+timed beside it on cold solves (`cold_solve.reference_rule`).
+
+A step is one time step of the reference's loop (Citcom.c:111-161) on state
+resident in HBM: PG_timestep, then general_stokes_solver (forces, viscosity
+from T, projection to every level, operator assembly, the Uzawa/multigrid
+solve from the previous step's U, P, and V).  Each mode starts from the
+seeded state with one untimed cold solve, runs `--warmup` untimed steps and
+then `--steps` timed ones.  `value` is the mean device time (CUDA events
+inside the library, on its stream) of the Stokes part of a timed step in the
+headline configuration: FP32 multigrid inside FP64 refinement with the
+learned warm start.  `ms_per_step` adds PG_timestep.  The same loop runs
+without the network (`mixed`) and on the FP64 plain path (`fp64_plain`); each
+mode reports the errors of its U, P, Nu and Vrms against the FP64 plain path
+after the same steps.  The network is trained online first on converged
+solves of other seeds (training time reported, not timed into `value`).
+`e2e` runs the headline loop through the C ABI with host buffers (pinned):
+PG_timestep and general_stokes_solver per step, the copies inside the timed
+region.  `drift` runs the 64^3 box (mixed vs FP64 plain) for --drift-steps
+steps and reports the per-step Nu / Vrms drift.
 
   python bench.py [--steps K] [--warmup W] [--gpus N] [--impl reference]
-                  [--size 64|32] [--no-cpu] [--no-learned]
-                  [--workload cube|cfg2|sphere]
-
---workload cfg2 is the 2x2x1 box of 128x128x64 elements (10^4 contrast,
-Ra 1e6, Q0 1); --workload sphere the 192x192x96 regional spherical segment
-(10^5 contrast x30 below r 0.9, Ra 1e7; no CPU baseline: the oracle has no
-spherical geometry).  Both report the same fields as the headline.
+                  [--workload cfg2|cube|sphere] [--no-cpu] [--no-learned]
 """
 from __future__ import annotations
 
@@ -52,19 +54,16 @@ sys.path.insert(0, ROOT)
 
 METRIC = "Stokes ms/step to 1e-6 residual: FP64 plain vs FP32 MG + learned warm start"
 UNIT = "ms/step"
-# multigrid passes of one full Stokes solve of the default workload under the
-# reference's stopping rule, counted by running the oracle's complete solve
-# (lexicographic smoother, the reference's order): 376 solve_del2_u calls and
-# 440 multigrid passes (the Uzawa loop stops at its 375-iteration cap).  The
-# CPU baseline times a bounded sample of passes and scales by this count.
-REF_FULL_SOLVE_PASSES = {64: 440, 32: 462}
+TOL = 1e-6
+ITER_CAP = 1000
 
 
 def workload(size: int):
+    """The unit box of size^3 elements, eta = exp(-ln(1e3) T), Ra 1e5."""
     from citcomcu_gb300 import Config
-    levels = {64: 5, 32: 4, 128: 6}[size]
+    levels = {64: 5, 32: 4, 128: 6, 16: 3}[size]
     return Config(mgunit=(4, 4, 4), levels=levels, rayleigh=1e5, tdepv=True, visc0=(1.0,),
-                  viscE=(math.log(1e3),), viscT=(0.0,), accuracy=1e-6, piterations=375)
+                  viscE=(math.log(1e3),), viscT=(0.0,), accuracy=TOL, piterations=ITER_CAP, stop_rule=1)
 
 
 def cfg2_workload():
@@ -74,7 +73,7 @@ def cfg2_workload():
     from citcomcu_gb300 import Config
     return Config(mgunit=(4, 4, 2), levels=6, dimen=(2.0, 2.0, 1.0), rayleigh=1e6, Q0=1.0, tdepv=True,
                   visc0=(1.0, 30.0), viscE=(math.log(1e4), math.log(1e4)), viscT=(0.0, 0.0), z_layer=(0.8,),
-                  accuracy=1e-6, piterations=375)
+                  accuracy=TOL, piterations=ITER_CAP, stop_rule=1)
 
 
 def sphere_workload():
@@ -83,8 +82,8 @@ def sphere_workload():
     eta = exp(-ln(1e5) T) times 30 below r = 0.9, Ra 1e7."""
     from citcomcu_gb300 import Config
     return Config(mgunit=(6, 6, 3), levels=6, rayleigh=1e7, tdepv=True, visc0=(1.0, 30.0),
-                  viscE=(math.log(1e5), math.log(1e5)), viscT=(0.0, 0.0), z_layer=(0.9,), accuracy=1e-6,
-                  piterations=375, sphere=(45.0, 135.0, 0.0, 90.0, 0.55, 1.0))
+                  viscE=(math.log(1e5), math.log(1e5)), viscT=(0.0, 0.0), z_layer=(0.9,), accuracy=TOL,
+                  piterations=ITER_CAP, stop_rule=1, sphere=(45.0, 135.0, 0.0, 90.0, 0.55, 1.0))
 
 
 def seeded_T0_sphere(case, seed: int = 0):
@@ -195,34 +194,110 @@ def peaks():
         return 6800.0, "fallback"
 
 
-# --------------------------------------------------------------- GPU arm
-def run_mode(cg, case, precision, T0, steps, warmup):
-    s = cg.Solver(cg.Config.like(case, precision=precision))
-    f = s.fine
-    zeros_n, zeros_u, zeros_p = np.zeros(f["nno"]), np.zeros(f["neq"]), np.zeros(f["nel"])
-    recs = []
-    l0 = None
-    for i in range(warmup + steps):
-        s.load_state(T=T0, Tdot=zeros_n, U=zeros_u, P=zeros_p)  # seeded initial state, cold start
-        if i == warmup:
-            l0 = s.stats()["kernel_launches"]
-        s.stokes_resident()
-        if i >= warmup:
-            recs.append(s.stats())
-    launches = s.stats()["kernel_launches"] - l0
-    res = s.stokes_residuals()
-    nu = s.heat_flux()
-    vr = s.vrms()
-    s.step_resident(0.0)  # one SUPG time step (then a warm solve) on the solved state
-    energy_ms = s.stats()["energy_ms"]
-    s.close()
-    return recs, launches, res, nu, vr, energy_ms
+# ------------------------------------------------------- algorithmic bytes
+def gs_sweep_bytes(nno: int, nel: int, word: int) -> int:
+    """Algorithmic bytes of one Gauss-Seidel sweep (all 8 colours) of a
+    level: read F, read and write d (9 words per node), read 1/diag K (3 words
+    per node), the viscosity at the 8 Gauss points of every element (FP32)
+    and one byte of boundary flags per node."""
+    return nno * word * 12 + 32 * nel + nno
+
+
+def bytes_per_sweep(nno: int, word: int) -> int:
+    """Bytes one sweep of the stored-stencil smoother moves at the least: the
+    243 coefficients and 3 inverse diagonals of every node, the right-hand
+    side, one write of d, and the whole d vector read once per colour launch
+    (its 27-neighbourhoods)."""
+    return nno * word * (243 + 3 + 3 + 3 + 8 * 3)
 
 
 # DRAM bytes (read + write) of one finest-level FP32 Gauss-Seidel colour launch
-# (k_tile<float, 0>, 274,625-node level), median of three launches of an
-# ncu --set full capture of this workload.
+# of the stored-stencil kernel (k_tile<float, 0>, 274,625-node level), median
+# of three launches of an ncu --set full capture; scaled by nodes elsewhere.
 TRAFFIC_PER_LAUNCH_64 = 38.57e6
+
+
+# --------------------------------------------------------------- GPU arm
+def rel(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def run_loop(cg, case, T0, precision, steps, warmup, solver=None, net=None):
+    """The reference's time loop on resident state: one cold solve of the
+    seeded state (untimed), then per step PG_timestep and general_stokes_solver
+    warm from the previous step's U, P.  Device time per step (CUDA events
+    inside the library), after `warmup` untimed steps."""
+    s = solver or cg.Solver(cg.Config.like(case, precision=precision))
+    if net is not None:
+        net.attach(True)
+    f = s.fine
+    s.load_state(T=T0, Tdot=np.zeros(f["nno"]), U=np.zeros(f["neq"]), P=np.zeros(f["nel"]))
+    s.stokes_resident()
+    cold = s.stats()
+    t = 0.0
+    recs, nus, vrs = [], [], []
+    l0 = None
+    for i in range(warmup + steps):
+        if i == warmup:
+            l0 = s.stats()["kernel_launches"]
+        adv = s.step_resident(t)
+        t = adv["elapsed_time"]
+        st = s.stats()
+        if i >= warmup:
+            recs.append(st)
+        nus.append(s.heat_flux()[0])
+        vrs.append(s.vrms())
+    launches = recs[-1]["kernel_launches"] - l0 if recs else 0
+    state = s.store_state()
+    if net is not None:
+        net.attach(False)
+    if solver is None:
+        s.close()
+    return {"recs": recs, "cold": cold, "launches": launches, "state": state, "nu": nus, "vrms": vrs,
+            "elapsed_time": t}
+
+
+def loop_summary(r, ref=None):
+    recs = r["recs"]
+    d = {"stokes_ms_per_step": float(np.mean([x["stokes_ms"] for x in recs])),
+         "ms_per_step": float(np.mean([x["stokes_ms"] + x["energy_ms"] for x in recs])),
+         "multigrid_ms_per_step": float(np.mean([x["pass_ms"] for x in recs])),
+         "uzawa_iterations": [x["uzawa"] for x in recs], "mg_passes": [x["mg_passes"] for x in recs],
+         "corrections": [x["corrections"] for x in recs],
+         "residuals_final_max": [max(x["final_momentum"] for x in recs), max(x["final_continuity"] for x in recs)],
+         "cold_solve_ms": r["cold"]["stokes_ms"], "cold_uzawa": r["cold"]["uzawa"],
+         "nu_top": r["nu"][-1], "vrms": r["vrms"][-1]}
+    if ref is not None:
+        a, b = r["state"], ref["state"]
+        d["errors_vs_fp64"] = {"U": rel(a["U"], b["U"]), "P": rel(a["P"], b["P"]), "T": rel(a["T"], b["T"]),
+                               "Nu": abs(r["nu"][-1] - ref["nu"][-1]) / abs(ref["nu"][-1]),
+                               "Vrms": abs(r["vrms"][-1] - ref["vrms"][-1]) / abs(ref["vrms"][-1])}
+    return d
+
+
+def cold_solves(cg, case, T0, precision, reps, solver=None, net=None, **over):
+    """`reps` cold solves of the seeded state (U = P = 0) with the given
+    stopping rule; device ms, iterations and passes of each."""
+    s = solver or cg.Solver(cg.Config.like(case, precision=precision, **over))
+    if net is not None:
+        net.attach(True)
+    f = s.fine
+    out = []
+    for _ in range(reps):
+        s.load_state(T=T0, Tdot=np.zeros(f["nno"]), U=np.zeros(f["neq"]), P=np.zeros(f["nel"]))
+        s.stokes_resident()
+        st = s.stats()
+        res = s.stokes_residuals()
+        out.append({"ms": st["stokes_ms"], "uzawa": st["uzawa"], "mg_passes": st["mg_passes"],
+                    "residuals": list(res), "warm_start": st["warm_start"]})
+    if net is not None:
+        net.attach(False)
+    if solver is None:
+        s.close()
+    return {"ms": float(np.mean([o["ms"] for o in out])), "uzawa": [o["uzawa"] for o in out],
+            "mg_passes": [o["mg_passes"] for o in out], "residuals": out[-1]["residuals"],
+            "warm_start": [o["warm_start"] for o in out]}
 
 
 def train_warm_start(cg, case, T0_of, seeds: int, steps_per_seed: int, train_steps: int):
@@ -253,82 +328,26 @@ def train_warm_start(cg, case, T0_of, seeds: int, steps_per_seed: int, train_ste
     return s, n, info
 
 
-def run_learned(cg, case, T0, steps, warmup, solver, net):
-    """Cold solves of the benchmark state with the warm start attached: each
-    solve runs the network on the state, compares the Uzawa initial residual
-    of its guess with that of the zero start and iterates from the better."""
-    s, n = solver, net
-    f = s.fine
-    n.attach(True)
-    zn, zu, zp = np.zeros(f["nno"]), np.zeros(f["neq"]), np.zeros(f["nel"])
-    recs = []
-    l0 = None
-    for i in range(warmup + steps):
-        s.load_state(T=T0, Tdot=zn, U=zu, P=zp)
-        if i == warmup:
-            l0 = s.stats()["kernel_launches"]
-        s.stokes_resident()
-        if i >= warmup:
-            recs.append(s.stats())
-    launches = s.stats()["kernel_launches"] - l0
-    res = s.stokes_residuals()
-    nu = s.heat_flux()
-    vr = s.vrms()
-    return recs, launches, res, nu, vr
-
-
-def time_loop(cg, case, T0, precision, steps, warmup):
-    """The reference's time loop on resident state: one cold solve of the
-    seeded state, then per step PG_timestep and general_stokes_solver warm
-    from the previous step's U, P (step_resident).  Device time per step
-    (CUDA events inside the library), after `warmup` untimed steps."""
-    s = cg.Solver(cg.Config.like(case, precision=precision))
-    f = s.fine
-    s.load_state(T=T0, Tdot=np.zeros(f["nno"]), U=np.zeros(f["neq"]), P=np.zeros(f["nel"]))
-    s.stokes_resident()
-    t = 0.0
-    recs = []
-    for i in range(warmup + steps):
-        adv = s.step_resident(t)
-        t = adv["elapsed_time"]
-        if i >= warmup:
-            st = s.stats()
-            recs.append((st["stokes_ms"], st["energy_ms"], st["uzawa"], st["mg_passes"]))
-    nu = s.heat_flux()
-    vr = s.vrms()
-    s.close()
-    return {"steps": steps, "warmup": warmup,
-            "stokes_ms_per_step": float(np.mean([r[0] for r in recs])),
-            "ms_per_step": float(np.mean([r[0] + r[1] for r in recs])),
-            "uzawa_iterations": [r[2] for r in recs], "mg_passes": [r[3] for r in recs],
-            "nu_top": nu[0], "vrms": vr, "elapsed_time": t}
-
-
-def bytes_per_sweep(nno: int, word: int) -> int:
-    """Algorithmic bytes of one Gauss-Seidel sweep (8 colour launches) on a
-    level with stored 27-block stencils: the 243 coefficients and 3 inverse
-    diagonals of every node, the right-hand side, one write of d, and the
-    whole d vector read once per colour launch (its 27-neighbourhoods)."""
-    return nno * word * (243 + 3 + 3 + 3 + 8 * 3)
-
-
-def e2e_mode(cg, s, T0, steps, warmup):
-    """The same cold solve through the C ABI with host buffers: each call
-    copies T, U, P host->device and U, P, V device->host (pinned memory)."""
+def e2e_loop(cg, s, T0, steps, warmup):
+    """The headline loop through the C ABI with host buffers: per step
+    PG_timestep (T, Tdot in/out, V in) and general_stokes_solver (T in, U, P
+    in/out, V out), all pinned host memory; wall time of the Stokes call,
+    its host<->device copies included."""
     import torch
     f = s.fine
 
     def pinned(n):
         return torch.zeros(n, dtype=torch.float64, pin_memory=True).numpy()
 
-    T, U, P = pinned(f["nno"]), pinned(f["neq"]), pinned(f["nel"])
+    T, Tdot, U, P = pinned(f["nno"]), pinned(f["nno"]), pinned(f["neq"]), pinned(f["nel"])
+    T[:] = T0
+    V = s.general_stokes_solver(T, U, P)  # the cold solve (untimed)
+    t = 0.0
     ms = []
     for i in range(warmup + steps):
-        T[:] = T0
-        U[:] = 0.0
-        P[:] = 0.0
+        t = s.PG_timestep(T, Tdot, V, t)["elapsed_time"]
         t0 = time.perf_counter()
-        s.general_stokes_solver(T, U, P)
+        V = s.general_stokes_solver(T, U, P)
         t1 = time.perf_counter()
         if i >= warmup:
             ms.append(1e3 * (t1 - t0))
@@ -356,59 +375,69 @@ def output_step(s, reps: int = 10):
             "fields": "T, V, P, heatflux, heatflux_adv, Have (T, vrms, Vi, Rho, F, f), shflux, bhflux, Nut, Nub, Vrms"}
 
 
+def drift_run(cg, size, steps):
+    """The 64^3 box (eta = exp(-ln(1e3) T), Ra 1e5) from its seeded state:
+    `steps` time steps of the mixed path and of the FP64 plain path; the
+    per-step relative differences of Nu and Vrms and the final U, P, T."""
+    case = workload(size)
+    T0 = seeded_T0(case)
+    r = {}
+    for name, prec in (("mixed", cg.MIXED), ("fp64_plain", cg.FP64)):
+        r[name] = run_loop(cg, case, T0, prec, steps, 0)
+    m, p = r["mixed"], r["fp64_plain"]
+    dnu = [abs(a - b) / abs(b) for a, b in zip(m["nu"], p["nu"])]
+    dvr = [abs(a - b) / abs(b) for a, b in zip(m["vrms"], p["vrms"])]
+    return {"workload": workload_name(case), "steps": steps,
+            "nu_rel_drift_per_step": dnu, "vrms_rel_drift_per_step": dvr,
+            "nu_rel_drift_max": max(dnu), "vrms_rel_drift_max": max(dvr),
+            "final_errors": {"U": rel(m["state"]["U"], p["state"]["U"]), "P": rel(m["state"]["P"], p["state"]["P"]),
+                             "T": rel(m["state"]["T"], p["state"]["T"])},
+            "stokes_ms_per_step": {"mixed": loop_summary(m)["stokes_ms_per_step"],
+                                   "fp64_plain": loop_summary(p)["stokes_ms_per_step"]},
+            "nu_top_final": {"mixed": m["nu"][-1], "fp64_plain": p["nu"][-1]}}
+
+
 # --------------------------------------------------------------- CPU side
-def cpu_sample(case, T0, uzawa_sample: int = 3, full_passes=None):
-    """The oracle port (FP64, lexicographic smoother = the reference's
-    algorithm) on the same workload: the set-up of one Stokes solve (forces,
-    viscosity on all levels, stiffness assembly) timed in full, plus the first
-    Uzawa iterations of the solve timed per multigrid pass and scaled to the
-    full solve's pass count."""
-    from oracle import oracle as O
+def oracle_case(case, stop_rule=1):
     from oracle.decks import Case
-    O.build()
     c = Case(**{k: getattr(case, k) for k in ("mgunit", "levels", "dimen", "rayleigh", "Q0", "tdepv", "visc0",
                                                "viscE", "viscT", "z_layer", "vmin", "vmax", "aug_lagr",
                                                "aug_number", "precond", "mg_cycle", "down_heavy", "up_heavy",
-                                               "vlowstep", "vhighstep", "accuracy")})
+                                               "vlowstep", "vhighstep", "accuracy", "piterations")})
+    c.stop_rule = stop_rule
+    return c
+
+
+def cpu_sample(case, T0, passes_per_step: float):
+    """A bounded sample of the oracle port (FP64, lexicographic smoother = the
+    reference's algorithm) on the same workload: the set-up of a Stokes solve
+    (forces, viscosity on all levels, stiffness assembly) timed in full, then
+    the head of the cold solve (one solve_del2_u) timed per multigrid pass;
+    scaled to `passes_per_step` passes per time step."""
+    from oracle import oracle as O
+    O.build()
+    c = oracle_case(case)
     o = O.Oracle(c, gs_colored=False)
     o.set_T(T0)
     t0 = time.perf_counter()
     o.setup_operators()
     t1 = time.perf_counter()
-    info = o.solve_Ahat_p_fhat(c.accuracy, uzawa_sample)
+    info = o.solve_Ahat_p_fhat(c.accuracy, 0)
     t2 = time.perf_counter()
     per_pass = (t2 - t1) / max(info["mg_calls"], 1)
-    full = full_passes if full_passes else REF_FULL_SOLVE_PASSES.get(case.nox - 1, info["mg_calls"])
-    value = 1e3 * ((t1 - t0) + per_pass * full)
+    value = 1e3 * ((t1 - t0) + per_pass * passes_per_step)
     return {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
             "sample": f"oracle (C, FP64, lexicographic Gauss-Seidel) on this workload: set-up {t1 - t0:.2f} s timed in "
-                      f"full, then the first {info['del2_calls']} solve_del2_u calls ({info['mg_calls']} multigrid "
-                      f"passes, {t2 - t1:.1f} s) of the first Uzawa solve; {1e3 * per_pass:.1f} ms per pass x "
-                      f"{full} passes of the full solve"}
-
-
-def _sample_worker(job):
-    case, T0, full = job
-    return cpu_sample(case, T0, uzawa_sample=2, full_passes=full)["value"]
-
-
-def all_cores_sample(case, T0, full):
-    """The reference has no thread parallelism (its parallelism is MPI
-    domains, and no MPI exists on the host): with every host core, one
-    single-rank solve per core at once.  Returns the ms per solve of that
-    aggregate throughput, the process count and the per-process time."""
-    import multiprocessing as mp
-    try:
-        n = len(os.sched_getaffinity(0))
-    except AttributeError:
-        n = os.cpu_count() or 1
-    n = max(1, min(n, 32))
-    with mp.get_context("spawn").Pool(n) as pool:
-        per = pool.map(_sample_worker, [(case, T0, full)] * n)
-    return float(np.mean(per)) / n, n, float(np.mean(per))
+                      f"full, then the velocity solve of the cold solve's head ({info['mg_calls']} multigrid passes, "
+                      f"{t2 - t1:.1f} s): {1e3 * per_pass:.1f} ms per pass x {passes_per_step:.1f} passes per time "
+                      f"step (the FP64 GPU path's mean over the timed steps, the same algorithm in 8 colours)"}
 
 
 def reference_arm(args):
+    """The oracle port's own time loop on the host cores: a cold solve
+    (untimed), then per step PG_timestep and the Stokes solve (set-up and
+    residual-rule Uzawa solve from the previous step); wall time of the Stokes
+    part of each step, measured in full (no extrapolation)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
@@ -416,73 +445,86 @@ def reference_arm(args):
         print(json.dumps({"impl": "reference", "unavailable": "the spherical segment has no CPU port of the path "
                                                                "(the oracle is Cartesian)"}))
         return 0
+    from oracle import oracle as O
+    O.build()
     case = cfg2_workload() if args.workload == "cfg2" else workload(args.size)
     T0 = seeded_T0(case)
-    # full-solve pass count of the 128x128x64 box: the FP64 GPU path's 788
-    # (the same algorithm in 8 colours; the oracle's own count is not measured)
-    full = 788 if args.workload == "cfg2" else None
-    vals = []
+    c = oracle_case(case)
+    o = O.Oracle(c, gs_colored=False)
+    o.set_T(T0)
+    o.thermal_buoyancy()
+    t0 = time.perf_counter()
+    cold = o.stokes()
+    cold_s = time.perf_counter() - t0
+    vals, pg, its, passes = [], [], [], []
     for i in range(args.warmup + args.steps):
-        r = cpu_sample(case, T0, uzawa_sample=2, full_passes=full)
+        t0 = time.perf_counter()
+        o.pg_timestep()
+        t1 = time.perf_counter()
+        info = o.stokes()
+        t2 = time.perf_counter()
         if i >= args.warmup:
-            vals.append(r["value"])
+            vals.append(1e3 * (t2 - t1))
+            pg.append(1e3 * (t1 - t0))
+            its.append(info["uzawa"])
+            passes.append(info["mg_calls"])
     v = float(np.mean(vals))
-    try:
-        agg, nproc, per = all_cores_sample(case, T0, full)
-        all_cores = {"value": agg, "unit": UNIT, "processes": nproc, "ms_per_solve_per_process": per,
-                     "note": "one single-rank solve per host core at once; value = ms per solve of the aggregate "
-                             "throughput (no single solve gets faster: the reference parallelises by MPI domains)"}
-    except Exception as e:  # noqa: BLE001 - the one-core figure above stands on its own
-        all_cores = {"unavailable": f"{type(e).__name__}: {e}"}
+    sample = (f"oracle port (C, FP64, lexicographic Gauss-Seidel: the reference's algorithm), one core: a cold solve "
+              f"({cold_s:.1f} s, {cold['uzawa']} Uzawa iterations, untimed), {args.warmup} untimed and {args.steps} "
+              f"timed time steps, each PG_timestep plus a complete Stokes solve to the residual rule; value = mean "
+              f"wall time of the Stokes solves")
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": v, "higher_is_better": False, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": workload_name(case)},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "sample": r["sample"]},
-            "cpu_all_cores": all_cores,
+            "warmup": args.warmup, "ms_per_step": v + float(np.mean(pg)), "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": workload_name(case), "step": STEP_DESC},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
+            "uzawa_iterations": its, "mg_passes": passes,
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
 
 
+STEP_DESC = ("one time step of the reference's loop on resident state: PG_timestep, then general_stokes_solver "
+             "(forces, viscosity, projection, operator assembly, Uzawa/multigrid solve from the previous step to the "
+             "residual rule, V); value = the Stokes part")
+
+
 def workload_name(case):
+    rule = (f"residual rule |F-KU-GP|/|F| and |BU|/(|U| sqrt(npno/neq)) <= {case.accuracy:g}, "
+            f"Uzawa cap {case.piterations}") if case.stop_rule == 1 else \
+        f"reference rule dv/v, dp/p < {case.accuracy:g}, piterations {case.piterations}"
     if case.sphere is not None:
         return ("regional spherical shell segment, colatitude 45-135 deg, longitude 0-90 deg, r 0.55-1.0, "
                 f"{case.nox - 1}x{case.noy - 1}x{case.noz - 1} Q1 elements, {case.levels} multigrid levels, "
-                "eta=exp(-ln(1e5) T) x30 below r=0.9, Ra=1e7, conductive T0 + U(-0.01,0.01) seed 0, "
-                f"accuracy 1e-6, piterations {case.piterations}")
+                "eta=exp(-ln(1e5) T) x30 below r=0.9, Ra=1e7, conductive T0 + U(-0.01,0.01) seed 0, " + rule)
     if case.dimen[0] == 2.0:
         return (f"2x2x1 box, {case.nox - 1}x{case.noy - 1}x{case.noz - 1} Q1 elements, {case.levels} multigrid levels, "
-                "eta=exp(-ln(1e4) T) x30 below z=0.8, Ra=1e6, Q0=1, free slip, T0=1-z+U(-0.01,0.01) seed 0, "
-                "accuracy 1e-6, piterations 375")
+                "eta=exp(-ln(1e4) T) x30 below z=0.8, Ra=1e6, Q0=1, free slip, T0=1-z+U(-0.01,0.01) seed 0, " + rule)
     return (f"{case.nox - 1}^3 Q1 elements, {case.levels} multigrid levels, eta=exp(-ln(1e3) T), Ra=1e5, free slip, "
-            f"T0=1-z+U(-0.01,0.01) seed 0, accuracy 1e-6, piterations 375")
+            f"T0=1-z+U(-0.01,0.01) seed 0, " + rule)
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--size", type=int, default=64, choices=[32, 64, 128])
+    ap.add_argument("--workload", default="cfg2", choices=["cfg2", "cube", "sphere"],
+                    help="cfg2: the 128x128x64 box with a 10^4 contrast (default); cube: the --size^3 unit box; "
+                         "sphere: the 192x192x96 regional spherical segment")
+    ap.add_argument("--size", type=int, default=64, choices=[16, 32, 64, 128])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--modes", default="both", choices=["both", "mixed"],
+    ap.add_argument("--modes", default="all", choices=["all", "mixed"],
                     help="'mixed' skips the FP64 plain comparison (profiling runs)")
     ap.add_argument("--no-learned", action="store_true",
                     help="headline without the learned warm start (profiling runs)")
     ap.add_argument("--learn-seeds", type=int, default=10)
     ap.add_argument("--learn-steps", type=int, default=4, help="time steps recorded after each seed's cold solve")
     ap.add_argument("--learn-adam", type=int, default=1000, help="Adam steps of the online training")
-    ap.add_argument("--workload", default="cube", choices=["cube", "sphere", "cfg2"],
-                    help="sphere: the 192x192x96 regional spherical segment; cfg2: the 128x128x64 box with a 10^4 "
-                         "contrast, instead of the headline 64^3 box")
-    ap.add_argument("--loop-steps", type=int, default=10,
-                    help="timed steps of the time-loop measurement (0: skip it)")
-    ap.add_argument("--loop-warmup", type=int, default=3)
-    ap.add_argument("--piterations", type=int, default=375,
-                    help="Uzawa iteration cap; lower values only for short profiling runs")
+    ap.add_argument("--cold-reps", type=int, default=2, help="cold solves per mode (0: skip)")
+    ap.add_argument("--drift-steps", type=int, default=50, help="time steps of the 64^3 drift run (0: skip)")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
@@ -504,7 +546,6 @@ def main():
     else:
         case = cfg2_workload() if args.workload == "cfg2" else workload(args.size)
         T0_of = lambda sd: seeded_T0(case, sd)  # noqa: E731
-    case.piterations = args.piterations
     T0 = T0_of(0)
 
     def barrier():
@@ -512,114 +553,106 @@ def main():
         if world > 1:
             torch.distributed.barrier()
 
+    learned = ls = ln = train_info = None
+    if not args.no_learned:
+        ls, ln, train_info = train_warm_start(cg, case, T0_of, args.learn_seeds, args.learn_steps, args.learn_adam)
     barrier()
-    learned = None
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
-        mixed, launches, res_mixed, nu_mixed, vr_mixed, energy_ms = run_mode(cg, case, cg.MIXED, T0, args.steps,
-                                                                            args.warmup)
+        if ls is not None:
+            learned = run_loop(cg, case, T0, cg.MIXED, args.steps, args.warmup, solver=ls, net=ln)
+        mixed = run_loop(cg, case, T0, cg.MIXED, args.steps, args.warmup)
+        fp64 = run_loop(cg, case, T0, cg.FP64, args.steps, args.warmup) if args.modes == "all" else None
         t1 = time.perf_counter()
-        if args.modes == "both":
-            fp64, _, res_fp64, nu_fp64, vr_fp64, _ = run_mode(cg, case, cg.FP64, T0, args.steps, args.warmup)
-        else:
-            fp64, res_fp64, nu_fp64, vr_fp64 = mixed, res_mixed, nu_mixed, vr_mixed
-        if not args.no_learned:
-            ls, ln, train_info = train_warm_start(cg, case, T0_of, args.learn_seeds,
-                                                  args.learn_steps, args.learn_adam)
-            t2 = time.perf_counter()
-            lrecs, llaunches, res_l, nu_l, vr_l = run_learned(cg, case, T0, args.steps, args.warmup, ls, ln)
-            t3 = time.perf_counter()
-            learned = (lrecs, llaunches, res_l, nu_l, vr_l, train_info, t3 - t2)
     barrier()
 
-    mixed_ms = float(np.mean([r["stokes_ms"] for r in mixed]))
-    stokes_ms_fp64 = float(np.mean([r["stokes_ms"] for r in fp64]))
-    head = learned[0] if learned else mixed
-    stokes_ms = float(np.mean([r["stokes_ms"] for r in head]))
-    step_ms = stokes_ms + float(energy_ms)
+    head = learned or mixed
+    recs = head["recs"]
+    stokes_ms = float(np.mean([r["stokes_ms"] for r in recs]))
+    step_ms = float(np.mean([r["stokes_ms"] + r["energy_ms"] for r in recs]))
     stokes_ms, step_ms = max_over_ranks([stokes_ms, step_ms], world)
     value = whole_job_value(stokes_ms, world)
 
-    # dominant kernel: finest-level FP32 Gauss-Seidel colour launches, timed live
-    nno = case.nno
-    sweeps = sum(r["smoother_sweeps"] for r in head)
-    sm_ms = sum(r["smoother_ms"] for r in head)
+    # dominant kernel: the finest-level FP32 Gauss-Seidel colour launches, timed
+    # live by CUDA events inside the multigrid pass (on the library's stream)
+    sweeps = sum(r["smoother_sweeps"] for r in recs)
+    sm_ms = sum(r["smoother_ms"] for r in recs)
     per_launch_s = sm_ms * 1e-3 / max(8 * sweeps, 1)
-    per_launch_bytes = bytes_per_sweep(nno, 4) / 8.0
+    nno, nel = case.nno, (case.nox - 1) * (case.noy - 1) * (case.noz - 1)
+    alg_bytes = gs_sweep_bytes(nno, nel, 4) / 8.0
+    stored_bytes = bytes_per_sweep(nno, 4) / 8.0
     peak, peak_kind = peaks()
-    achieved = per_launch_bytes / per_launch_s / 1e9 if per_launch_s > 0 else None
+    achieved = alg_bytes / per_launch_s / 1e9 if per_launch_s > 0 else None
+    achieved_stored = stored_bytes / per_launch_s / 1e9 if per_launch_s > 0 else None
 
     if rank != 0:
         return 0
 
-    def summary(recs, res, nu, vr):
-        return {"stokes_ms_per_step": float(np.mean([r["stokes_ms"] for r in recs])),
-                "multigrid_ms_per_step": float(np.mean([r["pass_ms"] for r in recs])),
-                "uzawa_iterations": [r["uzawa"] for r in recs], "mg_passes": [r["mg_passes"] for r in recs],
-                "residuals_final": res, "nu_top": nu[0], "vrms": vr,
-                "nu_rel_err_vs_fp64": abs(nu[0] - nu_fp64[0]) / abs(nu_fp64[0]),
-                "vrms_rel_err_vs_fp64": abs(vr - vr_fp64) / vr_fp64}
-
-    mode = "FP32 multigrid + FP64 refinement + learned warm start" if learned else "FP32 multigrid + FP64 refinement"
+    ref = fp64 if fp64 is not None else None
+    mode = ("FP32 multigrid + FP64 refinement + learned warm start" if learned
+            else "FP32 multigrid + FP64 refinement")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": step_ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64", "data": "synthetic",
-        "config": {"workload": workload_name(case), "mode": mode + " (headline)",
-                   "step": "cold Stokes solve of the seeded initial state (general_stokes_solver)",
-                   "parallelism": f"replicas{world}", "l2": f"inputs larger than L2 (finest FP32 stencil {case.nno * 972 / 1e6:.0f} MB, FP64 "
+        "config": {"workload": workload_name(case), "mode": mode + " (headline)", "step": STEP_DESC,
+                   "parallelism": f"replicas{world}",
+                   "l2": f"inputs larger than L2 (finest FP32 stencil {case.nno * 972 / 1e6:.0f} MB, FP64 "
                          f"{case.nno * 1944 / 1e6:.0f} MB)",
                    "timing": "CUDA events around each Stokes solve inside the library, mean over timed steps"},
-        "fp64_plain": {"stokes_ms_per_step": stokes_ms_fp64,
-                       "uzawa_iterations": [r["uzawa"] for r in fp64], "mg_passes": [r["mg_passes"] for r in fp64],
-                       "residuals_final": res_fp64, "nu_top": nu_fp64[0], "vrms": vr_fp64},
-        "mixed": summary(mixed, res_mixed, nu_mixed, vr_mixed),
-        "speedup_vs_fp64": stokes_ms_fp64 / stokes_ms,
+        "mixed": loop_summary(mixed, ref),
         "roofline": {"bound": "hbm", "kernel": "k_tile<float, 0> (finest-level Gauss-Seidel colour)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None,
-                     # the ncu capture at 64^3 scaled by the nodes of one colour launch (the
-                     # kernel's DRAM bytes per node do not depend on the level's size)
                      "traffic": TRAFFIC_PER_LAUNCH_64 * nno / 274625 if nno >= 274625 else None,
-                     "peak_kind": peak_kind, "bytes_per_launch": per_launch_bytes,
-                     "launch_us": per_launch_s * 1e6},
+                     "peak_kind": peak_kind, "bytes_per_launch": alg_bytes,
+                     "bytes_kind": "algorithmic (per colour: F, d, 1/diag K, Gauss-point viscosity, flags)",
+                     "launch_us": per_launch_s * 1e6,
+                     "stored_stencil": {"bytes_per_launch": stored_bytes, "achieved": achieved_stored,
+                                        "frac": (achieved_stored / peak) if achieved_stored else None}},
         "clocks": clk.summary(),
-        "gpu_launches": int(learned[1] if learned else launches),
-        "wall_s_mixed": t1 - t0,
+        "gpu_launches": int(head["launches"]),
+        "wall_s_loops": t1 - t0,
     }
+    if fp64 is not None:
+        line["fp64_plain"] = loop_summary(fp64)
+        line["speedup_vs_fp64"] = line["fp64_plain"]["stokes_ms_per_step"] / stokes_ms
     if learned:
-        lrecs, _, res_l, nu_l, vr_l, train_info, wall = learned
-        d = summary(lrecs, res_l, nu_l, vr_l)
-        d.update({"warm_start_used": [r["warm_start"] for r in lrecs],
-                  "initial_residual_zero_start": lrecs[-1]["base_residual"],
-                  "initial_residual_network": lrecs[-1]["warm_residual"],
-                  "speedup_vs_mixed": mixed_ms / d["stokes_ms_per_step"], "training": train_info})
+        d = loop_summary(learned, ref)
+        d.update({"warm_start_used": [r["warm_start"] for r in learned["recs"]],
+                  "initial_residual_previous_step": [r["base_residual"] for r in learned["recs"]],
+                  "initial_residual_network": [r["warm_residual"] for r in learned["recs"]],
+                  "speedup_vs_mixed": line["mixed"]["stokes_ms_per_step"] / d["stokes_ms_per_step"],
+                  "training": train_info})
         line["learned"] = d
+    if args.cold_reps > 0:
+        cs = {"mixed": cold_solves(cg, case, T0, cg.MIXED, args.cold_reps)}
+        if ls is not None:
+            cs["learned"] = cold_solves(cg, case, T0, cg.MIXED, args.cold_reps, solver=ls, net=ln)
+        if args.modes == "all":
+            cs["fp64_plain"] = cold_solves(cg, case, T0, cg.FP64, args.cold_reps)
+            cs["reference_rule"] = {
+                "mixed": cold_solves(cg, case, T0, cg.MIXED, 1, stop_rule=0, piterations=375),
+                "fp64_plain": cold_solves(cg, case, T0, cg.FP64, 1, stop_rule=0, piterations=375)}
+        line["cold_solve"] = cs
     if not args.no_e2e:
-        es = ls if learned else cg.Solver(cg.Config.like(case, precision=cg.MIXED))
-        e2e_ms, h2d, d2h = e2e_mode(cg, es, T0, min(args.steps, 3), 1)
+        es = ls if ls is not None else cg.Solver(cg.Config.like(case, precision=cg.MIXED))
+        if ln is not None:
+            ln.attach(True)
+        e2e_ms, h2d, d2h = e2e_loop(cg, es, T0, args.steps, args.warmup)
         line["e2e"] = {"value": e2e_ms, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                       "mode": mode}
+                       "mode": mode, "steps": args.steps, "warmup": args.warmup}
         line["output_step"] = output_step(es)
-    if learned:
+        if es is not ls:
+            es.close()
+    if ln is not None:
         ln.close()
         ls.close()
-    if args.loop_steps > 0:
-        # per time step as the reference's loop runs it: warm solves from the
-        # previous step (mixed path, and FP64 plain for comparison)
-        tl = {"mixed": time_loop(cg, case, T0, cg.MIXED, args.loop_steps, args.loop_warmup)}
-        if args.modes == "both":
-            tl["fp64_plain"] = time_loop(cg, case, T0, cg.FP64, args.loop_steps, args.loop_warmup)
-            tl["speedup_vs_fp64"] = tl["fp64_plain"]["ms_per_step"] / tl["mixed"]["ms_per_step"]
-            tl["nu_rel_err_vs_fp64"] = abs(tl["mixed"]["nu_top"] - tl["fp64_plain"]["nu_top"]) / abs(
-                tl["fp64_plain"]["nu_top"])
-        line["time_loop"] = tl
+    if args.drift_steps > 0 and args.workload != "sphere":
+        line["drift"] = drift_run(cg, 64, args.drift_steps)
     if not args.no_cpu and case.sphere is None:  # the oracle has no spherical geometry
-        # full-solve pass count: the oracle's own count where it was measured,
-        # else the FP64 GPU path's (the same algorithm in 8 colours)
-        full = REF_FULL_SOLVE_PASSES.get(case.nox - 1) if args.workload == "cube" else int(np.mean(
-            [r["mg_passes"] for r in fp64]))
-        line["cpu_baseline"] = cpu_sample(case, T0, full_passes=full)
+        pps = float(np.mean([r["mg_passes"] for r in (fp64 or mixed)["recs"]]))
+        line["cpu_baseline"] = cpu_sample(case, T0, pps)
     print(json.dumps(line))
     return 0
 

@@ -20,10 +20,12 @@ from .build import LIB as LIB_PATH
 from .build import build as _build_lib
 
 __all__ = ["Config", "Solver", "WarmStart", "CitcomGPUError", "load_library", "build", "heat_flux_noalloc", "FP64",
-           "MIXED"]
+           "MIXED", "STOP_REFERENCE", "STOP_RESIDUAL"]
 
 FP64 = 0
 MIXED = 1
+STOP_REFERENCE = 0
+STOP_RESIDUAL = 1
 
 _ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "invalid state", -4: "no convergence"}
 
@@ -75,6 +77,9 @@ class Config:
     sdepv_misfit: float = 0.001
     max_sdep_visc_iter: int = 50
     sdepv_iter_damp: float = 1.0
+    # Uzawa stopping rule: STOP_REFERENCE (dv/v and dp/p below accuracy) or
+    # STOP_RESIDUAL (both FP64 residuals of the solution at most accuracy)
+    stop_rule: int = 0
 
     @property
     def nox(self):
@@ -142,6 +147,7 @@ class _CConfig(ctypes.Structure):
         ("sdepv_misfit", ctypes.c_double),
         ("sdepv_iter_damp", ctypes.c_double),
         ("max_sdep_visc_iter", ctypes.c_int),
+        ("stop_rule", ctypes.c_int),
     ]
 
 
@@ -157,7 +163,8 @@ class _CStats(ctypes.Structure):
                 ("kernel_launches", ctypes.c_ulonglong), ("visc_iterations", ctypes.c_int),
                 ("visc_misfit", ctypes.c_double), ("warm_start", ctypes.c_int),
                 ("warm_residual", ctypes.c_double), ("base_residual", ctypes.c_double),
-                ("pass_ms", ctypes.c_double)]
+                ("pass_ms", ctypes.c_double), ("final_momentum", ctypes.c_double),
+                ("final_continuity", ctypes.c_double), ("corrections", ctypes.c_int)]
 
 
 # every symbol of include/citcom_gb300.h with its argument types
@@ -327,6 +334,7 @@ class Solver:
         c.sdepv_misfit = cfg.sdepv_misfit
         c.sdepv_iter_damp = cfg.sdepv_iter_damp
         c.max_sdep_visc_iter = cfg.max_sdep_visc_iter
+        c.stop_rule = int(cfg.stop_rule)
         if cfg.sphere is not None:
             tn, ts, fw, fe, ri, ro = cfg.sphere
             c.sphere = 1
@@ -373,7 +381,9 @@ class Solver:
                     initial_residual=s.initial_residual, stokes_ms=s.stokes_ms, energy_ms=s.energy_ms,
                     smoother_ms=s.smoother_ms, smoother_sweeps=s.smoother_sweeps, kernel_launches=s.kernel_launches,
                     warm_start=s.warm_start, warm_residual=s.warm_residual, base_residual=s.base_residual,
-                    visc_iterations=s.visc_iterations, visc_misfit=s.visc_misfit, pass_ms=s.pass_ms)
+                    visc_iterations=s.visc_iterations, visc_misfit=s.visc_misfit, pass_ms=s.pass_ms,
+                    final_momentum=s.final_momentum, final_continuity=s.final_continuity,
+                    corrections=s.corrections)
 
     def stokes_residuals(self):
         """(|F - K U - G P| / |F|, |div U| / (|U| sqrt(npno/neq))) of the resident solution."""

@@ -598,8 +598,10 @@ int nn_guess(citcom_nn *n);
 
 // The head of solve_Ahat_p_fhat (Stokes_flow_Incomp.c:360-371): the velocity
 // correction V += K^-1 (F - G P - K V) for the pressure P, then r1 = B V and
-// the initial residual |r1| / sqrt(npno) that the function returns.
-int uzawa_start(citcom_gpu *h, double *V, const double *P, const double *F, double acc, double *residual)
+// the initial residual |r1| / sqrt(npno) that the function returns.  With
+// vv != null also V.V (the residual rule's continuity test needs it).
+int uzawa_start(citcom_gpu *h, double *V, const double *P, const double *F, double acc, double *r1, double *residual,
+                double *vv = nullptr)
 {
 	const int lmax = h->L - 1;
 	const Lvl &Lf = h->lv[lmax];
@@ -613,17 +615,43 @@ int uzawa_start(citcom_gpu *h, double *V, const double *P, const double *F, doub
 	TRY(solve_del2_u(h, acc, &valid));
 	launch_strip(st, Lf, h->u1);
 	launch_axpby(st, Lf.neq, V, 1.0, h->u1, 1.0);
-	launch_div(st, Lf, geo, V, h->r1);
-	launch_dot(st, Lf.nel, h->r1, h->r1, red_of(h), h->dscal + S_R0);
-	TRY(readback(h, S_R0, 1));
+	launch_div(st, Lf, geo, V, r1);
+	launch_dot(st, Lf.nel, r1, r1, red_of(h), h->dscal + S_R0);
+	if(vv)
+		launch_dot(st, Lf.neq, V, V, red_of(h), h->dscal + S_R0 + 1);
+	TRY(readback(h, S_R0, vv ? 2 : 1));
 	*residual = std::sqrt(h->hscal[S_R0] / Lf.nel);
+	if(vv)
+		*vv = h->hscal[S_R0 + 1];
 	return CITCOM_GPU_OK;
+}
+
+// |F - K V - G P|^2 with the FP64 operator of the finest level (constrained
+// rows are zero in F, G P and K V alike)
+int momentum_rr(citcom_gpu *h, const double *V, const double *P, const double *F, double *rr)
+{
+	const int lmax = h->L - 1;
+	const Lvl &Lf = h->lv[lmax];
+	launch_grad(h->st, Lf, h->geo[lmax], P, h->Ah);
+	launch_kmul<double>(h->st, Lf, h->K64[lmax], V, h->u1);
+	launch_sub3(h->st, Lf.neq, h->r64, F, h->Ah, h->u1);
+	launch_dot(h->st, Lf.neq, h->r64, h->r64, red_of(h), h->dscal + S_R0 + 2);
+	TRY(readback(h, S_R0 + 2, 1));
+	*rr = h->hscal[S_R0 + 2];
+	return CITCOM_GPU_OK;
+}
+
+// continuity residual of the residual rule: |B V| / (|V| sqrt(npno/neq))
+double continuity(double bvbv, double vv, int neq, int npno)
+{
+	return std::sqrt(bvbv / (vv > 0.0 ? vv : 1e-300) * ((double)neq / (double)npno));
 }
 
 // solve_Ahat_p_fhat (Stokes_flow_Incomp.c:295-497) on device buffers.  With a
 // warm-start network attached, the head runs for the network's guess as well
 // as for the given V, P, and the loop continues from the pair with the smaller
-// initial residual.
+// initial residual.  Stopping: the reference's rule (dv/v, dp/p) or the
+// residual rule of citcom_gpu_config.stop_rule.
 int uzawa(citcom_gpu *h, double *V, double *P, const double *F, double imp, int *steps_max, double *initial_residual)
 {
 	const int lmax = h->L - 1;
@@ -632,25 +660,31 @@ int uzawa(citcom_gpu *h, double *V, double *P, const double *F, double imp, int 
 	const Geo *geo = h->geo[lmax];
 	cudaStream_t st = h->st;
 	double *Ah = h->Ah, *u1 = h->u1;
+	const bool resid_rule = h->cfg.stop_rule == CITCOM_GPU_STOP_RESIDUAL;
 	int valid;
 	if(!h->stiffness_ready)
 		return fail(h, CITCOM_GPU_ERR_STATE, "construct_stiffness_B_matrix has not been called");
 
 	launch_dot(st, neq, F, F, red_of(h), h->dscal + S_R0);
 	TRY(readback(h, S_R0, 1));
-	const double v_res = std::sqrt(h->hscal[S_R0] / neq);
+	const double ff = h->hscal[S_R0];
+	const double v_res = std::sqrt(ff / neq);
 
 	h->stats.warm_start = 0;
 	h->stats.warm_residual = 0.0;
 	h->stats.base_residual = 0.0;
-	double residual = 0.0;
+	h->stats.corrections = 0;
+	h->stats.final_momentum = 0.0;
+	h->stats.final_continuity = 0.0;
+	double residual = 0.0, vv = 0.0;
+	double *vvp = resid_rule ? &vv : nullptr;
 	citcom_nn *n = h->warm;
 	if(n && n->scaled)
 	{
-		double r_net = 0.0;
+		double r_net = 0.0, vv_net = 0.0;
 		TRY(nn_guess(n));
-		TRY(uzawa_start(h, n->Ug, n->Pg, F, imp * v_res, &r_net));
-		TRY(uzawa_start(h, V, P, F, imp * v_res, &residual));
+		TRY(uzawa_start(h, n->Ug, n->Pg, F, imp * v_res, h->r1, &r_net, resid_rule ? &vv_net : nullptr));
+		TRY(uzawa_start(h, V, P, F, imp * v_res, h->r1, &residual, vvp));
 		if(nn_device_error(n->net) != 0)
 			return fail(h, CITCOM_GPU_ERR_CUDA, "warm-start network: a tensor-core wait timed out");
 		h->stats.warm_residual = r_net;
@@ -661,22 +695,56 @@ int uzawa(citcom_gpu *h, double *V, double *P, const double *F, double imp, int 
 			CK(cudaMemcpyAsync(P, n->Pg, sizeof(double) * npno, cudaMemcpyDeviceToDevice, st));
 			launch_div(st, Lf, geo, V, h->r1);
 			residual = r_net;
+			vv = vv_net;
 			h->stats.warm_start = 1;
 		}
 	}
 	else
-		TRY(uzawa_start(h, V, P, F, imp * v_res, &residual));
+		TRY(uzawa_start(h, V, P, F, imp * v_res, h->r1, &residual, vvp));
 	double *r0 = h->r0, *r1 = h->r1, *r2 = h->r2, *z0 = h->z0, *z1 = h->z1, *s1 = h->s1, *s2 = h->s2, *sh;
 
 	int count = 0;
 	double dpressure = 1.0, dvelocity = 1.0;
+	// residual rule: continuity of the current V (from r1 = B V) and whether
+	// the next iteration starts a new search direction
+	double cont = resid_rule ? continuity(residual * residual * npno, vv, neq, npno) : 0.0;
+	bool restart = true;
 	double *sc = h->dscal + S_UZ;
 	CK(cudaMemsetAsync(sc, 0, 5 * sizeof(double), st));
-	while(count < *steps_max && (dpressure >= imp || dvelocity >= imp))
+	for(;;)
 	{
+		if(resid_rule)
+		{
+			if(cont <= imp)
+			{
+				double rr = 0.0;
+				TRY(momentum_rr(h, V, P, F, &rr));
+				const double mom = std::sqrt(rr / (ff > 0.0 ? ff : 1.0));
+				h->stats.final_momentum = mom;
+				h->stats.final_continuity = cont;
+				if(mom <= imp || h->stats.corrections >= 8)
+					break;
+				// velocity correction to half the tolerance, then B V afresh
+				double rc = 0.0;
+				TRY(uzawa_start(h, V, P, F, 0.5 * imp * v_res, r1, &rc, &vv));
+				h->stats.corrections++;
+				cont = continuity(rc * rc * npno, vv, neq, npno);
+				h->stats.final_continuity = cont;
+				restart = true;
+				if(h->verbose)
+					fprintf(stderr, "AhatP correction %d: momentum %9.3e -> continuity %9.3e\n", h->stats.corrections, mom,
+					        cont);
+				continue;
+			}
+			if(count >= *steps_max)
+				break;
+		}
+		else if(!(count < *steps_max && (dpressure >= imp || dvelocity >= imp)))
+			break;
 		// z1 = BPI r1, r1.z1, search direction s2 (scalars stay on the device)
 		launch_uzawa_precond(st, npno, h->BPI, r1, z1, red_of(h), sc);
-		launch_uzawa_search(st, npno, s2, z1, s1, sc, count == 0);
+		launch_uzawa_search(st, npno, s2, z1, s1, sc, restart);
+		restart = false;
 		launch_grad(st, Lf, geo, s2, Ah);
 		TRY(solve_del2_u(h, imp * v_res, &valid));
 		launch_strip(st, Lf, u1);
@@ -684,20 +752,21 @@ int uzawa(citcom_gpu *h, double *V, double *P, const double *F, double imp, int 
 		launch_dot(st, npno, s2, Ah, red_of(h), sc + 2);
 		launch_uzawa_update(st, npno, neq, r2, r1, Ah, P, s2, V, u1, sc, valid);
 		launch_dots4(st, neq, V, V, u1, u1, nullptr, nullptr, nullptr, nullptr, red_of(h), h->dscal + S_DOT);
-		launch_dots4(st, npno, P, P, s2, s2, nullptr, nullptr, nullptr, nullptr, red_of(h), h->dscal + S_DOT + 4);
+		launch_dots4(st, npno, P, P, s2, s2, r2, r2, nullptr, nullptr, red_of(h), h->dscal + S_DOT + 4);
 		CK(cudaMemcpyAsync(h->hscal + S_DOT, h->dscal + S_DOT, 8 * sizeof(double), cudaMemcpyDeviceToHost, st));
 		TRY(readback(h, S_UZ, 5));
 		if(h->hscal[S_UZ + 4] != 0.0)
 			return fail(h, CITCOM_GPU_ERR_NOCONV, "solve_Ahat_p_fhat: division by zero in head of incompressibility iteration");
 		const double alpha = h->hscal[S_UZ + 3];
 		const double vdotv = h->hscal[S_DOT], u1u1 = h->hscal[S_DOT + 1];
-		const double pdotp = h->hscal[S_DOT + 4], s2s2 = h->hscal[S_DOT + 5];
+		const double pdotp = h->hscal[S_DOT + 4], s2s2 = h->hscal[S_DOT + 5], r2r2 = h->hscal[S_DOT + 6];
 		dpressure = alpha * std::sqrt(s2s2 / (1.0e-32 + pdotp));
 		dvelocity = alpha * std::sqrt(u1u1 / (1.0e-32 + vdotv));
+		cont = continuity(r2r2, vdotv, neq, npno);
 		++count;
 		if(h->verbose)
-			fprintf(stderr, "AhatP (%03d) v %12.6e dv/v %9.3e p %12.6e dp/p %9.3e mg %d\n", count, std::sqrt(vdotv / neq),
-			        dvelocity, std::sqrt(pdotp / npno), dpressure, h->stats.mg_passes);
+			fprintf(stderr, "AhatP (%03d) v %12.6e dv/v %9.3e p %12.6e dp/p %9.3e cont %9.3e mg %d\n", count,
+			        std::sqrt(vdotv / neq), dvelocity, std::sqrt(pdotp / npno), dpressure, cont, h->stats.mg_passes);
 		sh = s1; s1 = s2; s2 = sh;
 		sh = r0; r0 = r1; r1 = r2; r2 = sh;
 		sh = z0; z0 = z1; z1 = sh;

@@ -89,7 +89,18 @@ typedef struct citcom_gpu_config
 	double sdepv_expt[8], sdepv_trns[8];
 	double sdepv_misfit, sdepv_iter_damp;
 	int max_sdep_visc_iter;
+	/* Uzawa stopping rule.  CITCOM_GPU_STOP_REFERENCE (0): the reference's,
+	 * dv/v and dp/p below accuracy or piterations iterations
+	 * (Stokes_flow_Incomp.c:393, 442-443).  CITCOM_GPU_STOP_RESIDUAL (1): no
+	 * counterpart in the reference; the solve runs until both FP64 residuals
+	 * of the solution are at most accuracy: |F - K U - G P| / |F| (momentum)
+	 * and |B U| / (|U| sqrt(npno/neq)) (continuity), or piterations Uzawa
+	 * iterations (see citcom_gpu_solve_Ahat_p_fhat). */
+	int stop_rule;
 } citcom_gpu_config;
+
+#define CITCOM_GPU_STOP_REFERENCE 0
+#define CITCOM_GPU_STOP_RESIDUAL 1
 
 /* Time-step bookkeeping that PG_timestep updates in E->advection / E->monitor. */
 typedef struct citcom_gpu_advection
@@ -118,6 +129,11 @@ typedef struct citcom_gpu_stats
 	double warm_residual;       /* |F - K U - G P| / |F| of the network's guess */
 	double base_residual;       /* the same of the resident U, P it was compared with */
 	double pass_ms;             /* device time of the multigrid passes (multi_grid calls) */
+	/* residual rule only (CITCOM_GPU_STOP_RESIDUAL): the FP64 residuals at the
+	 * end of the last Uzawa solve and the velocity corrections it made */
+	double final_momentum;      /* |F - K U - G P| / |F| */
+	double final_continuity;    /* |B U| / (|U| sqrt(npno/neq)) */
+	int corrections;
 } citcom_gpu_stats;
 
 /* Allocates every device buffer the solver will use (on the current
@@ -146,7 +162,15 @@ int citcom_gpu_assemble_forces(citcom_gpu *h, const double *T, double *F, double
 /* solve_Ahat_p_fhat (Stokes_flow_Incomp.c:295): Uzawa / Schur-complement
  * PCG with the multigrid velocity solve.  V (neq) and P (npno) are updated
  * in place; *steps_max is the iteration cap on entry and the iteration
- * count on return; *initial_residual receives the reference's return value. */
+ * count on return; *initial_residual receives the reference's return value.
+ * With stop_rule CITCOM_GPU_STOP_RESIDUAL the loop tests the continuity
+ * residual (from the recursively updated B V) before every iteration; once
+ * it is at most imp, the momentum residual is evaluated with the FP64
+ * operator, and if it is above imp a velocity correction
+ * V += K^-1 (F - G P - K V) (the reference's own head, :360-366, solved to
+ * imp/2 relative to |F|) follows, B V is recomputed and the iteration
+ * restarts its search direction if continuity is above imp again.  At most 8
+ * corrections are made per solve. */
 int citcom_gpu_solve_Ahat_p_fhat(citcom_gpu *h, double *V, double *P, const double *F, double imp, int *steps_max,
                                  double *initial_residual);
 int citcom_gpu_solve_Ahat_p_fhat_device(citcom_gpu *h, double *dV, double *dP, const double *dF, double imp, int *steps_max,

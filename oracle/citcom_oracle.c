@@ -66,6 +66,10 @@ struct oracle
 	   rates, and how often visc_from_S ran (its static `visits`) */
 	double *oldU, *edot;
 	int sdepv_visits;
+	/* the residual rule's last momentum and continuity residuals and its
+	   velocity corrections */
+	double last_momentum, last_continuity;
+	int last_corrections;
 };
 
 static void *xcalloc(size_t n, size_t s)
@@ -1109,41 +1113,101 @@ int oracle_solve_del2_u(oracle *o, double *d0, double *F, double acc, int *mg_ca
 	return valid;
 }
 
-/* solve_Ahat_p_fhat (Stokes_flow_Incomp.c:295-497); returns the initial
- * pressure residual as the reference does */
-double oracle_solve_Ahat_p_fhat(oracle *o, double *V, double *P, const double *F, double imp, int *steps, int *del2_calls, int *mg_calls)
+/* The head of solve_Ahat_p_fhat (Stokes_flow_Incomp.c:360-371): V += K^-1
+ * (F - G P - K V) solved to acc, then r1 = B V; returns |r1| / sqrt(npno). */
+static double uzawa_head(oracle *o, double *V, const double *P, const double *F, double acc, double *r1, int *del2_calls,
+                         int *mg_calls)
 {
 	const level *f = &o->lv[o->L - 1];
 	const int npno = f->nel, neq = f->neq, lev = o->L - 1;
-	const int gnpno = npno, gneq = neq;
-	double v_res, residual, alpha, delta, s2dotAhat, r0dotr0, r1dotz1;
-	double vdotv, pdotp;
-	double dpressure = 1.0, dvelocity = 1.0;
-	double *r0 = o->r0, *r1 = o->r1, *r2 = o->r2, *z0 = o->z0, *z1 = o->z1, *s1 = o->s1, *s2 = o->s2, *sh;
 	double *Ah = o->Ah, *u1 = o->u1;
-	int i, j, count = 0, valid;
-
-	v_res = sqrt(vdot(neq, F, F) / gneq);
+	int i;
 	oracle_grad_p(o, lev, P, Ah);
 	oracle_kmul(o, lev, V, u1, 1);
 	for(i = 0; i < neq; i++)
 		Ah[i] = F[i] - Ah[i] - u1[i];
 	oracle_strip_bcs(o, lev, Ah);
-	valid = oracle_solve_del2_u(o, u1, Ah, imp * v_res, mg_calls);
+	oracle_solve_del2_u(o, u1, Ah, acc, mg_calls);
 	if(del2_calls)
 		(*del2_calls)++;
 	oracle_strip_bcs(o, lev, u1);
 	for(i = 0; i < neq; i++)
 		V[i] += u1[i];
 	oracle_div_u(o, lev, V, r1);
-	residual = sqrt(vdot(npno, r1, r1) / gnpno);
+	return sqrt(vdot(npno, r1, r1) / npno);
+}
 
-	while((count < *steps) && (dpressure >= imp || dvelocity >= imp))
+/* continuity residual of the residual rule: |B V| / (|V| sqrt(npno/neq)) */
+static double continuity(double bvbv, double vv, int neq, int npno)
+{
+	return sqrt(bvbv / (vv > 0.0 ? vv : 1e-300) * ((double)neq / (double)npno));
+}
+
+/* solve_Ahat_p_fhat (Stokes_flow_Incomp.c:295-497); returns the initial
+ * pressure residual as the reference does.  stop_rule 0 is the reference's
+ * loop (dv/v and dp/p, :393, 442-443).  stop_rule 1 is the GPU library's
+ * residual rule (no counterpart in the reference), restated step for step:
+ * before every iteration the continuity residual of the recursively updated
+ * r1 = B V is tested; once it is at most imp the momentum residual
+ * |F - K V - G P| / |F| is evaluated, and above imp a velocity correction
+ * (the head again, solved to imp/2 relative to |F|) follows and the search
+ * direction restarts; at most 8 corrections. */
+double oracle_solve_Ahat_p_fhat(oracle *o, double *V, double *P, const double *F, double imp, int *steps, int *del2_calls, int *mg_calls)
+{
+	const level *f = &o->lv[o->L - 1];
+	const int npno = f->nel, neq = f->neq, lev = o->L - 1;
+	const int gneq = neq;
+	const int resid_rule = o->p.stop_rule == 1;
+	double v_res, ff, residual, alpha, delta, s2dotAhat, r0dotr0, r1dotz1;
+	double vdotv, pdotp, cont = 0.0;
+	double dpressure = 1.0, dvelocity = 1.0;
+	double *r0 = o->r0, *r1 = o->r1, *r2 = o->r2, *z0 = o->z0, *z1 = o->z1, *s1 = o->s1, *s2 = o->s2, *sh;
+	double *Ah = o->Ah, *u1 = o->u1;
+	int i, j, count = 0, valid, restart = 1;
+
+	ff = vdot(neq, F, F);
+	v_res = sqrt(ff / gneq);
+	o->last_momentum = o->last_continuity = 0.0;
+	o->last_corrections = 0;
+	residual = uzawa_head(o, V, P, F, imp * v_res, r1, del2_calls, mg_calls);
+	if(resid_rule)
+		cont = continuity(residual * residual * npno, vdot(neq, V, V), neq, npno);
+
+	for(;;)
 	{
+		if(resid_rule)
+		{
+			if(cont <= imp)
+			{
+				double rr = 0.0, mom, rc;
+				oracle_grad_p(o, lev, P, Ah);
+				oracle_kmul(o, lev, V, u1, 1);
+				for(i = 0; i < neq; i++)
+				{
+					const double r = F[i] - Ah[i] - u1[i];
+					rr += r * r;
+				}
+				mom = sqrt(rr / (ff > 0.0 ? ff : 1.0));
+				o->last_momentum = mom;
+				o->last_continuity = cont;
+				if(mom <= imp || o->last_corrections >= 8)
+					break;
+				rc = uzawa_head(o, V, P, F, 0.5 * imp * v_res, r1, del2_calls, mg_calls);
+				o->last_corrections++;
+				cont = continuity(rc * rc * npno, vdot(neq, V, V), neq, npno);
+				o->last_continuity = cont;
+				restart = 1;
+				continue;
+			}
+			if(count >= *steps)
+				break;
+		}
+		else if(!((count < *steps) && (dpressure >= imp || dvelocity >= imp)))
+			break;
 		for(j = 0; j < npno; j++)
 			z1[j] = f->BPI[j] * r1[j];
 		r1dotz1 = vdot(npno, r1, z1);
-		if(count == 0)
+		if(restart)
 			for(j = 0; j < npno; j++)
 				s2[j] = z1[j];
 		else
@@ -1153,6 +1217,7 @@ double oracle_solve_Ahat_p_fhat(oracle *o, double *V, double *P, const double *F
 			for(j = 0; j < npno; j++)
 				s2[j] = z1[j] + delta * s1[j];
 		}
+		restart = 0;
 		oracle_grad_p(o, lev, s2, Ah);
 		valid = oracle_solve_del2_u(o, u1, Ah, imp * v_res, mg_calls);
 		if(del2_calls)
@@ -1173,6 +1238,8 @@ double oracle_solve_Ahat_p_fhat(oracle *o, double *V, double *P, const double *F
 		pdotp = vdot(npno, P, P);
 		dpressure = alpha * sqrt(vdot(npno, s2, s2) / (1.0e-32 + pdotp));
 		dvelocity = alpha * sqrt(vdot(neq, u1, u1) / (1.0e-32 + vdotv));
+		if(resid_rule)
+			cont = continuity(vdot(npno, r2, r2), vdotv, neq, npno);
 		count++;
 		sh = s1; s1 = s2; s2 = sh;
 		sh = r0; r0 = r1; r1 = r2; r2 = sh;
@@ -1182,6 +1249,13 @@ double oracle_solve_Ahat_p_fhat(oracle *o, double *V, double *P, const double *F
 	o->r0 = r0; o->r1 = r1; o->r2 = r2; o->z0 = z0; o->z1 = z1; o->s1 = s1; o->s2 = s2;
 	*steps = count;
 	return residual;
+}
+
+void oracle_last_residuals(const oracle *o, double out[3])
+{
+	out[0] = o->last_momentum;
+	out[1] = o->last_continuity;
+	out[2] = o->last_corrections;
 }
 
 /* general_stokes_solver (Drive_solvers.c:45-165), with

@@ -49,6 +49,10 @@ typedef struct oracle_params
 	double sdepv_expt[ORACLE_MAX_MAT], sdepv_trns[ORACLE_MAX_MAT];
 	double sdepv_misfit, sdepv_iter_damp;
 	int max_sdep_visc_iter;
+	/* 0: the reference's Uzawa stopping rule (dv/v, dp/p); 1: the residual
+	   rule of the GPU library (both FP64 residuals at most accuracy, velocity
+	   corrections), restated in oracle_solve_Ahat_p_fhat */
+	int stop_rule;
 } oracle_params;
 
 typedef struct oracle oracle;
@@ -97,6 +101,8 @@ void oracle_grad_p(oracle *o, int lev, const double *P, double *gradP);
 double oracle_multi_grid(oracle *o, double *d1, double *F, double acc);
 int oracle_solve_del2_u(oracle *o, double *d0, double *F, double acc, int *mg_calls);
 double oracle_solve_Ahat_p_fhat(oracle *o, double *V, double *P, const double *F, double imp, int *steps, int *del2_calls, int *mg_calls);
+/* residual rule of the last solve: momentum, continuity, corrections */
+void oracle_last_residuals(const oracle *o, double out[3]);
 /* general_stokes_solver: conform BCs, forces, viscosity, stiffness, Uzawa, V */
 double oracle_stokes(oracle *o, int *steps, int *del2_calls, int *mg_calls);
 

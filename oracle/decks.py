@@ -48,6 +48,9 @@ class Case:
     vhighstep: int = 3
     piterations: int = 375
     accuracy: float = 1.0e-6
+    # Uzawa stopping rule: 0 the reference's (dv/v, dp/p); 1 the residual rule
+    # (GPU library and oracle only; the reference build has no such rule)
+    stop_rule: int = 0
     # energy equation
     adv_sub_iterations: int = 2
     finetunedt: float = 0.75

@@ -60,6 +60,7 @@ class _Params(ctypes.Structure):
         ("sdepv_misfit", ctypes.c_double),
         ("sdepv_iter_damp", ctypes.c_double),
         ("max_sdep_visc_iter", ctypes.c_int),
+        ("stop_rule", ctypes.c_int),
     ]
 
 
@@ -131,6 +132,7 @@ def lib():
         L.oracle_solve_del2_u.argtypes = [P, D, D, ctypes.c_double, I]
         L.oracle_solve_Ahat_p_fhat.restype = ctypes.c_double
         L.oracle_solve_Ahat_p_fhat.argtypes = [P, D, D, D, ctypes.c_double, I, I, I]
+        L.oracle_last_residuals.argtypes = [P, D]
         L.oracle_stokes.restype = ctypes.c_double
         L.oracle_stokes.argtypes = [P, I, I, I]
         L.oracle_heat_flux.argtypes = [P, D, D]
@@ -180,6 +182,7 @@ def params_from_case(case, gs_colored: bool = False) -> _Params:
     p.finetunedt = case.finetunedt
     p.fixed_timestep = case.fixed_timestep
     p.gs_colored = int(gs_colored)
+    p.stop_rule = int(getattr(case, "stop_rule", 0))
     p.sdepv = int(getattr(case, "sdepv", False))
     if p.sdepv:
         p.sdepv_rheology = case.sdepv_rheology
@@ -360,12 +363,19 @@ class Oracle:
         r = lib().oracle_solve_Ahat_p_fhat(self.h, lib().oracle_U(self.h), lib().oracle_P(self.h),
                                            lib().oracle_F(self.h), imp, ctypes.byref(st), ctypes.byref(c),
                                            ctypes.byref(m))
-        return dict(residual=r, uzawa=st.value, del2_calls=c.value, mg_calls=m.value)
+        return dict(residual=r, uzawa=st.value, del2_calls=c.value, mg_calls=m.value, **self.last_residuals())
+
+    def last_residuals(self):
+        """The residual rule's final momentum and continuity residuals and
+        velocity corrections of the last solve (zeros under the reference rule)."""
+        out = np.zeros(3)
+        lib().oracle_last_residuals(self.h, _dp(out))
+        return dict(momentum=float(out[0]), continuity=float(out[1]), corrections=int(out[2]))
 
     def stokes(self):
         s, c, m = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
         r = lib().oracle_stokes(self.h, ctypes.byref(s), ctypes.byref(c), ctypes.byref(m))
-        return dict(residual=r, uzawa=s.value, del2_calls=c.value, mg_calls=m.value)
+        return dict(residual=r, uzawa=s.value, del2_calls=c.value, mg_calls=m.value, **self.last_residuals())
 
     def pg_timestep(self):
         lib().oracle_pg_timestep(self.h)

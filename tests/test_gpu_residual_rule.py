@@ -1,0 +1,138 @@
+"""The residual stopping rule (stop_rule 1) of the GPU library against the
+oracle's restatement of the same rule, and on meshes of benchmark scale.
+
+The rule stops the Uzawa solve once both FP64 residuals of the solution are at
+most `accuracy`: |F - K U - G P| / |F| and |B U| / (|U| sqrt(npno/neq)).
+Against the oracle in the GPU's 8-colour order the arithmetic is the same, so
+every solve must take the same Uzawa iterations, multigrid passes and velocity
+corrections, and agree to FP64 rounding.  The 32^3 case is the 64^3 benchmark
+box (eta = exp(-ln(1e3) T), Ra 1e5, seeded T0 = 1 - z + U(-0.01, 0.01)) on
+four levels instead of five: one cold solve and one time step.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from oracle.decks import Case, conductive_T0
+from tests.golden.make_golden import small_case
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def box_case(size):
+    levels = {16: 3, 32: 4}[size]
+    return Case(mgunit=(4, 4, 4), levels=levels, rayleigh=1e5, tdepv=True, visc0=(1.0,), viscE=(math.log(1e3),),
+                viscT=(0.0,), accuracy=1e-6, piterations=1000, stop_rule=1)
+
+
+def seeded_T0(case, seed=0):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    z = np.linspace(0.0, case.dimen[2], case.noz)
+    T = np.empty((case.noy, case.nox, case.noz))
+    T[:] = 1.0 - z / case.dimen[2]
+    T += rng.uniform(-0.01, 0.01, size=T.shape)
+    T[:, :, 0] = 1.0
+    T[:, :, -1] = 0.0
+    return T.reshape(-1)
+
+
+@pytest.fixture(scope="module")
+def cg():
+    import citcomcu_gb300 as cg
+    cg.build()
+    return cg
+
+
+def steps_against_oracle(cg, olib, case, T0, nsteps, precision=0):
+    s = cg.Solver(cg.Config.like(case, precision=precision))
+    o = olib.Oracle(case, gs_colored=True)
+    f = s.fine
+    U, P, Tdot = np.zeros(f["neq"]), np.zeros(f["nel"]), np.zeros(f["nno"])
+    T = T0.copy()
+    o.set_T(T0)
+    o.thermal_buoyancy()
+    out = []
+    for step in range(nsteps + 1):
+        if step:
+            s.PG_timestep(T, Tdot, V)
+            o.pg_timestep()
+        V = s.general_stokes_solver(T, U, P)
+        st = s.stats()
+        info = o.stokes()
+        nut, _ = s.heat_flux(T, V)
+        onut, _ = o.heat_flux()
+        out.append(dict(step=step, st=st, info=info, U=rel(U, o.U()[: f["neq"]]), P=rel(P, o.P()),
+                        T=float(np.max(np.abs(T - o.T()))), nut=(nut, onut), res=s.stokes_residuals()))
+    s.close()
+    return out
+
+
+@pytest.mark.parametrize("name", ["small", "box32"])
+def test_residual_rule_matches_coloured_oracle(cg, oracle_lib, name):
+    if name == "small":
+        case = small_case()
+        case.accuracy, case.piterations, case.stop_rule = 1e-6, 1000, 1
+        T0 = conductive_T0(case, amp=0.01, seed=0)
+        nsteps = 3
+    else:
+        case = box_case(32)
+        T0 = seeded_T0(case)
+        nsteps = 1
+    for r in steps_against_oracle(cg, oracle_lib, case, T0, nsteps):
+        st, info = r["st"], r["info"]
+        print(r["step"], st["uzawa"], info["uzawa"], st["mg_passes"], info["mg_calls"], st["corrections"],
+              info["corrections"], r["res"], r["U"], r["nut"])
+        assert st["uzawa"] == info["uzawa"] and st["mg_passes"] == info["mg_calls"], r
+        assert st["corrections"] == info["corrections"], r
+        # both residuals of the GPU solution at the tolerance, in FP64
+        assert r["res"][0] <= case.accuracy and r["res"][1] <= case.accuracy, r
+        assert abs(st["final_momentum"] - info["momentum"]) <= 1e-6 * info["momentum"] + 1e-14, r
+        assert r["U"] < 1e-9 and r["P"] < 1e-8 and r["T"] < 1e-11, r
+        assert abs(r["nut"][0] - r["nut"][1]) < 1e-11 * abs(r["nut"][1]), r
+
+
+def test_residual_rule_mixed_precision(cg):
+    """FP32 multigrid inside FP64 refinement under the residual rule: its
+    solution meets both FP64 residuals, and differs from the FP64 plain
+    solution by no more than the two solutions' tolerance carried through the
+    operator (U, P to 1e-4, Nu to 1e-6)."""
+    case = box_case(16)
+    T0 = seeded_T0(case)
+    res = {}
+    for prec in (0, 1):
+        s = cg.Solver(cg.Config.like(case, precision=prec))
+        f = s.fine
+        U, P = np.zeros(f["neq"]), np.zeros(f["nel"])
+        V = s.general_stokes_solver(T0, U, P)
+        res[prec] = dict(U=U, P=P, nu=s.heat_flux(T0, V)[0], r=s.stokes_residuals(), st=s.stats())
+        s.close()
+    print(res[0]["st"], res[1]["st"], res[0]["r"], res[1]["r"])
+    assert max(res[1]["r"]) <= case.accuracy
+    assert rel(res[1]["U"], res[0]["U"]) < 1e-4 and rel(res[1]["P"], res[0]["P"]) < 1e-4
+    assert abs(res[1]["nu"] - res[0]["nu"]) < 1e-6 * abs(res[0]["nu"])
+
+
+def test_residual_rule_stops_earlier_than_the_reference_rule(cg):
+    """The reference's rule (dv/v and dp/p below 1e-6) runs this cold solve to
+    its iteration cap; the residual rule stops once the solution meets the
+    tolerance, and the reference rule's longer solve meets it too."""
+    case = box_case(16)
+    T0 = seeded_T0(case)
+    out = {}
+    for rule in (0, 1):
+        s = cg.Solver(cg.Config.like(case, precision=0, stop_rule=rule, piterations=375))
+        f = s.fine
+        U, P = np.zeros(f["neq"]), np.zeros(f["nel"])
+        s.general_stokes_solver(T0, U, P)
+        out[rule] = (s.stats()["uzawa"], s.stokes_residuals())
+        s.close()
+    print(out)
+    assert out[1][0] < out[0][0]
+    assert max(out[1][1]) <= 1e-6
