@@ -217,6 +217,7 @@ _SIGNATURES = {
     "citcom_gpu_op_multi_grid": (ctypes.c_int, [_H, _D, _D, _D]),
     "citcom_gpu_op_solve_del2_u": (ctypes.c_int, [_H, _D, _D, ctypes.c_double, _I]),
     "citcom_gpu_op_diagonals": (ctypes.c_int, [_H, ctypes.c_int, _D, _D]),
+    "citcom_gpu_test_hold_tile_copy": (ctypes.c_int, []),
     "citcom_gpu_heat_flux_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _D, ctypes.c_void_p,
                                                     ctypes.c_void_p, _D, _D]),
     "citcom_nn_create": (ctypes.c_int, [_H, ctypes.c_int, ctypes.c_uint, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
@@ -230,6 +231,7 @@ _SIGNATURES = {
     "citcom_nn_record": (ctypes.c_int, [_H]),
     "citcom_nn_train": (ctypes.c_int, [_H, ctypes.c_int, ctypes.c_int, ctypes.c_double, _D]),
     "citcom_nn_attach": (ctypes.c_int, [_H, ctypes.c_int]),
+    "citcom_nn_set_mode": (ctypes.c_int, [_H, ctypes.c_int]),
     "citcom_nn_predict": (ctypes.c_int, [_H, _D, _D]),
     "citcom_nn_forward": (ctypes.c_int, [_H, _F, _F]),
     "citcom_nn_loss_grad": (ctypes.c_int, [_H, _F, _F, _D, _F]),
@@ -614,14 +616,24 @@ class WarmStart:
     `record()` adds the solver's converged state to the training set,
     `train()` runs Adam steps on it, `attach()` makes every Stokes solve of the
     solver start from the network's guess when that guess has the smaller
-    momentum residual.  Destroy (close) it before its solver."""
+    Uzawa initial residual.  With mode=INCREMENT the network instead predicts
+    the change of U and P from the change of T since the last solve, and the
+    solve starts from the previous solution plus that change scaled by the
+    step minimising the momentum residual.  Destroy (close) it before its
+    solver."""
 
-    def __init__(self, solver: Solver, level: int = -1, seed: int = 0, capacity: int = 64):
+    ABSOLUTE = 0
+    INCREMENT = 1
+
+    def __init__(self, solver: Solver, level: int = -1, seed: int = 0, capacity: int = 64, mode: int = 0):
         self.solver = solver
         self.lib = solver.lib
         h = ctypes.c_void_p()
         solver._check(self.lib.citcom_nn_create(solver.h, level, seed, capacity, ctypes.byref(h)))
         self.h = h
+        self.mode = mode
+        if mode:
+            self._check(self.lib.citcom_nn_set_mode(self.h, mode))
         info = (ctypes.c_int * 6)()
         self._check(self.lib.citcom_nn_info(self.h, info))
         self.grid = (info[0], info[1], info[2])

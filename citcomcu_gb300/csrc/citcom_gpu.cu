@@ -61,6 +61,7 @@ struct citcom_gpu
 	float *K32[CITCOM_MAX_LEVELS];
 	float *BI32[CITCOM_MAX_LEVELS];
 	float4 *Kt32[CITCOM_MAX_LEVELS];  // padded FP32 stencil of the levels k_gs_tiny smooths, else null
+	float *eta32[CITCOM_MAX_LEVELS];  // FP32 Gauss-point viscosity of the levels the matrix-free smoother relaxes, else null
 	double *BPI;
 	MG<double> mg64;
 	MG<float> mg32;
@@ -88,6 +89,7 @@ struct citcom_gpu
 	bool no_graph;
 	bool level_timing;            // CITCOM_GPU_LEVEL_TIMING: time every smoother call (no graph)
 	bool no_tiny;                 // CITCOM_GPU_NO_TINY: coarsest FP32 levels use k_gs_small instead of k_gs_tiny
+	bool mf;                      // matrix-free FP32 smoother on the large box levels (CITCOM_GPU_MF)
 	// FP32 multigrid work of levels 0..co_LC runs as one cluster program per
 	// stretch of consecutive coarse operations (co_LC = -1: off;
 	// CITCOM_GPU_NO_CLUSTER disables it)
@@ -109,6 +111,9 @@ struct citcom_gpu
 	citcom_nn *warm;   // warm-start network attached to the Stokes solve (not owned), or null
 	double diff_ts;    // diffusive time-step limit of the finest level
 	double *oldU;      // the previous viscosity iteration's U (general_stokes_solver's oldU, kept across solves)
+	double *T_sol;     // T of the last completed Stokes solve (the increment warm start's reference state)
+	bool T_sol_valid;  // false until a solve completes after the last load_state
+	unsigned state_gen;  // counts load_state calls (a new state sequence)
 	double *edot;      // strain-rate invariant per fine element
 	int sdepv_visits;  // calls of visc_from_S so far (the first one takes a unit strain rate)
 	// output steps: device staging of the fields (allocated on first use), the
@@ -138,6 +143,13 @@ struct citcom_nn
 	double *work;           // FP64 scratch of the input/target/guess kernels
 	double su, sp, mp;      // output scales per unit anomaly RMS: velocity, pressure; pressure offset
 	bool scaled;
+	// increment mode (CITCOM_NN_INCREMENT): the state of the previous record,
+	// the fine temperature increment, and the last line-search step
+	int mode;
+	double *Tp, *Up, *Pp, *dT;
+	bool have_prev;
+	unsigned prev_gen;
+	double alpha;
 	bool attached;
 	unsigned long long rng;
 	std::vector<void *> allocs;
@@ -232,6 +244,41 @@ int readback(citcom_gpu *h, int slot, int n)
 	CK(cudaMemcpyAsync(h->hscal + slot, h->dscal + slot, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
 	CK(cudaStreamSynchronize(h->st));
 	return CITCOM_GPU_OK;
+}
+
+// The error words of the kernels' bounded waits (the tile kernels' g_tile_err,
+// the cluster program's dscal[S_ERR]) to zero, on the stream.
+int device_errors_reset(citcom_gpu *h)
+{
+	if(tile_error_reset_async(h->st) != 0)
+		return fail(h, CITCOM_GPU_ERR_CUDA, "clearing the tile kernels' error word failed");
+	CK(cudaMemsetAsync(h->dscal + S_ERR, 0, sizeof(double), h->st));
+	return CITCOM_GPU_OK;
+}
+
+// After h->hscal[S_TERR] and [S_ERR] were read back: CITCOM_GPU_ERR_CUDA with
+// the reason when a bounded wait ran out (the words are cleared again, so the
+// next call starts clean), else OK.
+int device_errors_report(citcom_gpu *h, const char *where)
+{
+	const bool tile = h->hscal[S_TERR] != 0.0, clus = h->hscal[S_ERR] != 0.0;
+	if(!tile && !clus)
+		return CITCOM_GPU_OK;
+	h->hscal[S_TERR] = h->hscal[S_ERR] = 0.0;
+	device_errors_reset(h);
+	cudaStreamSynchronize(h->st);
+	return fail(h, CITCOM_GPU_ERR_CUDA, "%s: %s", where,
+	            tile ? "a stencil tile copy did not arrive (a bounded wait ran out)"
+	                 : "a wait of the cluster smoother timed out");
+}
+
+// reads both error words (synchronises) and reports as above
+int device_errors_check(citcom_gpu *h, const char *where)
+{
+	if(tile_error_async(h->hscal + S_TERR, h->st) != 0)
+		return fail(h, CITCOM_GPU_ERR_CUDA, "%s: reading the tile kernels' error word failed", where);
+	TRY(readback(h, S_ERR, 1));
+	return device_errors_report(h, where);
 }
 
 Rheo rheo_of(const citcom_gpu_config &c)
@@ -353,11 +400,23 @@ template <typename T> void gs_inner(citcom_gpu *h, MG<T> &B, int lev, T *d, cons
 {
 	const Lvl &L = h->lv[lev];
 	if constexpr(std::is_same<T, float>::value)
+	{
 		if(h->Kt32[lev] && !h->no_tiny)
 		{
 			launch_gs_tiny(h->st, L, h->Kt32[lev], B.BI[lev], F, d, cycles, zero_start);
 			return;
 		}
+		if(h->eta32[lev])
+		{
+			// matrix-free colours (mf.cu) instead of the stored stencil
+			if(zero_start)
+				cudaMemsetAsync(d, 0, sizeof(T) * L.neq, h->st);
+			for(int c = 0; c < cycles; ++c)
+				for(int col = 0; col < 8; ++col)
+					launch_mf_gs(h->st, L, h->eta32[lev], h->cfg.aug_lagr, h->cfg.aug_number, B.BI[lev], F, d, col);
+			return;
+		}
+	}
 	if(gs_small_fits(L, sizeof(T)))
 	{
 		launch_gs_small<T>(h->st, L, B.K[lev], B.BI[lev], F, d, cycles, zero_start);
@@ -560,10 +619,7 @@ int solve_del2_u(citcom_gpu *h, double acc, int *valid)
 		if(tile_error_async(h->hscal + S_TERR, h->st) != 0)
 			return fail(h, CITCOM_GPU_ERR_CUDA, "solve_del2_u: reading the tile kernels' error word failed");
 		TRY(readback(h, S_RES, 2));
-		if(h->hscal[S_ERR] != 0.0)
-			return fail(h, CITCOM_GPU_ERR_CUDA, "solve_del2_u: a wait of the cluster smoother timed out");
-		if(h->hscal[S_TERR] != 0.0)
-			return fail(h, CITCOM_GPU_ERR_CUDA, "solve_del2_u: a stencil tile copy did not arrive");
+		TRY(device_errors_report(h, "solve_del2_u"));
 		residual = std::sqrt(h->hscal[S_RES] / neq);
 		{
 			float ms = 0.f;
@@ -595,6 +651,7 @@ int solve_del2_u(citcom_gpu *h, double acc, int *valid)
 // ---------------------------------------------------------------- Uzawa
 
 int nn_guess(citcom_nn *n);
+int nn_increment_start(citcom_nn *n, double *V, double *P, const double *F, double ff);
 
 // The head of solve_Ahat_p_fhat (Stokes_flow_Incomp.c:360-371): the velocity
 // correction V += K^-1 (F - G P - K V) for the pressure P, then r1 = B V and
@@ -665,8 +722,14 @@ int uzawa(citcom_gpu *h, double *V, double *P, const double *F, double imp, int 
 	if(!h->stiffness_ready)
 		return fail(h, CITCOM_GPU_ERR_STATE, "construct_stiffness_B_matrix has not been called");
 
+	// F.F, and the error words of the kernels since the last check (operator
+	// assembly: the coarsest level's dense smoother is built by the cluster
+	// program's smoother)
 	launch_dot(st, neq, F, F, red_of(h), h->dscal + S_R0);
-	TRY(readback(h, S_R0, 1));
+	if(tile_error_async(h->hscal + S_TERR, st) != 0)
+		return fail(h, CITCOM_GPU_ERR_CUDA, "solve_Ahat_p_fhat: reading the tile kernels' error word failed");
+	TRY(readback(h, 0, S_R0 + 1));
+	TRY(device_errors_report(h, "solve_Ahat_p_fhat"));
 	const double ff = h->hscal[S_R0];
 	const double v_res = std::sqrt(ff / neq);
 
@@ -679,7 +742,18 @@ int uzawa(citcom_gpu *h, double *V, double *P, const double *F, double imp, int 
 	double residual = 0.0, vv = 0.0;
 	double *vvp = resid_rule ? &vv : nullptr;
 	citcom_nn *n = h->warm;
-	if(n && n->scaled)
+	if(n && n->scaled && n->mode == CITCOM_NN_INCREMENT)
+	{
+		// the previous solution plus the network's increment for T - T_sol,
+		// scaled by the step that minimises the momentum residual (0 keeps the
+		// previous solution); then the one head of the reference
+		if(h->T_sol_valid)
+			TRY(nn_increment_start(n, V, P, F, ff));
+		TRY(uzawa_start(h, V, P, F, imp * v_res, h->r1, &residual, vvp));
+		if(nn_device_error(n->net) != 0)
+			return fail(h, CITCOM_GPU_ERR_CUDA, "warm-start network: a tensor-core wait timed out");
+	}
+	else if(n && n->scaled)
 	{
 		double r_net = 0.0, vv_net = 0.0;
 		TRY(nn_guess(n));
@@ -792,6 +866,8 @@ int construct_stiffness(citcom_gpu *h)
 		                need32 ? h->K32[l] : nullptr, need64 ? h->BI64[l] : nullptr, need32 ? h->BI32[l] : nullptr);
 		if(h->Kt32[l])
 			launch_tiny_stencil(h->st, h->lv[l], h->K32[l], h->Kt32[l]);
+		if(h->eta32[l])
+			launch_mf_eta32(h->st, h->lv[l], h->evi[l], h->eta32[l]);
 		if(l == 0 && h->co_dense)
 			launch_coarse_dense_build(h->st, h->lv[0], h->Kt32[0], h->BI32[0], c.vlowstep, h->co_dense_work, h->co_dense,
 			                          h->dscal + S_ERR);
@@ -893,6 +969,8 @@ int stokes_resident(citcom_gpu *h)
 	h->stats.uzawa_iterations = uzawa_total;
 	h->stats.visc_iterations = vcount;
 	h->stats.visc_misfit = misfit;
+	CK(cudaMemcpyAsync(h->T_sol, h->T, sizeof(double) * Lf.nno, cudaMemcpyDeviceToDevice, h->st));
+	h->T_sol_valid = true;
 	CK(cudaEventRecord(h->ev1, h->st));
 	CK(cudaEventSynchronize(h->ev1));
 	float ms = 0.f;
@@ -1058,6 +1136,8 @@ int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 			h->no_graph = true;
 		const char *tn = getenv("CITCOM_GPU_NO_TINY");
 		h->no_tiny = tn && tn[0] && tn[0] != '0';
+		const char *mf = getenv("CITCOM_GPU_MF");
+		h->mf = mf && mf[0] && mf[0] != '0';
 		const char *q = getenv("CITCOM_GPU_NO_PDL");
 		if(q && q[0] && q[0] != '0')
 			g_use_pdl = 0;
@@ -1150,12 +1230,17 @@ int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 				TRYC(dalloc(h, &h->BI64[l], (size_t)3 * L.npad));
 			}
 			h->Kt32[l] = nullptr;
+			h->eta32[l] = nullptr;
 			if(need32)
 			{
 				TRYC(dalloc(h, &h->K32[l], cg_kwords(L)));
 				TRYC(dalloc(h, &h->BI32[l], (size_t)3 * L.npad));
 				if(gs_tiny_fits(L, sizeof(float)) || l <= h->co_LC)
 					TRYC(dalloc(h, &h->Kt32[l], (size_t)63 * L.nno));
+				// box levels smoothed colour by colour (not by the single-CTA or
+				// cluster programs): matrix-free unless switched off
+				else if(h->mf && !L.aos && !L.sphere && !gs_small_fits(L, sizeof(float)))
+					TRYC(dalloc(h, &h->eta32[l], (size_t)8 * L.nel));
 			}
 			h->mg64.K[l] = h->K64[l];
 			h->mg64.BI[l] = h->BI64[l];
@@ -1212,6 +1297,7 @@ int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 		TRYC(dalloc(h, &h->u1, Lf.neq + 2));
 		TRYC(dalloc(h, &h->r64, Lf.neq + 2));
 		TRYC(dalloc(h, &h->oldU, Lf.neq + 2));
+		TRYC(dalloc(h, &h->T_sol, Lf.nno));
 		TRYC(dalloc(h, &h->edot, Lf.nel));
 		TRYC(dalloc(h, &h->Eres, (size_t)8 * Lf.nel));
 		TRYC(dalloc(h, &h->DTdot, Lf.nno));
@@ -1480,6 +1566,8 @@ int citcom_gpu_load_state(citcom_gpu *h, const double *T, const double *Tdot, co
 		TRY(h2d(h, h->U, U, sizeof(double) * Lf.neq));
 	if(P)
 		TRY(h2d(h, h->P, P, sizeof(double) * Lf.nel));
+	h->state_gen++;
+	h->T_sol_valid = false;
 	return sync(h);
 }
 
@@ -1585,7 +1673,7 @@ int citcom_gpu_output_wait(citcom_gpu *h)
 	return CITCOM_GPU_OK;
 }
 
-int citcom_gpu_stokes_residuals(citcom_gpu *h, double out[2])
+static int stokes_residuals_impl(citcom_gpu *h, double out[2])
 {
 	TRY(check_handle(h));
 	if(!out)
@@ -1608,6 +1696,19 @@ int citcom_gpu_stokes_residuals(citcom_gpu *h, double out[2])
 	return CITCOM_GPU_OK;
 }
 
+int citcom_gpu_stokes_residuals(citcom_gpu *h, double out[2])
+{
+	TRY(check_handle(h));
+	TRY(device_errors_reset(h));
+	TRY(stokes_residuals_impl(h, out));
+	return device_errors_check(h, "stokes_residuals");
+}
+
+int citcom_gpu_test_hold_tile_copy(void)
+{
+	return tile_hold_next_copy() == 0 ? CITCOM_GPU_OK : CITCOM_GPU_ERR_CUDA;
+}
+
 int citcom_gpu_last_stats(const citcom_gpu *h, citcom_gpu_stats *s)
 {
 	if(!h || !s)
@@ -1619,7 +1720,7 @@ int citcom_gpu_last_stats(const citcom_gpu *h, citcom_gpu_stats *s)
 
 // ------------------------------------------------------------ single operators
 
-int citcom_gpu_op_kmul(citcom_gpu *h, int lev, const double *u, double *Au)
+static int op_kmul_impl(citcom_gpu *h, int lev, const double *u, double *Au)
 {
 	TRY(check_handle(h));
 	TRY(check_level(h, lev));
@@ -1649,7 +1750,15 @@ int citcom_gpu_op_kmul(citcom_gpu *h, int lev, const double *u, double *Au)
 	return CITCOM_GPU_OK;
 }
 
-int citcom_gpu_op_gauss_seidel(citcom_gpu *h, int lev, double *d0, const double *F, double *Ad, int cycles, int guess)
+int citcom_gpu_op_kmul(citcom_gpu *h, int lev, const double *u, double *Au)
+{
+	TRY(check_handle(h));
+	TRY(device_errors_reset(h));
+	TRY(op_kmul_impl(h, lev, u, Au));
+	return device_errors_check(h, "op_kmul");
+}
+
+static int op_gauss_seidel_impl(citcom_gpu *h, int lev, double *d0, const double *F, double *Ad, int cycles, int guess)
 {
 	TRY(check_handle(h));
 	TRY(check_level(h, lev));
@@ -1692,6 +1801,14 @@ int citcom_gpu_op_gauss_seidel(citcom_gpu *h, int lev, double *d0, const double 
 	TRY(d2h(h, d0, B.vel[lev], sizeof(double) * L.neq));
 	TRY(d2h(h, Ad, B.AU[lev], sizeof(double) * L.neq));
 	return sync(h);
+}
+
+int citcom_gpu_op_gauss_seidel(citcom_gpu *h, int lev, double *d0, const double *F, double *Ad, int cycles, int guess)
+{
+	TRY(check_handle(h));
+	TRY(device_errors_reset(h));
+	TRY(op_gauss_seidel_impl(h, lev, d0, F, Ad, cycles, guess));
+	return device_errors_check(h, "op_gauss_seidel");
 }
 
 int citcom_gpu_op_project(citcom_gpu *h, int fine_lev, const double *AU, double *AD)
@@ -1764,7 +1881,7 @@ int citcom_gpu_op_grad(citcom_gpu *h, int lev, const double *P, double *gradP)
 	return sync(h);
 }
 
-int citcom_gpu_op_multi_grid(citcom_gpu *h, double *d1, double *F, double *residual)
+static int op_multi_grid_impl(citcom_gpu *h, double *d1, double *F, double *residual)
 {
 	TRY(check_handle(h));
 	if(!h->stiffness_ready)
@@ -1810,7 +1927,15 @@ int citcom_gpu_op_multi_grid(citcom_gpu *h, double *d1, double *F, double *resid
 	return sync(h);
 }
 
-int citcom_gpu_op_solve_del2_u(citcom_gpu *h, double *d0, const double *F, double acc, int *valid)
+int citcom_gpu_op_multi_grid(citcom_gpu *h, double *d1, double *F, double *residual)
+{
+	TRY(check_handle(h));
+	TRY(device_errors_reset(h));
+	TRY(op_multi_grid_impl(h, d1, F, residual));
+	return device_errors_check(h, "op_multi_grid");
+}
+
+static int op_solve_del2_u_impl(citcom_gpu *h, double *d0, const double *F, double acc, int *valid)
 {
 	TRY(check_handle(h));
 	if(!h->stiffness_ready)
@@ -1825,6 +1950,14 @@ int citcom_gpu_op_solve_del2_u(citcom_gpu *h, double *d0, const double *F, doubl
 	if(valid)
 		*valid = v;
 	return sync(h);
+}
+
+int citcom_gpu_op_solve_del2_u(citcom_gpu *h, double *d0, const double *F, double acc, int *valid)
+{
+	TRY(check_handle(h));
+	TRY(device_errors_reset(h));
+	TRY(op_solve_del2_u_impl(h, d0, F, acc, valid));
+	return device_errors_check(h, "op_solve_del2_u");
 }
 
 int citcom_gpu_op_diagonals(citcom_gpu *h, int lev, double *BI, double *BPI)
@@ -1894,6 +2027,57 @@ int nn_guess(citcom_nn *n)
 		double *dst = (l + 1 == lmax) ? n->Ug : n->Uv[l + 1];
 		launch_interp<double>(h->st, h->lv[l], h->lv[l + 1], h->geo[l + 1], n->Uv[l], dst);
 		launch_strip(h->st, h->lv[l + 1], dst);
+	}
+	CK(cudaGetLastError());
+	return CITCOM_GPU_OK;
+}
+
+// Increment mode: the network maps the temperature change since the last
+// solve (T - T_sol) and the viscosity to the change of U and P.  The start is
+// V, P + alpha (dU, dP), alpha minimising |F - K V - G P| along (dU, dP)
+// (clipped to [0, 2]; 0 keeps the previous solution).  ff = F.F.
+int nn_increment_start(citcom_nn *n, double *V, double *P, const double *F, double ff)
+{
+	citcom_gpu *h = n->h;
+	const int lmax = h->L - 1;
+	const Lvl &Lf = h->lv[lmax], &Lc = h->lv[n->lev];
+	const Geo *geo = h->geo[lmax];
+	cudaStream_t st = h->st;
+	launch_lin2(st, Lf.nno, n->dT, 1.0, h->T, -1.0, h->T_sol);
+	launch_nn_inputs(st, Lf, Lc, n->r, n->dT, h->evi[n->lev], n->x, n->work);
+	if(nn_forward(n->net, n->x, n->y) != 0)
+		return fail(h, CITCOM_GPU_ERR_CUDA, "warm-start network: forward launch failed");
+	launch_nn_guess(st, Lf, Lc, n->r, n->y, n->su, n->sp, 0.0, n->work, n->Uv[n->lev], n->Pg);
+	for(int l = n->lev; l < lmax; ++l)
+	{
+		double *dst = (l + 1 == lmax) ? n->Ug : n->Uv[l + 1];
+		launch_interp<double>(st, h->lv[l], h->lv[l + 1], h->geo[l + 1], n->Uv[l], dst);
+		launch_strip(st, h->lv[l + 1], dst);
+	}
+	// r = F - K V - G P (r64), w = K dU + G dP (Ah)
+	launch_grad(st, Lf, geo, P, h->Ah);
+	launch_kmul<double>(st, Lf, h->K64[lmax], V, h->u1);
+	launch_sub3(st, Lf.neq, h->r64, F, h->Ah, h->u1);
+	launch_grad(st, Lf, geo, n->Pg, h->Ah);
+	launch_kmul<double>(st, Lf, h->K64[lmax], n->Ug, h->u1);
+	launch_axpby(st, Lf.neq, h->Ah, 1.0, h->u1, 1.0);
+	launch_dots4(st, Lf.neq, h->r64, h->Ah, h->Ah, h->Ah, h->r64, h->r64, nullptr, nullptr, red_of(h), h->dscal + S_DOT);
+	TRY(readback(h, S_DOT, 3));
+	const double rw = h->hscal[S_DOT], ww = h->hscal[S_DOT + 1], rr = h->hscal[S_DOT + 2];
+	double alpha = (ww > 0.0 && rw > 0.0) ? rw / ww : 0.0;
+	if(!(alpha == alpha))
+		alpha = 0.0;
+	alpha = std::min(alpha, 2.0);
+	const double rr1 = std::max(rr - 2.0 * alpha * rw + alpha * alpha * ww, 0.0);
+	const double fn = ff > 0.0 ? ff : 1.0;
+	h->stats.base_residual = std::sqrt(rr / fn);
+	h->stats.warm_residual = std::sqrt(rr1 / fn);
+	h->stats.warm_start = alpha > 0.0 ? 1 : 0;
+	n->alpha = alpha;
+	if(alpha > 0.0)
+	{
+		launch_axpby(st, Lf.neq, V, 1.0, n->Ug, alpha);
+		launch_axpby(st, Lf.nel, P, 1.0, n->Pg, alpha);
 	}
 	CK(cudaGetLastError());
 	return CITCOM_GPU_OK;
@@ -1987,6 +2171,10 @@ int citcom_nn_create(citcom_gpu *h, int level, unsigned seed, int capacity, citc
 	r = r ? r : nn_alloc(n, &n->Ug, (size_t)h->lv[lmax].neq + 2);
 	r = r ? r : nn_alloc(n, &n->Pg, (size_t)h->lv[lmax].nel);
 	r = r ? r : nn_alloc(n, &n->work, (size_t)Lc.nno + Lc.noz + 2);
+	r = r ? r : nn_alloc(n, &n->Tp, (size_t)h->lv[lmax].nno);
+	r = r ? r : nn_alloc(n, &n->dT, (size_t)h->lv[lmax].nno);
+	r = r ? r : nn_alloc(n, &n->Up, (size_t)h->lv[lmax].neq + 2);
+	r = r ? r : nn_alloc(n, &n->Pp, (size_t)h->lv[lmax].nel);
 	if(r != CITCOM_GPU_OK)
 	{
 		fail(h, r, "%s", n->err);
@@ -2077,14 +2265,38 @@ int citcom_nn_record(citcom_nn *n)
 		return nn_fail(n, CITCOM_GPU_ERR_STATE, "no viscosity: record after a Stokes solve");
 	__nv_bfloat16 *xs = n->xs + (size_t)n->next * n->V * NN_CH;
 	float *ts = n->ts + (size_t)n->next * n->V * NN_OUT;
-	launch_nn_inputs(h->st, Lf, Lc, n->r, h->T, h->evi[n->lev], xs, n->work);
+	const double *Ts = h->T, *Us = h->U, *Ps = h->P;
+	if(n->mode == CITCOM_NN_INCREMENT)
+	{
+		// a sample is the change since the previous record of the same state
+		// sequence (no load_state in between); the first record of a sequence
+		// only remembers its state
+		const bool sample = n->have_prev && n->prev_gen == h->state_gen;
+		if(sample)
+		{
+			launch_lin2(h->st, Lf.nno, n->dT, 1.0, h->T, -1.0, n->Tp);
+			launch_lin2(h->st, Lf.neq, n->Ug, 1.0, h->U, -1.0, n->Up);
+			launch_lin2(h->st, Lf.nel, n->Pg, 1.0, h->P, -1.0, n->Pp);
+			Ts = n->dT;
+			Us = n->Ug;
+			Ps = n->Pg;
+		}
+		CK(cudaMemcpyAsync(n->Tp, h->T, sizeof(double) * Lf.nno, cudaMemcpyDeviceToDevice, h->st));
+		CK(cudaMemcpyAsync(n->Up, h->U, sizeof(double) * Lf.neq, cudaMemcpyDeviceToDevice, h->st));
+		CK(cudaMemcpyAsync(n->Pp, h->P, sizeof(double) * Lf.nel, cudaMemcpyDeviceToDevice, h->st));
+		n->have_prev = true;
+		n->prev_gen = h->state_gen;
+		if(!sample)
+			return CITCOM_GPU_OK;
+	}
+	launch_nn_inputs(h->st, Lf, Lc, n->r, Ts, h->evi[n->lev], xs, n->work);
 	if(!n->scaled)
 	{
-		// output scales from the first recorded solution: RMS velocity dof and
+		// output scales from the first recorded sample: RMS velocity dof and
 		// RMS pressure deviation, per unit anomaly RMS
 		std::vector<double> U(Lf.neq), P(Lf.nel);
 		double ss = 0.0;
-		if(d2h(h, U.data(), h->U, sizeof(double) * Lf.neq) || d2h(h, P.data(), h->P, sizeof(double) * Lf.nel) ||
+		if(d2h(h, U.data(), Us, sizeof(double) * Lf.neq) || d2h(h, P.data(), Ps, sizeof(double) * Lf.nel) ||
 		   d2h(h, &ss, n->work + Lc.nno + Lc.noz, sizeof(double)) || sync(h))
 			return nn_fail(n, CITCOM_GPU_ERR_CUDA, "state download failed");
 		const double a = std::sqrt(ss / Lc.nno);
@@ -2103,7 +2315,7 @@ int citcom_nn_record(citcom_nn *n)
 		n->mp = 0.0;
 		n->scaled = true;
 	}
-	launch_nn_targets(h->st, Lf, Lc, n->r, h->U, h->P, n->su, n->sp, n->work, ts);
+	launch_nn_targets(h->st, Lf, Lc, n->r, Us, Ps, n->su, n->sp, n->work, ts);
 	n->next = (n->next + 1) % n->capacity;
 	if(n->count < n->capacity)
 		n->count++;
@@ -2140,6 +2352,17 @@ int citcom_nn_train(citcom_nn *n, int steps, int batch, double lr, double *loss)
 	return CITCOM_GPU_OK;
 }
 
+int citcom_nn_set_mode(citcom_nn *n, int mode)
+{
+	NTRY(nn_check(n));
+	if(mode != CITCOM_NN_ABSOLUTE && mode != CITCOM_NN_INCREMENT)
+		return nn_fail(n, CITCOM_GPU_ERR_ARG, "unknown warm-start mode %d", mode);
+	if(n->count > 0 || n->have_prev || n->scaled)
+		return nn_fail(n, CITCOM_GPU_ERR_STATE, "the mode must be set before the first record");
+	n->mode = mode;
+	return CITCOM_GPU_OK;
+}
+
 int citcom_nn_attach(citcom_nn *n, int on)
 {
 	NTRY(nn_check(n));
@@ -2156,6 +2379,8 @@ int citcom_nn_predict(citcom_nn *n, double *U, double *P)
 		return nn_fail(n, CITCOM_GPU_ERR_STATE, "no output scales: record a solution or set the scales first");
 	if(!h->visc_ready)
 		return nn_fail(n, CITCOM_GPU_ERR_STATE, "no viscosity: call get_system_viscosity or solve first");
+	if(n->mode != CITCOM_NN_ABSOLUTE)
+		return nn_fail(n, CITCOM_GPU_ERR_STATE, "predict needs the absolute mode (an increment has no state of its own)");
 	const Lvl &Lf = h->lv[h->L - 1];
 	if(nn_guess(n) != CITCOM_GPU_OK)
 		return nn_fail(n, CITCOM_GPU_ERR_CUDA, "%s", h->err);

@@ -147,8 +147,17 @@ void launch_coarse_dense_build(cudaStream_t st, const Lvl &L, const float4 *Kt, 
 
 // Stencil kernels of the tiled (large) levels, tile.cu: persistent CTAs
 // streaming tiles through shared memory with bulk copies
+// matrix-free FP32 Gauss-Seidel colour of a box level (mf.cu): eta = the
+// level's Gauss-point viscosity in FP32 (8 per element), BI = 1/diag K in
+// colour-position order
+void launch_mf_eta32(cudaStream_t st, const Lvl &L, const double *evi, float *eta);
+void launch_mf_gs(cudaStream_t st, const Lvl &L, const float *eta, int aug, double lambda, const float *BI, const float *F,
+                  float *d, int colour);
+
 int tile_init();                                   // attributes and grid sizes; 0 on success
-int tile_error_async(double *host, cudaStream_t st);  // 1 in *host if a stage wait ever timed out
+int tile_error_async(double *host, cudaStream_t st);  // 1 in *host if a stage wait timed out since the last reset
+int tile_error_reset_async(cudaStream_t st);         // the tile kernels' error word to zero
+int tile_hold_next_copy();                           // failure-path test hook (tile.cu: g_tile_hold)
 template <typename T> void launch_tile_gs(cudaStream_t st, const Lvl &L, const T *K, const T *BI, const T *F, T *d, int colour);
 template <typename T> void launch_tile_kmul(cudaStream_t st, const Lvl &L, const T *K, const T *u, T *out);
 template <typename T> void launch_tile_residual(cudaStream_t st, const Lvl &L, const T *K, const T *f, const T *u, T *out);

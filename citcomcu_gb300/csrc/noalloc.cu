@@ -19,6 +19,7 @@
 
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 
 #include "../../include/citcom_gb300.h"
 #include "kernels.h"
@@ -45,8 +46,9 @@ namespace {
 
 // device address of g_noalloc_scratch on each device, looked up once per
 // device with that device current (the host-side symbol is not an address
-// the GPU can use)
+// the GPU can use); the lock orders first calls made on several host threads
 void *g_scratch_addr[MAX_DEVICES];
+std::mutex g_scratch_lock;
 
 int scratch_for_current_device(double **out)
 {
@@ -57,6 +59,7 @@ int scratch_for_current_device(double **out)
 		fprintf(stderr, "citcom_gpu_heat_flux_noalloc: no usable current device (%s)\n", cudaGetErrorString(e));
 		return CITCOM_GPU_ERR_CUDA;
 	}
+	std::lock_guard<std::mutex> lock(g_scratch_lock);
 	if(!g_scratch_addr[dev])
 	{
 		void *p = nullptr;

@@ -74,6 +74,23 @@ __device__ __forceinline__ bool t_wait(unsigned bar, unsigned parity)
 }
 
 __device__ double g_tile_err;  // 1 when a stage wait timed out
+// Failure-path test hook: while nonzero, the next CTA to start takes it (an
+// atomic exchange to zero) and arms its first stage without issuing the copy,
+// so that the bounded wait on that stage runs out with no copy in flight.
+__device__ int g_tile_hold;
+
+// bounded wait for the copies a CTA still has in flight after a stage wait
+// timed out.  These copies read stencil words that exist in global memory, so
+// they complete within microseconds; the limit (about 16 s) only keeps the
+// wait finite, and the CTA does not leave before it while a copy may still
+// write into its shared memory.
+__device__ __forceinline__ bool t_drain(unsigned bar, unsigned parity)
+{
+	for(int it = 0; it < 16; ++it)
+		if(t_wait(bar, parity))
+			return true;
+	return false;
+}
 
 template <typename T, int KIND>
 __global__ void __launch_bounds__(TT, TileCfg<T>::MIN_CTAS) k_tile(Lvl L, const T *__restrict__ K, const T *__restrict__ BI,
@@ -101,10 +118,20 @@ __global__ void __launch_bounds__(TT, TileCfg<T>::MIN_CTAS) k_tile(Lvl L, const 
 		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 	}
 	__syncthreads();
-	int issued = 0;
+	int issued = 0, held = -1;
 	if(threadIdx.x == 0)
+	{
+		if(nmine > 0 && g_tile_hold != 0 && atomicExch(&g_tile_hold, 0) != 0)
+		{
+			// test hook: stage 0 expects its bytes, but no copy is issued
+			asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar0), "r"(TileCfg<T>::BYTES)
+			             : "memory");
+			held = 0;
+			issued = 1;
+		}
 		for(; issued < S && issued < nmine; ++issued)
 			issue(issued);
+	}
 	// The stencil is written only by the assembly, long before any launch
 	// here, so its first copies start before the wait on the preceding kernel
 	// (under programmatic dependent launch they overlap that kernel's tail);
@@ -229,10 +256,13 @@ __global__ void __launch_bounds__(TT, TileCfg<T>::MIN_CTAS) k_tile(Lvl L, const 
 	if(!ok)
 	{
 		g_tile_err = 1.0;
-		// thread 0 issued every copy: the ones still in flight land before the CTA leaves
+		// No copy was issued after the first wait that ran out.  Thread 0
+		// issued every earlier one: those still in flight land before the CTA
+		// leaves (a held stage has none).
 		if(threadIdx.x == 0)
 			for(int k = max(0, issued - S); k < issued; ++k)
-				t_wait(bar0 + 8 * (k % S), (unsigned)((k / S) & 1));
+				if(k != held)
+					t_drain(bar0 + 8 * (k % S), (unsigned)((k / S) & 1));
 	}
 }
 
@@ -297,6 +327,18 @@ int tile_init()
 int tile_error_async(double *host, cudaStream_t st)
 {
 	return cudaMemcpyFromSymbolAsync(host, g_tile_err, sizeof(double), 0, cudaMemcpyDeviceToHost, st) == cudaSuccess ? 0 : -1;
+}
+
+int tile_error_reset_async(cudaStream_t st)
+{
+	static const double zero = 0.0;
+	return cudaMemcpyToSymbolAsync(g_tile_err, &zero, sizeof(double), 0, cudaMemcpyHostToDevice, st) == cudaSuccess ? 0 : -1;
+}
+
+int tile_hold_next_copy()
+{
+	const int one = 1;
+	return cudaMemcpyToSymbol(g_tile_hold, &one, sizeof(int)) == cudaSuccess ? 0 : -1;
 }
 
 template <typename T> void launch_tile_gs(cudaStream_t st, const Lvl &L, const T *K, const T *BI, const T *F, T *d, int colour)

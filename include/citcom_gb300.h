@@ -126,7 +126,8 @@ typedef struct citcom_gpu_stats
 	int visc_iterations;        /* viscosity iterations of general_stokes_solver (1 unless SDEPV) */
 	double visc_misfit;         /* |dU| / |U| of the last stress-dependent iteration */
 	int warm_start;             /* 1: the attached network's guess started the Uzawa solve */
-	double warm_residual;       /* |F - K U - G P| / |F| of the network's guess */
+	double warm_residual;       /* the network's guess: absolute mode, the Uzawa initial residual
+	                               |B V| / sqrt(npno) after the head; increment mode, |F - K U - G P| / |F| */
 	double base_residual;       /* the same of the resident U, P it was compared with */
 	double pass_ms;             /* device time of the multigrid passes (multi_grid calls) */
 	/* residual rule only (CITCOM_GPU_STOP_RESIDUAL): the FP64 residuals at the
@@ -233,6 +234,16 @@ int citcom_gpu_output_wait(citcom_gpu *h);
  * dv/v and dp/p (Stokes_flow_Incomp.c:393, 442-443). */
 int citcom_gpu_stokes_residuals(citcom_gpu *h, double out[2]);
 
+/* Failure-path test hook (no counterpart in the reference).  The stencil
+ * kernels of the large levels wait, with a limit of about a second, for the
+ * bulk copies of their stencil tiles; when a wait runs out the kernel sets an
+ * error word, issues no further copy, waits for the copies it has in flight
+ * and returns, and the calling entry point returns CITCOM_GPU_ERR_CUDA with
+ * the reason (the word is then cleared; the context stays usable).  After this
+ * call the next such kernel to start arms one stage without issuing its copy,
+ * so that exactly one wait runs out.  For tests of that path only. */
+int citcom_gpu_test_hold_tile_copy(void);
+
 /* Single operators of level lev, host buffers (the kernels the solver uses;
  * exposed for parity checks against the reference's routines). */
 /* n_assemble_del2_u (Element_calculations.c:552), stripped */
@@ -262,11 +273,15 @@ int citcom_gpu_op_diagonals(citcom_gpu *h, int lev, double *BI, double *BPI);
  * array inside the library (about 4.4 MB, held by every GPU that loads the
  * library until the process exits); it calls no cudaMalloc/cudaFree and needs
  * no handle.  dT (nno) and dV (3*nno, layout of V above) are DEVICE pointers
- * of a nox*noy*noz box of size dimen; nut/nub receive the results on the
- * host.  Meshes above CITCOM_GPU_NOALLOC_MAX_NODES nodes or
- * CITCOM_GPU_NOALLOC_MAX_ELEMENTS elements are rejected with
- * CITCOM_GPU_ERR_ARG and a message on stderr.  Runs on the legacy default
- * stream and returns after the result is on the host.  The first call on a
+ * of a nox*noy*noz Cartesian box of size dimen (box geometry only: it takes
+ * no spherical segment, whose Nusselt numbers come from citcom_gpu_heat_flux);
+ * nut/nub receive the results on the host.  Meshes above
+ * CITCOM_GPU_NOALLOC_MAX_NODES nodes or CITCOM_GPU_NOALLOC_MAX_ELEMENTS
+ * elements are rejected with CITCOM_GPU_ERR_ARG and a message on stderr.
+ * Runs on the legacy default stream and returns after the result is on the
+ * host.  That stream does not wait for work on non-blocking streams, so dT
+ * and dV must be complete before the call: synchronise the stream that
+ * writes them first.  The first call on a
  * device looks up the array's device address (once per device, with that
  * device current), so make the first call before any stream capture.  All
  * calls share the one array: calls that overlap on the GPU race and must be
@@ -308,9 +323,26 @@ int citcom_nn_set_scales(citcom_nn *n, const double s[3]);
 int citcom_nn_record(citcom_nn *n);
 /* `steps` Adam steps on random minibatches of `batch` snapshots; loss of the last step */
 int citcom_nn_train(citcom_nn *n, int steps, int batch, double lr, double *loss);
+/* What the network predicts (set before the first record).
+ * CITCOM_NN_ABSOLUTE: U and P from T and the viscosity, as above.
+ * CITCOM_NN_INCREMENT: the change of U and P since the handle's last Stokes
+ * solve, from the change of T since that solve (T - T_sol, restricted to the
+ * network grid, minus its horizontal mean, over its RMS) and the viscosity.
+ * Training samples are the differences between consecutive records of one
+ * state sequence (a load_state starts a new sequence; its first record
+ * only remembers the state).  An attached network then starts each Uzawa
+ * solve that follows a completed solve of the same sequence from
+ * (U, P) + alpha (dU, dP), alpha in [0, 2] minimising |F - K U - G P| along
+ * the increment (alpha = 0 keeps the previous step's solution), followed by
+ * the reference's single head; warm_residual / base_residual of the stats are
+ * the momentum residuals |F - K U - G P| / |F| with and without it. */
+#define CITCOM_NN_ABSOLUTE 0
+#define CITCOM_NN_INCREMENT 1
+int citcom_nn_set_mode(citcom_nn *n, int mode);
 /* on != 0: warm-start every Stokes solve of the handle */
 int citcom_nn_attach(citcom_nn *n, int on);
-/* the guess for the resident T and viscosity: U (neq), P (nel) on the host */
+/* the guess for the resident T and viscosity: U (neq), P (nel) on the host
+ * (absolute mode only) */
 int citcom_nn_predict(citcom_nn *n, double *U, double *P);
 /* checks of the network alone, host buffers in the network's scaled units:
  * x (V x 2: temperature anomaly / its RMS, (log10 eta + 1.5) / 1.5), y and t
