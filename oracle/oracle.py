@@ -71,8 +71,10 @@ def build(quiet: bool = True) -> str:
     return LIB_PATH
 
 
-# the unchanged reference's sources, where they exist (the build container)
-REF_SRC = "/root/reference/src"
+# the unchanged reference's sources, where they exist: $CITCOM_REF_SRC, else
+# the reference tree beside the repository (../reference/src); absent on hosts
+# that only run the GPU library
+REF_SRC = os.environ.get("CITCOM_REF_SRC") or os.path.normpath(os.path.join(HERE, "..", "..", "reference", "src"))
 
 
 def build_reference(quiet: bool = True) -> bool:
@@ -80,7 +82,7 @@ def build_reference(quiet: bool = True) -> bool:
     present (this container); returns False where they are absent."""
     if not os.path.isdir(REF_SRC):
         return False
-    subprocess.run(["make", "-s", "-j8", "-C", os.path.join(HERE, "ref")], check=True,
+    subprocess.run(["make", "-s", "-j8", "-C", os.path.join(HERE, "ref"), f"REF={REF_SRC}"], check=True,
                    stdout=subprocess.DEVNULL if quiet else None,
                    stderr=subprocess.DEVNULL if quiet else None)
     return True

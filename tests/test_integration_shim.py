@@ -1,9 +1,10 @@
-"""The reference-side shim that INTEGRATION.md shows (the replacement of
-Stokes_flow_Incomp.c's solvers and the GPU PG_timestep hook, plus the
-output-step function) compiles as C against the reference's own headers and
-include/citcom_gb300.h.  Skipped where the reference sources are absent."""
+"""The reference-side shim (citcomcu_gb300/shim/Gpu_stokes.c: the
+replacement of Stokes_flow_Incomp.c's solvers, construct_stiffness_B_matrix
+and the GPU PG_timestep hook, plus the output-step function and, optionally,
+the learned warm start) compiles as C against the reference's own headers and
+include/citcom_gb300.h, and links into a CitcomCU executable.  Skipped where
+the reference sources are absent."""
 import os
-import re
 import subprocess
 
 import pytest
@@ -11,20 +12,17 @@ import pytest
 from oracle.oracle import REF_SRC
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+SHIM = os.path.join(ROOT, "citcomcu_gb300", "shim", "Gpu_stokes.c")
 
 
 def test_integration_shim_compiles_against_the_reference_headers(tmp_path):
     if not os.path.isdir(REF_SRC):
         pytest.skip("reference sources not present")
-    blocks = re.findall(r"```c\n(.*?)```", open(os.path.join(ROOT, "INTEGRATION.md")).read(), re.S)
-    shim = [b for b in blocks if "solve_constrained_flow_iterative(struct All_variables *E)" in b]
-    out_step = [b for b in blocks if "gpu_output_step" in b]
-    assert len(shim) == 1 and len(out_step) == 1
-    src = tmp_path / "Gpu_stokes.c"
-    src.write_text(shim[0] + "\n" + out_step[0])
-    r = subprocess.run(["gcc", "-std=gnu99", "-c", "-Wall", "-Werror=implicit-function-declaration", "-I", REF_SRC, "-I", os.path.join(ROOT, "include"), str(src), "-o",
-                        str(tmp_path / "Gpu_stokes.o")], capture_output=True, text=True)
-    assert r.returncode == 0, r.stderr
+    for extra in ([], ["-DCITCOM_GPU_WARM_START"]):
+        r = subprocess.run(["gcc", "-std=gnu99", "-c", "-Wall", "-Werror=implicit-function-declaration"] + extra +
+                           ["-I", REF_SRC, "-I", os.path.join(ROOT, "include"), SHIM, "-o",
+                            str(tmp_path / "Gpu_stokes.o")], capture_output=True, text=True)
+        assert r.returncode == 0, (extra, r.stderr)
 
 
 def test_dropin_citcom_executable(tmp_path):
@@ -53,12 +51,8 @@ def test_dropin_citcom_executable(tmp_path):
     objs = os.path.join(ROOT, "oracle", "_ref", "f32")
     cflags = ["-O2", "-std=gnu99", "-w", "-D_GNU_SOURCE", "-I", ref_dir, "-I", REF_SRC,
               '-DCOMPRESS_BINARY="/usr/bin/compress"']
-    blocks = re.findall(r"```c\n(.*?)```", open(os.path.join(ROOT, "INTEGRATION.md")).read(), re.S)
-    shim = [b for b in blocks if "solve_constrained_flow_iterative(struct All_variables *E)" in b][0]
-    out_step = [b for b in blocks if "gpu_output_step" in b][0]
-    (tmp_path / "Gpu_stokes.c").write_text(shim + "\n" + out_step)
     units = {
-        "Gpu_stokes.o": (str(tmp_path / "Gpu_stokes.c"), ["-I", os.path.join(ROOT, "include")]),
+        "Gpu_stokes.o": (SHIM, ["-I", os.path.join(ROOT, "include"), "-DCITCOM_GPU_WARM_START"]),
         "Stokes_flow_Incomp.o": (os.path.join(REF_SRC, "Stokes_flow_Incomp.c"),
                                  ["-Dsolve_constrained_flow_iterative=ref_solve_constrained_flow_iterative",
                                   "-Dsolve_Ahat_p_fhat=ref_solve_Ahat_p_fhat"]),
