@@ -559,6 +559,9 @@ def main():
                     help="increment: the network predicts the change of U, P over a time step (default); "
                          "absolute: U, P themselves")
     ap.add_argument("--learn-adam", type=int, default=1000, help="Adam steps of the online training")
+    ap.add_argument("--learn-check", type=int, default=8,
+                    help="compare the network's start with the previous step's on every k-th solve (and whenever "
+                         "its initial residual grows past 4x the last winning one); 1: every solve")
     ap.add_argument("--cold-reps", type=int, default=2, help="cold solves per mode (0: skip)")
     ap.add_argument("--drift-steps", type=int, default=50, help="time steps of the 64^3 drift run (0: skip)")
     ap.add_argument("--ref-full-steps", type=int, default=2,
@@ -599,6 +602,7 @@ def main():
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
         if ls is not None:
+            ln.set_check_interval(args.learn_check)
             learned = run_loop(cg, case, T0, cg.MIXED, args.steps, args.warmup, solver=ls, net=ln)
         mixed = run_loop(cg, case, T0, cg.MIXED, args.steps, args.warmup)
         fp64 = run_loop(cg, case, T0, cg.FP64, args.steps, args.warmup) if args.modes == "all" else None
@@ -658,12 +662,24 @@ def main():
         line["speedup_vs_fp64"] = line["fp64_plain"]["stokes_ms_per_step"] / stokes_ms
     if learned:
         d = loop_summary(learned, ref)
-        d.update({"warm_start_used": [r["warm_start"] for r in learned["recs"]],
+        d.update({"check_interval": args.learn_check,
+                  "compared": [r["warm_compared"] for r in learned["recs"]],
+                  "warm_start_used": [r["warm_start"] for r in learned["recs"]],
                   "start_residual_previous_step": [r["base_residual"] for r in learned["recs"]],
                   "start_residual_network": [r["warm_residual"] for r in learned["recs"]],
                   "speedup_vs_mixed": line["mixed"]["stokes_ms_per_step"] / d["stokes_ms_per_step"],
                   "training": train_info})
         line["learned"] = d
+    if ls is not None and args.learn_check != 1:
+        # the same loop comparing the two starts on every solve (the fallback
+        # decided afresh each step, at the price of a second head per step)
+        ln.set_check_interval(1)
+        strict = run_loop(cg, case, T0, cg.MIXED, args.steps, args.warmup, solver=ls, net=ln)
+        ln.set_check_interval(args.learn_check)
+        d = loop_summary(strict, ref)
+        d["speedup_vs_mixed"] = line["mixed"]["stokes_ms_per_step"] / d["stokes_ms_per_step"]
+        d["warm_start_used"] = [r["warm_start"] for r in strict["recs"]]
+        line["learned_compare_every_step"] = d
     if args.cold_reps > 0:
         cs = {"mixed": cold_solves(cg, case, T0, cg.MIXED, args.cold_reps)}
         if ls is not None and args.learn_mode == "absolute":

@@ -164,7 +164,8 @@ class _CStats(ctypes.Structure):
                 ("visc_misfit", ctypes.c_double), ("warm_start", ctypes.c_int),
                 ("warm_residual", ctypes.c_double), ("base_residual", ctypes.c_double),
                 ("pass_ms", ctypes.c_double), ("final_momentum", ctypes.c_double),
-                ("final_continuity", ctypes.c_double), ("corrections", ctypes.c_int)]
+                ("final_continuity", ctypes.c_double), ("corrections", ctypes.c_int),
+                ("warm_compared", ctypes.c_int)]
 
 
 # every symbol of include/citcom_gb300.h with its argument types
@@ -232,6 +233,7 @@ _SIGNATURES = {
     "citcom_nn_train": (ctypes.c_int, [_H, ctypes.c_int, ctypes.c_int, ctypes.c_double, _D]),
     "citcom_nn_attach": (ctypes.c_int, [_H, ctypes.c_int]),
     "citcom_nn_set_mode": (ctypes.c_int, [_H, ctypes.c_int]),
+    "citcom_nn_set_check_interval": (ctypes.c_int, [_H, ctypes.c_int]),
     "citcom_nn_predict": (ctypes.c_int, [_H, _D, _D]),
     "citcom_nn_forward": (ctypes.c_int, [_H, _F, _F]),
     "citcom_nn_loss_grad": (ctypes.c_int, [_H, _F, _F, _D, _F]),
@@ -385,7 +387,7 @@ class Solver:
                     warm_start=s.warm_start, warm_residual=s.warm_residual, base_residual=s.base_residual,
                     visc_iterations=s.visc_iterations, visc_misfit=s.visc_misfit, pass_ms=s.pass_ms,
                     final_momentum=s.final_momentum, final_continuity=s.final_continuity,
-                    corrections=s.corrections)
+                    corrections=s.corrections, warm_compared=s.warm_compared)
 
     def stokes_residuals(self):
         """(|F - K U - G P| / |F|, |div U| / (|U| sqrt(npno/neq))) of the resident solution."""
@@ -686,6 +688,11 @@ class WarmStart:
         loss = ctypes.c_double()
         self._check(self.lib.citcom_nn_train(self.h, steps, batch, lr, ctypes.byref(loss)))
         return loss.value
+
+    def set_check_interval(self, every: int):
+        """Compare the network's start with the resident one on every
+        `every`-th solve (1: always; see citcom_nn_set_check_interval)."""
+        self._check(self.lib.citcom_nn_set_check_interval(self.h, int(every)))
 
     def attach(self, on: bool = True):
         self._check(self.lib.citcom_nn_attach(self.h, int(on)))

@@ -143,13 +143,20 @@ struct citcom_nn
 	double *work;           // FP64 scratch of the input/target/guess kernels
 	double su, sp, mp;      // output scales per unit anomaly RMS: velocity, pressure; pressure offset
 	bool scaled;
-	// increment mode (CITCOM_NN_INCREMENT): the state of the previous record,
-	// the fine temperature increment, and the last line-search step
+	// increment mode (CITCOM_NN_INCREMENT): the state of the previous record
+	// and the fine temperature increment
 	int mode;
 	double *Tp, *Up, *Pp, *dT;
+	// the comparison with the resident start: every check_every-th guessed
+	// solve; guesses so far, whether the network won the last comparison and
+	// its initial residual then
+	int check_every;
+	long guesses;
+	bool net_ok;
+	double r_ref;
 	bool have_prev;
 	unsigned prev_gen;
-	double alpha;
+
 	bool attached;
 	unsigned long long rng;
 	std::vector<void *> allocs;
@@ -651,7 +658,7 @@ int solve_del2_u(citcom_gpu *h, double acc, int *valid)
 // ---------------------------------------------------------------- Uzawa
 
 int nn_guess(citcom_nn *n);
-int nn_increment_start(citcom_nn *n, double *V, double *P, const double *F, double ff);
+int nn_increment_guess(citcom_nn *n, const double *V, const double *P);
 
 // The head of solve_Ahat_p_fhat (Stokes_flow_Incomp.c:360-371): the velocity
 // correction V += K^-1 (F - G P - K V) for the pressure P, then r1 = B V and
@@ -742,35 +749,54 @@ int uzawa(citcom_gpu *h, double *V, double *P, const double *F, double imp, int 
 	double residual = 0.0, vv = 0.0;
 	double *vvp = resid_rule ? &vv : nullptr;
 	citcom_nn *n = h->warm;
-	if(n && n->scaled && n->mode == CITCOM_NN_INCREMENT)
+	// increment mode: a guess exists once a solve of the same state sequence
+	// has completed (T_sol is its temperature)
+	const bool inc = n && n->scaled && n->mode == CITCOM_NN_INCREMENT;
+	h->stats.warm_compared = 0;
+	if(n && n->scaled && (!inc || h->T_sol_valid))
 	{
-		// the previous solution plus the network's increment for T - T_sol,
-		// scaled by the step that minimises the momentum residual (0 keeps the
-		// previous solution); then the one head of the reference
-		if(h->T_sol_valid)
-			TRY(nn_increment_start(n, V, P, F, ff));
-		TRY(uzawa_start(h, V, P, F, imp * v_res, h->r1, &residual, vvp));
-		if(nn_device_error(n->net) != 0)
-			return fail(h, CITCOM_GPU_ERR_CUDA, "warm-start network: a tensor-core wait timed out");
-	}
-	else if(n && n->scaled)
-	{
-		double r_net = 0.0, vv_net = 0.0;
-		TRY(nn_guess(n));
-		TRY(uzawa_start(h, n->Ug, n->Pg, F, imp * v_res, h->r1, &r_net, resid_rule ? &vv_net : nullptr));
-		TRY(uzawa_start(h, V, P, F, imp * v_res, h->r1, &residual, vvp));
-		if(nn_device_error(n->net) != 0)
-			return fail(h, CITCOM_GPU_ERR_CUDA, "warm-start network: a tensor-core wait timed out");
-		h->stats.warm_residual = r_net;
-		h->stats.base_residual = residual;
-		if(r_net < residual)
+		// The network's start is compared with the resident one (both heads
+		// run, the smaller initial residual wins) on every check_every-th
+		// guessed solve, and whenever the guess's initial residual has grown
+		// past 4x that of the last comparison the network won.  Between
+		// comparisons the last winner is used alone.
+		const bool scheduled = n->check_every <= 1 || n->guesses % n->check_every == 0;
+		n->guesses++;
+		if(!scheduled && !n->net_ok)
+			TRY(uzawa_start(h, V, P, F, imp * v_res, h->r1, &residual, vvp));
+		else
 		{
-			CK(cudaMemcpyAsync(V, n->Ug, sizeof(double) * neq, cudaMemcpyDeviceToDevice, st));
-			CK(cudaMemcpyAsync(P, n->Pg, sizeof(double) * npno, cudaMemcpyDeviceToDevice, st));
-			launch_div(st, Lf, geo, V, h->r1);
-			residual = r_net;
-			vv = vv_net;
-			h->stats.warm_start = 1;
+			double r_net = 0.0, vv_net = 0.0;
+			if(inc)
+				TRY(nn_increment_guess(n, V, P));
+			else
+				TRY(nn_guess(n));
+			TRY(uzawa_start(h, n->Ug, n->Pg, F, imp * v_res, h->r1, &r_net, resid_rule ? &vv_net : nullptr));
+			const bool compare = scheduled || !(r_net <= 4.0 * n->r_ref);
+			residual = HUGE_VAL;
+			if(compare)
+				TRY(uzawa_start(h, V, P, F, imp * v_res, h->r1, &residual, vvp));
+			if(nn_device_error(n->net) != 0)
+				return fail(h, CITCOM_GPU_ERR_CUDA, "warm-start network: a tensor-core wait timed out");
+			h->stats.warm_compared = compare ? 1 : 0;
+			h->stats.warm_residual = r_net;
+			h->stats.base_residual = compare ? residual : 0.0;
+			if(r_net < residual)
+			{
+				CK(cudaMemcpyAsync(V, n->Ug, sizeof(double) * neq, cudaMemcpyDeviceToDevice, st));
+				CK(cudaMemcpyAsync(P, n->Pg, sizeof(double) * npno, cudaMemcpyDeviceToDevice, st));
+				launch_div(st, Lf, geo, V, h->r1);
+				residual = r_net;
+				vv = vv_net;
+				h->stats.warm_start = 1;
+				if(compare)
+				{
+					n->net_ok = true;
+					n->r_ref = r_net;
+				}
+			}
+			else
+				n->net_ok = false;
 		}
 	}
 	else
@@ -2033,15 +2059,13 @@ int nn_guess(citcom_nn *n)
 }
 
 // Increment mode: the network maps the temperature change since the last
-// solve (T - T_sol) and the viscosity to the change of U and P.  The start is
-// V, P + alpha (dU, dP), alpha minimising |F - K V - G P| along (dU, dP)
-// (clipped to [0, 2]; 0 keeps the previous solution).  ff = F.F.
-int nn_increment_start(citcom_nn *n, double *V, double *P, const double *F, double ff)
+// solve (T - T_sol) and the viscosity to the change of U and P; the guess is
+// Ug = V + dU (stripped), Pg = P + dP.
+int nn_increment_guess(citcom_nn *n, const double *V, const double *P)
 {
 	citcom_gpu *h = n->h;
 	const int lmax = h->L - 1;
 	const Lvl &Lf = h->lv[lmax], &Lc = h->lv[n->lev];
-	const Geo *geo = h->geo[lmax];
 	cudaStream_t st = h->st;
 	launch_lin2(st, Lf.nno, n->dT, 1.0, h->T, -1.0, h->T_sol);
 	launch_nn_inputs(st, Lf, Lc, n->r, n->dT, h->evi[n->lev], n->x, n->work);
@@ -2054,31 +2078,8 @@ int nn_increment_start(citcom_nn *n, double *V, double *P, const double *F, doub
 		launch_interp<double>(st, h->lv[l], h->lv[l + 1], h->geo[l + 1], n->Uv[l], dst);
 		launch_strip(st, h->lv[l + 1], dst);
 	}
-	// r = F - K V - G P (r64), w = K dU + G dP (Ah)
-	launch_grad(st, Lf, geo, P, h->Ah);
-	launch_kmul<double>(st, Lf, h->K64[lmax], V, h->u1);
-	launch_sub3(st, Lf.neq, h->r64, F, h->Ah, h->u1);
-	launch_grad(st, Lf, geo, n->Pg, h->Ah);
-	launch_kmul<double>(st, Lf, h->K64[lmax], n->Ug, h->u1);
-	launch_axpby(st, Lf.neq, h->Ah, 1.0, h->u1, 1.0);
-	launch_dots4(st, Lf.neq, h->r64, h->Ah, h->Ah, h->Ah, h->r64, h->r64, nullptr, nullptr, red_of(h), h->dscal + S_DOT);
-	TRY(readback(h, S_DOT, 3));
-	const double rw = h->hscal[S_DOT], ww = h->hscal[S_DOT + 1], rr = h->hscal[S_DOT + 2];
-	double alpha = (ww > 0.0 && rw > 0.0) ? rw / ww : 0.0;
-	if(!(alpha == alpha))
-		alpha = 0.0;
-	alpha = std::min(alpha, 2.0);
-	const double rr1 = std::max(rr - 2.0 * alpha * rw + alpha * alpha * ww, 0.0);
-	const double fn = ff > 0.0 ? ff : 1.0;
-	h->stats.base_residual = std::sqrt(rr / fn);
-	h->stats.warm_residual = std::sqrt(rr1 / fn);
-	h->stats.warm_start = alpha > 0.0 ? 1 : 0;
-	n->alpha = alpha;
-	if(alpha > 0.0)
-	{
-		launch_axpby(st, Lf.neq, V, 1.0, n->Ug, alpha);
-		launch_axpby(st, Lf.nel, P, 1.0, n->Pg, alpha);
-	}
+	launch_axpby(st, Lf.neq, n->Ug, 1.0, V, 1.0);
+	launch_axpby(st, Lf.nel, n->Pg, 1.0, P, 1.0);
 	CK(cudaGetLastError());
 	return CITCOM_GPU_OK;
 }
@@ -2149,6 +2150,7 @@ int citcom_nn_create(citcom_gpu *h, int level, unsigned seed, int capacity, citc
 		return fail(h, CITCOM_GPU_ERR_ARG, "training-set capacity must be positive");
 	citcom_nn *n = new citcom_nn();
 	n->h = h;
+	n->check_every = 1;
 	n->lev = level;
 	n->r = 1 << (lmax - level);
 	n->capacity = capacity;
@@ -2360,6 +2362,18 @@ int citcom_nn_set_mode(citcom_nn *n, int mode)
 	if(n->count > 0 || n->have_prev || n->scaled)
 		return nn_fail(n, CITCOM_GPU_ERR_STATE, "the mode must be set before the first record");
 	n->mode = mode;
+	return CITCOM_GPU_OK;
+}
+
+int citcom_nn_set_check_interval(citcom_nn *n, int every)
+{
+	NTRY(nn_check(n));
+	if(every < 1)
+		return nn_fail(n, CITCOM_GPU_ERR_ARG, "the check interval must be at least 1");
+	n->check_every = every;
+	n->guesses = 0;
+	n->net_ok = false;
+	n->r_ref = 0.0;
 	return CITCOM_GPU_OK;
 }
 

@@ -126,8 +126,7 @@ typedef struct citcom_gpu_stats
 	int visc_iterations;        /* viscosity iterations of general_stokes_solver (1 unless SDEPV) */
 	double visc_misfit;         /* |dU| / |U| of the last stress-dependent iteration */
 	int warm_start;             /* 1: the attached network's guess started the Uzawa solve */
-	double warm_residual;       /* the network's guess: absolute mode, the Uzawa initial residual
-	                               |B V| / sqrt(npno) after the head; increment mode, |F - K U - G P| / |F| */
+	double warm_residual;       /* the Uzawa initial residual |B V| / sqrt(npno) after the head, from the network's guess */
 	double base_residual;       /* the same of the resident U, P it was compared with */
 	double pass_ms;             /* device time of the multigrid passes (multi_grid calls) */
 	/* residual rule only (CITCOM_GPU_STOP_RESIDUAL): the FP64 residuals at the
@@ -135,6 +134,7 @@ typedef struct citcom_gpu_stats
 	double final_momentum;      /* |F - K U - G P| / |F| */
 	double final_continuity;    /* |B U| / (|U| sqrt(npno/neq)) */
 	int corrections;
+	int warm_compared;          /* 1: both starts' heads ran (base_residual is then set) */
 } citcom_gpu_stats;
 
 /* Allocates every device buffer the solver will use (on the current
@@ -302,9 +302,10 @@ int citcom_gpu_heat_flux_noalloc(int nox, int noy, int noz, const double dimen[3
  * runs its head -- the velocity correction for the given pressure and the
  * initial residual |div V| / sqrt(npno) that solve_Ahat_p_fhat returns -- for
  * the network's guess as well as for the resident U, P (the previous solution,
- * or zero), and iterates from the pair with the smaller initial residual.  The
- * solve then runs to the same stopping rule, so the network changes only the
- * iteration count (at the price of one extra velocity solve).  The network
+ * or zero), and iterates from the pair with the smaller initial residual (see
+ * citcom_nn_set_check_interval for comparing less often).  The solve then runs
+ * to the same stopping rule, so the network changes only the iteration count
+ * (at the price of one extra velocity solve per comparison).  The network
  * must be destroyed before its solver handle, or at least not used after it. */
 typedef struct citcom_nn citcom_nn;
 int citcom_nn_create(citcom_gpu *h, int level, unsigned seed, int capacity, citcom_nn **out);
@@ -330,15 +331,21 @@ int citcom_nn_train(citcom_nn *n, int steps, int batch, double lr, double *loss)
  * network grid, minus its horizontal mean, over its RMS) and the viscosity.
  * Training samples are the differences between consecutive records of one
  * state sequence (a load_state starts a new sequence; its first record
- * only remembers the state).  An attached network then starts each Uzawa
- * solve that follows a completed solve of the same sequence from
- * (U, P) + alpha (dU, dP), alpha in [0, 2] minimising |F - K U - G P| along
- * the increment (alpha = 0 keeps the previous step's solution), followed by
- * the reference's single head; warm_residual / base_residual of the stats are
- * the momentum residuals |F - K U - G P| / |F| with and without it. */
+ * only remembers the state).  An attached network then offers (U + dU,
+ * P + dP) as the guess of each Uzawa solve that follows a completed solve of
+ * the same sequence, compared with the previous step's (U, P) as in the
+ * absolute mode. */
 #define CITCOM_NN_ABSOLUTE 0
 #define CITCOM_NN_INCREMENT 1
 int citcom_nn_set_mode(citcom_nn *n, int mode);
+/* How often the network's start is compared with the resident one (both
+ * heads run and the start with the smaller initial residual is kept).
+ * every = 1 (the default): every solve.  every = k > 1: every k-th solve the
+ * network could start, and also whenever its start's initial residual
+ * exceeds 4x that of the last comparison it won; between comparisons the
+ * last winner starts alone (no second head).  Resets the comparison
+ * history. */
+int citcom_nn_set_check_interval(citcom_nn *n, int every);
 /* on != 0: warm-start every Stokes solve of the handle */
 int citcom_nn_attach(citcom_nn *n, int on);
 /* the guess for the resident T and viscosity: U (neq), P (nel) on the host

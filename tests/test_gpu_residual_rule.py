@@ -7,7 +7,8 @@ Against the oracle in the GPU's 8-colour order the arithmetic is the same, so
 every solve must take the same Uzawa iterations, multigrid passes and velocity
 corrections, and agree to FP64 rounding.  The 32^3 case is the 64^3 benchmark
 box (eta = exp(-ln(1e3) T), Ra 1e5, seeded T0 = 1 - z + U(-0.01, 0.01)) on
-four levels instead of five: one cold solve and one time step.
+four levels instead of five: one cold solve and one time step; the 64^3 case
+is that box itself (one cold solve).
 """
 import math
 
@@ -27,7 +28,7 @@ def rel(a, b):
 
 
 def box_case(size):
-    levels = {16: 3, 32: 4}[size]
+    levels = {16: 3, 32: 4, 64: 5}[size]
     return Case(mgunit=(4, 4, 4), levels=levels, rayleigh=1e5, tdepv=True, visc0=(1.0,), viscE=(math.log(1e3),),
                 viscT=(0.0,), accuracy=1e-6, piterations=1000, stop_rule=1)
 
@@ -74,17 +75,22 @@ def steps_against_oracle(cg, olib, case, T0, nsteps, precision=0):
     return out
 
 
-@pytest.mark.parametrize("name", ["small", "box32"])
+@pytest.mark.parametrize("name", ["small", "box32", "box64"])
 def test_residual_rule_matches_coloured_oracle(cg, oracle_lib, name):
     if name == "small":
         case = small_case()
         case.accuracy, case.piterations, case.stop_rule = 1e-6, 1000, 1
         T0 = conductive_T0(case, amp=0.01, seed=0)
         nsteps = 3
-    else:
+    elif name == "box32":
         case = box_case(32)
         T0 = seeded_T0(case)
         nsteps = 1
+    else:
+        # the 64^3 benchmark box itself: its cold solve (about 100 s of oracle)
+        case = box_case(64)
+        T0 = seeded_T0(case)
+        nsteps = 0
     for r in steps_against_oracle(cg, oracle_lib, case, T0, nsteps):
         st, info = r["st"], r["info"]
         print(r["step"], st["uzawa"], info["uzawa"], st["mg_passes"], info["mg_calls"], st["corrections"],
@@ -120,9 +126,10 @@ def test_residual_rule_mixed_precision(cg):
 
 
 def test_residual_rule_stops_earlier_than_the_reference_rule(cg):
-    """The reference's rule (dv/v and dp/p below 1e-6) runs this cold solve to
-    its iteration cap; the residual rule stops once the solution meets the
-    tolerance, and the reference rule's longer solve meets it too."""
+    """The reference's rule (dv/v and dp/p below 1e-6) takes several times
+    the iterations on this cold solve (99 measured) and still leaves a
+    momentum residual above 1e-6 (5.8e-6: its inner solves' errors add up);
+    the residual rule stops once the solution meets both residuals."""
     case = box_case(16)
     T0 = seeded_T0(case)
     out = {}

@@ -142,3 +142,65 @@ def test_trained_warm_start_gain_on_held_out_states(cg):
     n.attach(False)
     n.close()
     s.close()
+
+
+def test_increment_warm_start_gain_in_the_time_loop(cg):
+    """Increment mode, the form the time loop needs: the network predicts the
+    change of U and P over a step from the change of T.  Trained online on the
+    solver's own consecutive converged solves of seeds 1..8, then run on a
+    held-out seed's time loop under the residual rule (both FP64 residuals at
+    most 1e-6): with the start compared against the previous step's solution
+    on every solve (the previous solution kept whenever the network's initial
+    residual is worse), the Uzawa solves of the same steps take fewer
+    iterations and multigrid passes than from the previous step alone, and
+    reach the same solution to the tolerance's effect (Nu within 1e-5)."""
+    cfg = cg.Config(mgunit=(4, 4, 4), levels=4, rayleigh=1e5, tdepv=True, viscE=(math.log(1e3),),
+                    accuracy=1e-6, piterations=1000, stop_rule=cg.STOP_RESIDUAL, precision=cg.MIXED)
+    s = cg.Solver(cfg)
+    base = cg.Solver(cfg)
+    f = s.fine
+    dims = (f["nox"], f["noy"], f["noz"])
+    n = cg.WarmStart(s, seed=3, capacity=128, mode=cg.WarmStart.INCREMENT)
+    zn, zu, zp = np.zeros(f["nno"]), np.zeros(f["neq"]), np.zeros(f["nel"])
+    for seed in range(1, 9):
+        s.load_state(T=seeded_T(dims, seed), Tdot=zn, U=zu, P=zp)
+        s.stokes_resident()
+        n.record()  # the first record of a sequence only remembers the state
+        for _ in range(12):
+            s.step_resident(0.0)
+            n.record()
+    assert n.recorded == 96
+    l0 = n.train(1, batch=4, lr=1e-3)
+    l1 = n.train(1000, batch=4, lr=1e-3)
+    assert l1 < 0.05 * l0, (l0, l1)
+
+    T0 = seeded_T(dims, 0)
+    runs = {}
+    for name, sv, net in (("previous step", base, None), ("network", s, n)):
+        sv.load_state(T=T0, Tdot=zn, U=zu, P=zp)
+        if net is not None:
+            net.attach(True)
+        sv.stokes_resident()
+        rows = []
+        for i in range(13):
+            sv.step_resident(0.0)
+            st = sv.stats()
+            if i >= 3:
+                rows.append((st["uzawa"], st["mg_passes"], st["warm_start"], st["base_residual"], st["warm_residual"],
+                             st["warm_compared"]))
+        runs[name] = (rows, sv.heat_flux()[0], sv.stokes_residuals())
+        if net is not None:
+            net.attach(False)
+    b, w = runs["previous step"], runs["network"]
+    print([r[:2] for r in b[0]], [r for r in w[0]])
+    it_b, it_w = sum(r[0] for r in b[0]), sum(r[0] for r in w[0])
+    print(f"uzawa {it_b} -> {it_w}, passes {sum(r[1] for r in b[0])} -> {sum(r[1] for r in w[0])}")
+    assert all(r[5] == 1 for r in w[0])                        # compared on every solve
+    assert sum(r[2] for r in w[0]) >= 8                        # the network's start won most steps
+    assert all(r[4] < r[3] for r in w[0] if r[2] == 1)         # ... on a smaller initial residual
+    assert it_w < it_b
+    assert max(w[2]) <= 1e-6
+    assert abs(w[1] - b[1]) < 1e-5 * abs(b[1])
+    n.close()
+    s.close()
+    base.close()

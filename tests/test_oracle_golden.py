@@ -177,3 +177,33 @@ def test_sdepv_run(oracle_lib):
         assert abs(o.vrms() - sc[2]) < 1e-12 * sc[2]
         assert rel(o.U()[: len(G[f"s{s}_U"])], G[f"s{s}_U"]) < 1e-12
         assert float(np.max(np.abs(o.T() - G[f"s{s}_T"]))) < 1e-13
+
+
+def test_residual_rule_on_the_oracle(oracle_lib):
+    """The residual stopping rule of the oracle (stop_rule 1, no counterpart in
+    the reference): the solution it stops on meets both residuals, recomputed
+    here from the oracle's own operators (pinned to the reference above), and
+    the rule stops far earlier than the reference's dv/v, dp/p rule on the
+    same state, which runs to its iteration cap."""
+    case = small_case()
+    case.accuracy, case.piterations, case.stop_rule = 1e-6, 1000, 1
+    T0 = conductive_T0(case, amp=0.01, seed=0)
+    o = oracle_lib.Oracle(case, gs_colored=False)
+    o.set_T(T0)
+    o.setup_operators()
+    info = o.solve_Ahat_p_fhat(case.accuracy, case.piterations)
+    f = o.fine
+    lev = len(o.dims) - 1
+    U, P, F = o.U()[: f["neq"]].copy(), o.P().copy(), o.F()[: f["neq"]].copy()
+    r = F - o.kmul(lev, U) - o.grad(lev, P)
+    mom = np.linalg.norm(r) / np.linalg.norm(F)
+    cont = np.linalg.norm(o.div(lev, U)) / (np.linalg.norm(U) * math.sqrt(f["nel"] / f["neq"]))
+    print(info, mom, cont)
+    assert mom <= case.accuracy and cont <= case.accuracy
+    assert abs(mom - info["momentum"]) <= 1e-8 * mom
+    case.stop_rule, case.piterations = 0, 375
+    o2 = oracle_lib.Oracle(case, gs_colored=False)
+    o2.set_T(T0)
+    o2.setup_operators()
+    info2 = o2.solve_Ahat_p_fhat(case.accuracy, case.piterations)
+    assert info["uzawa"] < info2["uzawa"]
