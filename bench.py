@@ -270,6 +270,7 @@ def loop_summary(r, ref=None):
     d = {"stokes_ms_per_step": float(np.mean([x["stokes_ms"] for x in recs])),
          "ms_per_step": float(np.mean([x["stokes_ms"] + x["energy_ms"] for x in recs])),
          "multigrid_ms_per_step": float(np.mean([x["pass_ms"] for x in recs])),
+         "assembly_ms_per_step": float(np.mean([x["assembly_ms"] for x in recs])),
          "uzawa_iterations": [x["uzawa"] for x in recs], "mg_passes": [x["mg_passes"] for x in recs],
          "corrections": [x["corrections"] for x in recs],
          "residuals_final_max": [max(x["final_momentum"] for x in recs), max(x["final_continuity"] for x in recs)],

@@ -165,7 +165,7 @@ class _CStats(ctypes.Structure):
                 ("warm_residual", ctypes.c_double), ("base_residual", ctypes.c_double),
                 ("pass_ms", ctypes.c_double), ("final_momentum", ctypes.c_double),
                 ("final_continuity", ctypes.c_double), ("corrections", ctypes.c_int),
-                ("warm_compared", ctypes.c_int)]
+                ("warm_compared", ctypes.c_int), ("assembly_ms", ctypes.c_double)]
 
 
 # every symbol of include/citcom_gb300.h with its argument types
@@ -387,7 +387,7 @@ class Solver:
                     warm_start=s.warm_start, warm_residual=s.warm_residual, base_residual=s.base_residual,
                     visc_iterations=s.visc_iterations, visc_misfit=s.visc_misfit, pass_ms=s.pass_ms,
                     final_momentum=s.final_momentum, final_continuity=s.final_continuity,
-                    corrections=s.corrections, warm_compared=s.warm_compared)
+                    corrections=s.corrections, warm_compared=s.warm_compared, assembly_ms=s.assembly_ms)
 
     def stokes_residuals(self):
         """(|F - K U - G P| / |F|, |div U| / (|U| sqrt(npno/neq))) of the resident solution."""

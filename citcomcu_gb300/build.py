@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libcitcom_gb300.so")
 BUILD = os.path.join(HERE, "_build")
-SOURCES = ["kernels.cu", "tile.cu", "coarse.cu", "citcom_gpu.cu", "noalloc.cu", "nn.cu", "geometry.cu", "mf.cu"]
+SOURCES = ["kernels.cu", "tile.cu", "coarse.cu", "citcom_gpu.cu", "noalloc.cu", "nn.cu", "geometry.cu", "mf.cu", "assemble.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 

@@ -62,6 +62,9 @@ struct citcom_gpu
 	float *BI32[CITCOM_MAX_LEVELS];
 	float4 *Kt32[CITCOM_MAX_LEVELS];  // padded FP32 stencil of the levels k_gs_tiny smooths, else null
 	float *eta32[CITCOM_MAX_LEVELS];  // FP32 Gauss-point viscosity of the levels the matrix-free smoother relaxes, else null
+	GeoDF *geodf[CITCOM_MAX_LEVELS];  // box element kernels as FP32 pairs (mixed configuration), else null
+	float2 *eta2[CITCOM_MAX_LEVELS];  // Gauss-point viscosity as FP32 pairs for the double-float assembly
+	bool fp64_assembly;               // CITCOM_GPU_FP64_ASSEMBLY: the mixed configuration assembles in FP64
 	double *BPI;
 	MG<double> mg64;
 	MG<float> mg32;
@@ -78,6 +81,7 @@ struct citcom_gpu
 	cudaEvent_t ev0, ev1;
 	cudaEvent_t ev_pass[2];  // brackets each multigrid pass
 	cudaEvent_t ev_energy[2];  // brackets the PG_timestep of step_resident
+	cudaEvent_t ev_asm[2];     // brackets the operator assembly of stokes_resident
 	cudaEvent_t ev_gs[8];   // brackets the finest-level smoother calls inside a multigrid pass
 	int n_gs_pairs;         // pairs recorded by the captured pass
 	cudaGraphExec_t mg_exec;
@@ -888,8 +892,12 @@ int construct_stiffness(citcom_gpu *h)
 	{
 		const bool need64 = (c.precision == CITCOM_GPU_FP64) || l == lmax;
 		const bool need32 = (c.precision == CITCOM_GPU_MIXED);
-		launch_assemble(h->st, h->lv[l], h->geo[l], h->evi[l], c.aug_lagr, c.aug_number, need64 ? h->K64[l] : nullptr,
-		                need32 ? h->K32[l] : nullptr, need64 ? h->BI64[l] : nullptr, need32 ? h->BI32[l] : nullptr);
+		if(h->geodf[l])
+			launch_assemble_df(h->st, h->lv[l], h->geodf[l], h->evi[l], h->eta2[l], c.aug_lagr, need64 ? h->K64[l] : nullptr,
+			                   need32 ? h->K32[l] : nullptr, need64 ? h->BI64[l] : nullptr, need32 ? h->BI32[l] : nullptr);
+		else
+			launch_assemble(h->st, h->lv[l], h->geo[l], h->evi[l], c.aug_lagr, c.aug_number, need64 ? h->K64[l] : nullptr,
+			                need32 ? h->K32[l] : nullptr, need64 ? h->BI64[l] : nullptr, need32 ? h->BI32[l] : nullptr);
 		if(h->Kt32[l])
 			launch_tiny_stencil(h->st, h->lv[l], h->K32[l], h->Kt32[l]);
 		if(h->eta32[l])
@@ -964,6 +972,7 @@ int stokes_resident(citcom_gpu *h)
 	// update, until |dU| / |U| <= sdepv_misfit or max_sdep_visc_iter
 	const bool iterate = h->cfg.sdepv != 0;
 	const bool update = h->cfg.tdepv || iterate;
+	bool asm_timed = false;
 	int vcount = 0, uzawa_total = 0;
 	double misfit = 0.0;
 	do
@@ -971,7 +980,12 @@ int stokes_resident(citcom_gpu *h)
 		if(update || !h->visc_ready)
 			TRY(viscosity_from_device_T(h));
 		if(update || !h->stiffness_ready)
+		{
+			CK(cudaEventRecord(h->ev_asm[0], h->st));
 			TRY(construct_stiffness(h));
+			CK(cudaEventRecord(h->ev_asm[1], h->st));
+			asm_timed = true;
+		}
 		int steps = h->cfg.piterations;
 		double r0;
 		TRY(uzawa(h, h->U, h->P, h->F, h->cfg.accuracy, &steps, &r0));
@@ -1002,6 +1016,9 @@ int stokes_resident(citcom_gpu *h)
 	float ms = 0.f;
 	CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
 	h->stats.stokes_ms = ms;
+	h->stats.assembly_ms = 0.0;
+	if(asm_timed && cudaEventElapsedTime(&ms, h->ev_asm[0], h->ev_asm[1]) == cudaSuccess)
+		h->stats.assembly_ms = ms;
 	return CITCOM_GPU_OK;
 }
 
@@ -1164,6 +1181,8 @@ int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 		h->no_tiny = tn && tn[0] && tn[0] != '0';
 		const char *mf = getenv("CITCOM_GPU_MF");
 		h->mf = mf && mf[0] && mf[0] != '0';
+		const char *fa = getenv("CITCOM_GPU_FP64_ASSEMBLY");
+		h->fp64_assembly = fa && fa[0] && fa[0] != '0';
 		const char *q = getenv("CITCOM_GPU_NO_PDL");
 		if(q && q[0] && q[0] != '0')
 			g_use_pdl = 0;
@@ -1189,7 +1208,8 @@ int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 		for(int k = 0; k < 8; ++k)
 			ev_ok = ev_ok && cudaEventCreate(&h->ev_gs[k]) == cudaSuccess;
 		for(int k = 0; k < 2; ++k)
-			ev_ok = ev_ok && cudaEventCreate(&h->ev_pass[k]) == cudaSuccess && cudaEventCreate(&h->ev_energy[k]) == cudaSuccess;
+			ev_ok = ev_ok && cudaEventCreate(&h->ev_pass[k]) == cudaSuccess && cudaEventCreate(&h->ev_energy[k]) == cudaSuccess &&
+			        cudaEventCreate(&h->ev_asm[k]) == cudaSuccess;
 		if(!ev_ok || cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess ||
 		   cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess)
 		{
@@ -1232,6 +1252,21 @@ int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 				{
 					r = fail(h, CITCOM_GPU_ERR_CUDA, "geometry upload failed");
 					goto failed;
+				}
+				h->geodf[l] = nullptr;
+				h->eta2[l] = nullptr;
+				if(cfg->precision == CITCOM_GPU_MIXED && !L.sphere && !h->fp64_assembly)
+				{
+					// the mixed configuration assembles the box levels in double-float
+					std::vector<GeoDF> gd(1);
+					geo_df_fill(g[0], cfg->aug_lagr, cfg->aug_number, gd.data());
+					TRYC(dalloc(h, &h->geodf[l], 1));
+					TRYC(dalloc(h, &h->eta2[l], (size_t)8 * L.nel));
+					if(cudaMemcpy(h->geodf[l], gd.data(), sizeof(GeoDF), cudaMemcpyHostToDevice) != cudaSuccess)
+					{
+						r = fail(h, CITCOM_GPU_ERR_CUDA, "geometry upload failed");
+						goto failed;
+					}
 				}
 				if(l == lmax)
 				{
@@ -1396,6 +1431,8 @@ void citcom_gpu_destroy(citcom_gpu *h)
 			cudaEventDestroy(h->ev_pass[k]);
 		if(h->ev_energy[k])
 			cudaEventDestroy(h->ev_energy[k]);
+		if(h->ev_asm[k])
+			cudaEventDestroy(h->ev_asm[k]);
 	}
 	if(h->st)
 		cudaStreamDestroy(h->st);

@@ -147,6 +147,20 @@ void launch_coarse_dense_build(cudaStream_t st, const Lvl &L, const float4 *Kt, 
 
 // Stencil kernels of the tiled (large) levels, tile.cu: persistent CTAs
 // streaming tiles through shared memory with bulk copies
+// Box-level element kernels as (hi, lo) FP32 pairs for the double-float
+// assembly (assemble.cu): Mk of Geo, and lambda g_a,i g_b,j of the augmented
+// term (zero without it)
+struct GeoDF
+{
+	float mh[8][8][8][9], ml[8][8][8][9];
+	float lgh[8][8][9], lgl[8][8][9];
+};
+void geo_df_fill(const Geo &g, int aug, double lambda, GeoDF *out);
+// construct_node_ks of a box level in double-float arithmetic: splits evi into
+// eta2 (8 nel float2), then K64 / K32 (either may be null) and BI64 / BI32
+void launch_assemble_df(cudaStream_t st, const Lvl &L, const GeoDF *G, const double *evi, float2 *eta2, int aug,
+                        double *K64, float *K32, double *BI64, float *BI32);
+
 // matrix-free FP32 Gauss-Seidel colour of a box level (mf.cu): eta = the
 // level's Gauss-point viscosity in FP32 (8 per element), BI = 1/diag K in
 // colour-position order

@@ -135,6 +135,7 @@ typedef struct citcom_gpu_stats
 	double final_continuity;    /* |B U| / (|U| sqrt(npno/neq)) */
 	int corrections;
 	int warm_compared;          /* 1: both starts' heads ran (base_residual is then set) */
+	double assembly_ms;         /* device time of the last operator assembly inside stokes_resident */
 } citcom_gpu_stats;
 
 /* Allocates every device buffer the solver will use (on the current

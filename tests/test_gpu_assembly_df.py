@@ -1,0 +1,66 @@
+"""The double-float operator assembly of the mixed configuration
+(assemble.cu) against the FP64 assembly (k_assemble) and the oracle.
+
+The mixed configuration assembles the box levels with every product and sum
+carried as a pair of FP32 numbers (about 46 significant bits).  Its FP64
+finest-level stencil (the one the refinement residual and the residual rule
+use) must then agree with the FP64 assembly to 1e-12 relative, its 1/diag K
+likewise, and the FP32 stencils of the coarser levels to FP32 rounding
+(1e-6); CITCOM_GPU_FP64_ASSEMBLY=1 restores the FP64 assembly.
+"""
+import math
+import os
+
+import numpy as np
+import pytest
+
+from oracle.decks import Case
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def cg():
+    import citcomcu_gb300 as cg
+    cg.build()
+    return cg
+
+
+@pytest.mark.parametrize("aug", [True, False])
+def test_double_float_assembly(cg, oracle_lib, aug):
+    # two viscosity layers and a 10^4 temperature contrast: entries spanning
+    # several orders of magnitude
+    case = Case(mgunit=(2, 3, 2), levels=4, dimen=(1.0, 1.5, 1.0), rayleigh=1e5, tdepv=True, visc0=(1.0, 30.0),
+                viscE=(math.log(1e4), math.log(1e4)), viscT=(0.0, 0.0), z_layer=(0.6,), aug_lagr=aug)
+    rng = np.random.Generator(np.random.PCG64(3))
+    nno = case.nox * case.noy * case.noz
+    z = np.tile(np.linspace(0.0, 1.0, case.noz), case.nox * case.noy)
+    T = np.clip(1.0 - z + 0.05 * rng.uniform(-1, 1, nno), 0.0, 1.0)
+    out = {}
+    for prec in (0, 1):
+        s = cg.Solver(cg.Config.like(case, precision=prec))
+        s.get_system_viscosity(T)
+        s.construct_stiffness_B_matrix()
+        lmax = case.levels - 1
+        u = np.sin(0.37 * np.arange(s.dims[lmax]["neq"]) + 0.3)
+        uc = np.sin(0.29 * np.arange(s.dims[lmax - 1]["neq"]) + 0.1)
+        out[prec] = dict(K=s.op_kmul(lmax, u), Kc=s.op_kmul(lmax - 1, uc), BI=s.op_diagonals(lmax)[0],
+                         BIc=s.op_diagonals(lmax - 1)[0])
+        s.close()
+    o = oracle_lib.Oracle(case)
+    o.set_T(T)
+    o.setup_operators()
+    lmax = case.levels - 1
+    u = np.sin(0.37 * np.arange(o.dims[lmax]["neq"]) + 0.3)
+    print(rel(out[1]["K"], out[0]["K"]), rel(out[1]["BI"], out[0]["BI"]), rel(out[1]["Kc"], out[0]["Kc"]))
+    assert rel(out[1]["K"], out[0]["K"]) < 1e-12
+    assert rel(out[1]["K"], o.kmul(lmax, u)) < 1e-12
+    assert rel(out[1]["BI"], out[0]["BI"]) < 1e-12
+    assert rel(out[1]["Kc"], out[0]["Kc"]) < 1e-6
+    assert rel(out[1]["BIc"], out[0]["BIc"]) < 1e-6
