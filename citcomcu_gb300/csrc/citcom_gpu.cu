@@ -105,6 +105,11 @@ struct citcom_gpu
 	// (CITCOM_GPU_NO_DENSE keeps the sweeps): N and its build scratch
 	float *co_dense;
 	float *co_dense_work;
+	// the same for level 1 (its sweeps of `co_dense1_cycles`, zero start or
+	// with a start through d0 + N (f - K d0)) when it runs in the cluster program
+	float *co_dense1;
+	float *co_dense1_work;
+	int co_dense1_cycles;
 	CoLevels co_lv;
 	CoProg co_prog;
 	double lt_ms[CITCOM_MAX_LEVELS];
@@ -357,6 +362,16 @@ template <typename T> bool co_level(citcom_gpu *h, int lev)
 
 void co_push(citcom_gpu *h, int type, int lev, int a, int b, int c, int cycles = 0, int zero = 0)
 {
+	if(type == CO_GS && lev == 1 && h->co_dense1 && cycles == h->co_dense1_cycles)
+	{
+		// level 1's sweeps as its dense smoother matrix: d = N f from a zero
+		// start, else AU = f - K d, then d += N AU (AU is free here: the line
+		// search that follows a smoothing call recomputes it)
+		if(!zero)
+			co_push(h, CO_RESID, lev, b, a, CO_AU);
+		co_push(h, CO_DENSE, lev, a, zero ? b : CO_AU, 0, cycles, zero);
+		return;
+	}
 	if(h->co_prog.n == CO_MAX_OPS)
 		co_flush(h);
 	CoOp &op = h->co_prog.op[h->co_prog.n++];
@@ -905,6 +920,9 @@ int construct_stiffness(citcom_gpu *h)
 		if(l == 0 && h->co_dense)
 			launch_coarse_dense_build(h->st, h->lv[0], h->Kt32[0], h->BI32[0], c.vlowstep, h->co_dense_work, h->co_dense,
 			                          h->dscal + S_ERR);
+		if(l == 1 && h->co_dense1)
+			launch_dense_build_gs(h->st, h->lv[1], h->K32[1], h->BI32[1], h->co_dense1_cycles, h->co_dense1_work,
+			                      h->co_dense1);
 	}
 	launch_bpi(h->st, h->lv[lmax], h->geo[lmax], h->BI64[lmax], h->BPI, c.precond);
 	CK(cudaGetLastError());
@@ -1336,7 +1354,25 @@ int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 				TRYC(dalloc(h, &h->co_dense_work, 2 * n * n));
 			}
 		}
-		h->co_lv.dense = h->co_dense;
+		h->co_dense1 = nullptr;
+		h->co_dense1_work = nullptr;
+		h->co_dense1_cycles = cfg->down_heavy;
+		if(h->co_dense && h->co_LC >= 1 && !h->co_local[1] && h->L > 2 && h->lv[1].neq <= CO_DENSE1_MAX_EQ)
+		{
+			int maxc = 0;
+			for(int c = 0; c < 8; ++c)
+				maxc = std::max(maxc, h->lv[1].coff[c + 1] - h->lv[1].coff[c]);
+			if(maxc <= CO_DENSE1_MAX_COLOUR)
+			{
+				const size_t n = (size_t)h->lv[1].neq;
+				TRYC(dalloc(h, &h->co_dense1, n * n));
+				TRYC(dalloc(h, &h->co_dense1_work, n * n));
+			}
+		}
+		for(int l = 0; l < CO_MAX_LEV; ++l)
+			h->co_lv.dense[l] = nullptr;
+		h->co_lv.dense[0] = h->co_dense;
+		h->co_lv.dense[1] = h->co_dense1;
 		TRYC(dalloc(h, &h->BPI, Lf.nel));
 		TRYC(dalloc(h, &h->visc_work[0], Lf.nno));
 		TRYC(dalloc(h, &h->visc_work[1], Lf.nno));

@@ -593,8 +593,8 @@ __global__ void __launch_bounds__(CO_THREADS) k_coarse(const __grid_constant__ C
 		}
 		case CO_DENSE:
 		{
-			// vec a = N vec b: this CTA's rows, one warp per row, the
-			// right-hand side staged in shared memory
+			// vec a = N vec b (or += with a start): this CTA's rows, one warp
+			// per row, the right-hand side staged in shared memory
 			float *sv = reinterpret_cast<float *>(arena);
 			const int n = L.neq;
 			co_stage(D.vec[l][op.b], n, sv);
@@ -602,9 +602,10 @@ __global__ void __launch_bounds__(CO_THREADS) k_coarse(const __grid_constant__ C
 			co_chunk(n, rank, ncta, lo, cnt);
 			const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 			float *out = D.vec[l][op.a];
+			const float *Nl = D.dense[l];
 			for(int i = lo + warp; i < lo + cnt; i += CO_WARPS)
 			{
-				const float *row = D.dense + (size_t)i * n;
+				const float *row = Nl + (size_t)i * n;
 				float s = 0.f;
 				for(int k = lane; k < n; k += 32)
 					s += __ldg(row + k) * sv[k];
@@ -612,7 +613,7 @@ __global__ void __launch_bounds__(CO_THREADS) k_coarse(const __grid_constant__ C
 				for(int o = 16; o > 0; o >>= 1)
 					s += __shfl_xor_sync(0xffffffffu, s, o);
 				if(lane == 0)
-					out[i] = s;
+					out[i] = op.zero ? s : __ldcg(out + i) + s;
 			}
 			halo_lev = -1;
 			break;
@@ -707,7 +708,64 @@ __global__ void k_co_dense_t(int n, const float *cols, float *N)
 	N[t] = cols[(size_t)j * n + i];
 }
 
+// column j of a level's smoother matrix: `cycles` zero-start sweeps of the
+// 8 colours (each node of a colour: r = f - K d over its 27 neighbours, then
+// d += r o 1/diag, the update of gauss_seidel) against f = e_j, d in
+// work[j n ..]; N[i n + j] = d_i.  The rows of a colour are formed before any
+// of its nodes is updated (a node's own block reads its old values).
+__global__ void __launch_bounds__(256) k_dense_build_gs(Lvl L, const float *__restrict__ K, const float *__restrict__ BI,
+                                                        int cycles, float *work, float *N)
+{
+	pdl_begin();
+	__shared__ float rs[3 * CO_DENSE1_MAX_COLOUR];
+	const int n = L.neq, j = blockIdx.x;
+	float *d = work + (size_t)j * n;
+	for(int i = threadIdx.x; i < n; i += blockDim.x)
+		d[i] = 0.f;
+	__syncthreads();
+	for(int cyc = 0; cyc < cycles; ++cyc)
+		for(int c = 0; c < 8; ++c)
+		{
+			const int cnt = L.coff[c + 1] - L.coff[c];
+			for(int t = threadIdx.x; t < 3 * cnt; t += blockDim.x)
+			{
+				const int q = t / 3, i = t - 3 * q, p = L.coff[c] + q;
+				int x, y, z;
+				cg_decode(L, c, q, x, y, z);
+				float r = (3 * cg_node(L, x, y, z) + i == j) ? 1.f : 0.f;
+				for(int s = 0; s < 27; ++s)
+				{
+					const int mz = z + s % 3 - 1, mx = x + (s / 3) % 3 - 1, my = y + s / 9 - 1;
+					if(mx < 0 || mx >= L.nox || my < 0 || my >= L.noy || mz < 0 || mz >= L.noz)
+						continue;
+					const int m = cg_node(L, mx, my, mz);
+#pragma unroll
+					for(int jj = 0; jj < 3; ++jj)
+						r -= K[cg_kidx(L, s, i, jj, p)] * d[3 * m + jj];
+				}
+				rs[t] = r * BI[3 * (size_t)p + i];
+			}
+			__syncthreads();
+			for(int t = threadIdx.x; t < 3 * cnt; t += blockDim.x)
+			{
+				const int q = t / 3, i = t - 3 * q;
+				int x, y, z;
+				cg_decode(L, c, q, x, y, z);
+				d[3 * cg_node(L, x, y, z) + i] += rs[t];
+			}
+			__syncthreads();
+		}
+	for(int i = threadIdx.x; i < n; i += blockDim.x)
+		N[(size_t)i * n + j] = d[i];
+}
+
 } // namespace
+
+void launch_dense_build_gs(cudaStream_t st, const Lvl &L, const float *K, const float *BI, int cycles, float *work, float *N)
+{
+	k_dense_build_gs<<<L.neq, 256, 0, st>>>(L, K, BI, cycles, work, N);
+	++g_kernel_launches;
+}
 
 int coarse_init(int *cluster_size)
 {

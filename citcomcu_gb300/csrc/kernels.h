@@ -101,7 +101,8 @@ enum CoOpType
 	CO_INTERP,  // vec b (level lev) = interpolation of vec a (level lev-1), stripped
 	CO_KDOT,    // vec c = K vec a; alpha = (c . vec b) / (c . c), FP64; if `zero`: then vel += alpha vec a
 	CO_UPD,     // vec a += alpha vec b
-	CO_DENSE    // vec a = N vec b: `cycles` zero-start sweeps of level 0 as one dense product
+	CO_DENSE    // `cycles` sweeps of a level as one dense product: vec a = N vec b (zero start, `zero`)
+	            // or vec a += N vec b (vec b the residual of vec a; a smoother with a start)
 };
 #define CO_MAX_LEV 6
 #define CO_MAX_OPS 96
@@ -126,7 +127,7 @@ struct CoLevels
 	int win[CO_MAX_LEV];  // ranks on either side of a node's owner that hold its neighbours
 	const Geo *geo[CO_MAX_LEV];  // geometry tables (TWW of the projection, sizes of the interpolation)
 	double *err;          // set to 1 if a wait of the cluster smoother timed out
-	const float *dense;   // N (neq x neq, row-major) of the level-0 smoother, or null
+	const float *dense[CO_MAX_LEV];  // N (neq x neq, row-major) of a level's smoother, or null
 };
 // cluster size the device supports for the program (16 or 8); -1 if none
 int coarse_init(int *cluster_size);
@@ -144,6 +145,14 @@ void launch_coarse(cudaStream_t st, const CoLevels &D, const CoProg &P, int clus
 #define CO_DENSE_MAX_EQ 2048
 void launch_coarse_dense_build(cudaStream_t st, const Lvl &L, const float4 *Kt, const float *BI, int cycles, float *work, float *N,
                                double *err);
+// The same matrix for a level above the one-CTA smoother's size (level 1 of
+// the cluster program): column j is `cycles` zero-start colour sweeps against
+// e_j, one CTA per column, with the level's FP32 stencil K (cg_kidx layout)
+// and 1/diag BI (position order).  A smoother with a start d0 is then
+// d = d0 + N (f - K d0), the same N.  work: neq^2 floats; N: neq^2 floats.
+#define CO_DENSE1_MAX_EQ 4096
+#define CO_DENSE1_MAX_COLOUR 1024   // nodes of the largest colour
+void launch_dense_build_gs(cudaStream_t st, const Lvl &L, const float *K, const float *BI, int cycles, float *work, float *N);
 
 // Stencil kernels of the tiled (large) levels, tile.cu: persistent CTAs
 // streaming tiles through shared memory with bulk copies

@@ -77,3 +77,41 @@ def test_dense_coarsest_smoother_whole_solve(cg):
     (U1, V1, it1, nu1), (U2, V2, it2, nu2) = res
     assert abs(it1 - it2) <= 1, (it1, it2)
     assert rel(V1, V2) < 1e-5 and abs(nu1 - nu2) < 1e-6 * abs(nu2)
+
+
+def test_dense_level1_smoother_matches_sweeps(cg):
+    """Level 1 of the cluster program: its down_heavy / up_heavy sweeps (3) as
+    one dense product, d = N f from a zero start and d = d0 + N (f - K d0)
+    with a start (the same N: the smoother is a stationary iteration), against
+    the sweeps themselves, to FP32 summation order."""
+    from oracle.decks import Case
+    case = Case(mgunit=(2, 3, 2), levels=4, dimen=(1.0, 1.5, 1.0), rayleigh=1e5, tdepv=True, visc0=(1.0,),
+                viscE=(np.log(1e3),), viscT=(0.0,))
+    nno = case.nox * case.noy * case.noz
+    rng = np.random.Generator(np.random.PCG64(5))
+    z = np.tile(np.linspace(0.0, 1.0, case.noz), case.nox * case.noy)
+    T0 = np.clip(1.0 - z + 0.02 * rng.uniform(-1, 1, nno), 0.0, 1.0)
+    out = []
+    for dense in (True, False):
+        s = make(cg, case, dense)
+        try:
+            s.get_system_viscosity(T0)
+            s.construct_stiffness_B_matrix()
+            dm = s.dims[1]
+            n1 = dm["neq"]
+            # free-slip: the dof normal to each wall is constrained (vectors
+            # stripped there, as the multigrid pass keeps them)
+            node = np.arange(dm["nno"])
+            zz, xx, yy = node % dm["noz"], (node // dm["noz"]) % dm["nox"], node // (dm["noz"] * dm["nox"])
+            free = np.stack([(xx > 0) & (xx < dm["nox"] - 1), (yy > 0) & (yy < dm["noy"] - 1),
+                             (zz > 0) & (zz < dm["noz"] - 1)], axis=1).reshape(-1)
+            F = np.sin(0.31 * np.arange(n1) + 0.4) * free
+            d0 = 0.5 * np.cos(0.17 * np.arange(n1)) * free
+            da, _ = s.op_gauss_seidel(1, F, 3)
+            db, _ = s.op_gauss_seidel(1, F, 3, d0=da + d0)
+            out.append((da, db))
+        finally:
+            s.close()
+    (a1, b1), (a2, b2) = out
+    print(rel(a1, a2), rel(b1, b2))
+    assert rel(a1, a2) < 1e-5 and rel(b1, b2) < 1e-5
