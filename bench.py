@@ -30,7 +30,7 @@ solves of other seeds (training time reported, not timed into `value`).
 `e2e` runs the headline loop through the C ABI with host buffers (pinned):
 PG_timestep and general_stokes_solver per step, the copies inside the timed
 region.  `drift` runs the 64^3 box (mixed vs FP64 plain) for --drift-steps
-steps and reports the per-step Nu / Vrms drift.
+steps (200, as configs[1] asks) and reports the per-step Nu / Vrms drift.
 
   python bench.py [--steps K] [--warmup W] [--gpus N] [--impl reference]
                   [--workload cfg2|cube|sphere] [--no-cpu] [--no-learned]
@@ -385,11 +385,13 @@ def output_step(s, reps: int = 10):
             "fields": "T, V, P, heatflux, heatflux_adv, Have (T, vrms, Vi, Rho, F, f), shflux, bhflux, Nut, Nub, Vrms"}
 
 
-def drift_run(cg, size, steps):
-    """The 64^3 box (eta = exp(-ln(1e3) T), Ra 1e5) from its seeded state:
-    `steps` time steps of the mixed path and of the FP64 plain path; the
-    per-step relative differences of Nu and Vrms and the final U, P, T."""
-    case = workload(size)
+def drift_run(cg, which, steps):
+    """A workload from its seeded state (`which`: "cube" the 64^3 box, eta =
+    exp(-ln(1e3) T), Ra 1e5; "cfg2" the 128x128x64 box): `steps` time steps of
+    the mixed path and of the FP64 plain path; the per-step relative
+    differences of Nu and Vrms (every step, and their maxima) and the final U,
+    P, T."""
+    case = cfg2_workload() if which == "cfg2" else workload(64)
     T0 = seeded_T0(case)
     r = {}
     for name, prec in (("mixed", cg.MIXED), ("fp64_plain", cg.FP64)):
@@ -564,7 +566,9 @@ def main():
                     help="compare the network's start with the previous step's on every k-th solve (and whenever "
                          "its initial residual grows past 4x the last winning one); 1: every solve")
     ap.add_argument("--cold-reps", type=int, default=2, help="cold solves per mode (0: skip)")
-    ap.add_argument("--drift-steps", type=int, default=50, help="time steps of the 64^3 drift run (0: skip)")
+    ap.add_argument("--drift-steps", type=int, default=200, help="time steps of the drift run (0: skip)")
+    ap.add_argument("--drift-workload", default="cube", choices=["cube", "cfg2"],
+                    help="drift run: the 64^3 box (configs[1], 200 steps by default) or the 128x128x64 box")
     ap.add_argument("--ref-full-steps", type=int, default=2,
                     help="reference arm: complete time steps timed in full after the cold solve")
     args = ap.parse_args()
@@ -705,7 +709,7 @@ def main():
         ln.close()
         ls.close()
     if args.drift_steps > 0 and args.workload != "sphere":
-        line["drift"] = drift_run(cg, 64, args.drift_steps)
+        line["drift"] = drift_run(cg, args.drift_workload, args.drift_steps)
     if not args.no_cpu and case.sphere is None:  # the oracle has no spherical geometry
         pps = float(np.mean([r["mg_passes"] for r in (fp64 or mixed)["recs"]]))
         line["cpu_baseline"] = cpu_sample(case, T0, pps)
