@@ -14,6 +14,10 @@
 // the FP64 stencil keeps 46 and the FP32 stencil 24.  The FP64 pipe only
 // converts the finished entries.
 //
+// With K32lo the entry's FP32 remainder (entry - K32) is written as well:
+// the finest level's FP64 operator held as the pair K32 + K32lo (tile.cu,
+// k_tile_split).
+//
 // Work split: one warp per (tile of 32 colour positions, slot); lane = node,
 // so the nine words a lane writes per slot are consecutive with its
 // neighbours' in the tile-major stencil (level.h, cg_kidx) and every lane of
@@ -62,7 +66,8 @@ constexpr int AS_THREADS = 256;
 __global__ void __launch_bounds__(AS_THREADS) k_assemble_df(Lvl L, const GeoDF *__restrict__ G,
                                                            const float2 *__restrict__ eta2, int aug,
                                                            double *__restrict__ K64, float *__restrict__ K32,
-                                                           double *__restrict__ BI64, float *__restrict__ BI32)
+                                                           float *__restrict__ K32lo, double *__restrict__ BI64,
+                                                           float *__restrict__ BI32)
 {
 	pdl_begin();
 	const int lane = threadIdx.x & 31;
@@ -175,10 +180,13 @@ __global__ void __launch_bounds__(AS_THREADS) k_assemble_df(Lvl L, const GeoDF *
 		for(int j = 0; j < 3; ++j)
 		{
 			const size_t off = cg_kidx(L, s, i, j, p);
+			const float hi = (float)blk[3 * i + j];
 			if(K64)
 				K64[off] = blk[3 * i + j];
 			if(K32)
-				K32[off] = (float)blk[3 * i + j];
+				K32[off] = hi;
+			if(K32lo)
+				K32lo[off] = (float)(blk[3 * i + j] - (double)hi);
 		}
 }
 
@@ -218,11 +226,11 @@ void geo_df_fill(const Geo &g, int aug, double lambda, GeoDF *out)
 }
 
 void launch_assemble_df(cudaStream_t st, const Lvl &L, const GeoDF *G, const double *evi, float2 *eta2, int aug,
-                        double *K64, float *K32, double *BI64, float *BI32)
+                        double *K64, float *K32, float *K32lo, double *BI64, float *BI32)
 {
 	const int n = 8 * L.nel;
 	as_launch(k_eta_split, (n + 255) / 256, 256, st, n, evi, eta2);
 	const long warps = 27L * L.toff[8];
 	as_launch(k_assemble_df, (int)((warps * 32 + AS_THREADS - 1) / AS_THREADS), AS_THREADS, st, L, G,
-	          (const float2 *)eta2, aug, K64, K32, BI64, BI32);
+	          (const float2 *)eta2, aug, K64, K32, K32lo, BI64, BI32);
 }

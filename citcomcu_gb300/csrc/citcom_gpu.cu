@@ -63,6 +63,8 @@ struct citcom_gpu
 	float4 *Kt32[CITCOM_MAX_LEVELS];  // padded FP32 stencil of the levels k_gs_tiny smooths, else null
 	float *eta32[CITCOM_MAX_LEVELS];  // FP32 Gauss-point viscosity of the levels the matrix-free smoother relaxes, else null
 	GeoDF *geodf[CITCOM_MAX_LEVELS];  // box element kernels as FP32 pairs (mixed configuration), else null
+	float *K32lo;                     // mixed box: the finest FP64 operator's FP32 remainder (K64 = K32 + K32lo), else null
+	bool no_split;                    // CITCOM_GPU_NO_SPLIT: keep the finest FP64 stencil instead
 	float2 *eta2[CITCOM_MAX_LEVELS];  // Gauss-point viscosity as FP32 pairs for the double-float assembly
 	bool fp64_assembly;               // CITCOM_GPU_FP64_ASSEMBLY: the mixed configuration assembles in FP64
 	double *BPI;
@@ -260,6 +262,26 @@ int readback(citcom_gpu *h, int slot, int n)
 	CK(cudaMemcpyAsync(h->hscal + slot, h->dscal + slot, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
 	CK(cudaStreamSynchronize(h->st));
 	return CITCOM_GPU_OK;
+}
+
+// K u and f - K u with the finest level's FP64 operator: the FP64 stencil,
+// or (mixed box) the FP32 pair K32 + K32lo in double-float arithmetic
+void fine_kmul64(citcom_gpu *h, const double *u, double *out)
+{
+	const int lmax = h->L - 1;
+	if(h->K32lo)
+		launch_tile_split(h->st, h->lv[lmax], h->K32[lmax], h->K32lo, nullptr, u, out);
+	else
+		launch_kmul<double>(h->st, h->lv[lmax], h->K64[lmax], u, out);
+}
+
+void fine_residual64(citcom_gpu *h, const double *f, const double *u, double *r)
+{
+	const int lmax = h->L - 1;
+	if(h->K32lo)
+		launch_tile_split(h->st, h->lv[lmax], h->K32[lmax], h->K32lo, f, u, r);
+	else
+		launch_residual<double>(h->st, h->lv[lmax], h->K64[lmax], f, u, r);
 }
 
 // The error words of the kernels' bounded waits (the tile kernels' g_tile_err,
@@ -581,7 +603,8 @@ int record_pass(citcom_gpu *h)
 		launch_copy_d2f(h->st, Lf.neq, h->mg32.fl[lmax], h->r64);
 		mg_pass<float>(h, h->mg32);
 		launch_add_f2d(h->st, Lf.neq, h->u1, h->mg32.vel[lmax]);
-		launch_residual64(h->st, Lf, h->K64[lmax], h->Ah, h->u1, h->r64, red_of(h), h->dscal + S_RES);
+		fine_residual64(h, h->Ah, h->u1, h->r64);
+		launch_dot(h->st, Lf.neq, h->r64, h->r64, red_of(h), h->dscal + S_RES);
 	}
 	return CITCOM_GPU_OK;
 }
@@ -692,7 +715,7 @@ int uzawa_start(citcom_gpu *h, double *V, const double *P, const double *F, doub
 	cudaStream_t st = h->st;
 	int valid;
 	launch_grad(st, Lf, geo, P, h->Ah);
-	launch_kmul<double>(st, Lf, h->K64[lmax], V, h->u1);
+	fine_kmul64(h, V, h->u1);
 	launch_sub3(st, Lf.neq, h->Ah, F, h->Ah, h->u1);
 	launch_strip(st, Lf, h->Ah);
 	TRY(solve_del2_u(h, acc, &valid));
@@ -716,7 +739,7 @@ int momentum_rr(citcom_gpu *h, const double *V, const double *P, const double *F
 	const int lmax = h->L - 1;
 	const Lvl &Lf = h->lv[lmax];
 	launch_grad(h->st, Lf, h->geo[lmax], P, h->Ah);
-	launch_kmul<double>(h->st, Lf, h->K64[lmax], V, h->u1);
+	fine_kmul64(h, V, h->u1);
 	launch_sub3(h->st, Lf.neq, h->r64, F, h->Ah, h->u1);
 	launch_dot(h->st, Lf.neq, h->r64, h->r64, red_of(h), h->dscal + S_R0 + 2);
 	TRY(readback(h, S_R0 + 2, 1));
@@ -909,7 +932,8 @@ int construct_stiffness(citcom_gpu *h)
 		const bool need32 = (c.precision == CITCOM_GPU_MIXED);
 		if(h->geodf[l])
 			launch_assemble_df(h->st, h->lv[l], h->geodf[l], h->evi[l], h->eta2[l], c.aug_lagr, need64 ? h->K64[l] : nullptr,
-			                   need32 ? h->K32[l] : nullptr, need64 ? h->BI64[l] : nullptr, need32 ? h->BI32[l] : nullptr);
+			                   need32 ? h->K32[l] : nullptr, l == lmax ? h->K32lo : nullptr, need64 ? h->BI64[l] : nullptr,
+			                   need32 ? h->BI32[l] : nullptr);
 		else
 			launch_assemble(h->st, h->lv[l], h->geo[l], h->evi[l], c.aug_lagr, c.aug_number, need64 ? h->K64[l] : nullptr,
 			                need32 ? h->K32[l] : nullptr, need64 ? h->BI64[l] : nullptr, need32 ? h->BI32[l] : nullptr);
@@ -1201,6 +1225,8 @@ int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 		h->mf = mf && mf[0] && mf[0] != '0';
 		const char *fa = getenv("CITCOM_GPU_FP64_ASSEMBLY");
 		h->fp64_assembly = fa && fa[0] && fa[0] != '0';
+		const char *ns = getenv("CITCOM_GPU_NO_SPLIT");
+		h->no_split = ns && ns[0] && ns[0] != '0';
 		const char *q = getenv("CITCOM_GPU_NO_PDL");
 		if(q && q[0] && q[0] != '0')
 			g_use_pdl = 0;
@@ -1303,9 +1329,16 @@ int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 			h->BI64[l] = nullptr;
 			h->K32[l] = nullptr;
 			h->BI32[l] = nullptr;
+			h->K32lo = l == lmax ? nullptr : h->K32lo;
+			// the finest FP64 operator of the mixed box: the FP32 stencil plus
+			// its FP32 remainder, applied in double-float (k_tile_split)
+			const bool split = l == lmax && cfg->precision == CITCOM_GPU_MIXED && h->geodf[l] && !L.aos && !h->no_split;
 			if(need64)
 			{
-				TRYC(dalloc(h, &h->K64[l], cg_kwords(L)));
+				if(split)
+					TRYC(dalloc(h, &h->K32lo, cg_kwords(L)));
+				else
+					TRYC(dalloc(h, &h->K64[l], cg_kwords(L)));
 				TRYC(dalloc(h, &h->BI64[l], (size_t)3 * L.npad));
 			}
 			h->Kt32[l] = nullptr;
@@ -1783,7 +1816,7 @@ static int stokes_residuals_impl(citcom_gpu *h, double out[2])
 	const Lvl &Lf = h->lv[lmax];
 	// momentum: F - K U - G P, with the FP64 operator
 	launch_grad(h->st, Lf, h->geo[lmax], h->P, h->Ah);
-	launch_kmul<double>(h->st, Lf, h->K64[lmax], h->U, h->u1);
+	fine_kmul64(h, h->U, h->u1);
 	launch_sub3(h->st, Lf.neq, h->r64, h->F, h->Ah, h->u1);
 	launch_div(h->st, Lf, h->geo[lmax], h->U, h->Eres);
 	launch_dots4(h->st, Lf.neq, h->r64, h->r64, h->F, h->F, h->U, h->U, nullptr, nullptr, red_of(h), h->dscal + S_DOT);
@@ -1832,7 +1865,10 @@ static int op_kmul_impl(citcom_gpu *h, int lev, const double *u, double *Au)
 		du = h->cfg.precision == CITCOM_GPU_FP64 ? h->mg64.del[lev] : h->r64;
 		dA = h->cfg.precision == CITCOM_GPU_FP64 ? h->mg64.AU[lev] : h->Ah;
 		TRY(h2d(h, du, u, sizeof(double) * L.neq));
-		launch_kmul<double>(h->st, L, h->K64[lev], du, dA);
+		if(lev == h->L - 1)
+			fine_kmul64(h, du, dA);
+		else
+			launch_kmul<double>(h->st, L, h->K64[lev], du, dA);
 		TRY(d2h(h, Au, dA, sizeof(double) * L.neq));
 		return sync(h);
 	}

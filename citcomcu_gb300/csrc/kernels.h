@@ -166,9 +166,10 @@ struct GeoDF
 };
 void geo_df_fill(const Geo &g, int aug, double lambda, GeoDF *out);
 // construct_node_ks of a box level in double-float arithmetic: splits evi into
-// eta2 (8 nel float2), then K64 / K32 (either may be null) and BI64 / BI32
+// eta2 (8 nel float2), then K64 / K32 / K32lo (the FP32 remainder entry - K32;
+// any may be null) and BI64 / BI32
 void launch_assemble_df(cudaStream_t st, const Lvl &L, const GeoDF *G, const double *evi, float2 *eta2, int aug,
-                        double *K64, float *K32, double *BI64, float *BI32);
+                        double *K64, float *K32, float *K32lo, double *BI64, float *BI32);
 
 // matrix-free FP32 Gauss-Seidel colour of a box level (mf.cu): eta = the
 // level's Gauss-point viscosity in FP32 (8 per element), BI = 1/diag K in
@@ -176,6 +177,12 @@ void launch_assemble_df(cudaStream_t st, const Lvl &L, const GeoDF *G, const dou
 void launch_mf_eta32(cudaStream_t st, const Lvl &L, const double *evi, float *eta);
 void launch_mf_gs(cudaStream_t st, const Lvl &L, const float *eta, int aug, double lambda, const float *BI, const float *F,
                   float *d, int colour);
+
+// The finest level's FP64 operator as two FP32 stencils K = Kh + Kl (tile
+// layout), applied in double-float arithmetic (tile.cu): out = K u (f null)
+// or out = f - K u; FP64 vectors
+void launch_tile_split(cudaStream_t st, const Lvl &L, const float *Kh, const float *Kl, const double *f, const double *u,
+                       double *out);
 
 int tile_init();                                   // attributes and grid sizes; 0 on success
 int tile_error_async(double *host, cudaStream_t st);  // 1 in *host if a stage wait timed out since the last reset

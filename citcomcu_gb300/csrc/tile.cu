@@ -266,6 +266,183 @@ __global__ void __launch_bounds__(TT, TileCfg<T>::MIN_CTAS) k_tile(Lvl L, const 
 	}
 }
 
+// The finest level's FP64 operator held as two FP32 stencils of the same
+// layout, K = Kh + Kl (Kh the FP32 stencil the smoother uses, Kl the
+// remainder), applied to FP64 vectors in double-float arithmetic: each
+// product (Kh + Kl)(uh + ul) keeps its rounding error (an FMA recovers it)
+// and the sums use Knuth's two-sum, about 46 significant bits per row.  The
+// same bytes as the FP64 stencil, FP32 instructions instead of GB300's slow
+// FP64 ones.  Structure as k_tile: persistent CTAs, nine warps, a stage per
+// tile holding its Kh and Kl words (two bulk copies on one barrier).
+constexpr int SP_STAGES = 2;
+constexpr unsigned SP_BYTES = CG_TILE_WORDS * sizeof(float);
+constexpr size_t SP_SMEM = (size_t)SP_STAGES * 2 * CG_TILE_WORDS * sizeof(float) + 2 * 27 * TB * sizeof(double);
+
+// (sh, sl) += (ah + al) (bh + bl), dropping al bl (two-product and two-sum)
+__device__ __forceinline__ void sp_madd(float &sh, float &sl, float ah, float al, float bh, float bl)
+{
+	const float p = __fmul_rn(ah, bh);
+	const float e = __fmaf_rn(ah, bh, -p);
+	const float pl = __fmaf_rn(ah, bl, __fmaf_rn(al, bh, e));
+	const float t = __fadd_rn(sh, p);
+	const float bp = __fsub_rn(t, sh);
+	const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+	sh = t;
+	sl = __fadd_rn(sl, __fadd_rn(err, pl));
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(TT, 1) k_tile_split(Lvl L, const float *__restrict__ Kh, const float *__restrict__ Kl,
+                                                     const double *__restrict__ f, const double *u, double *out)
+{
+	constexpr int S = SP_STAGES;
+	extern __shared__ __align__(128) unsigned char smem_raw[];
+	float *stage = reinterpret_cast<float *>(smem_raw);  // [stage][hi, lo][CG_TILE_WORDS]
+	double *part = reinterpret_cast<double *>(stage + S * 2 * CG_TILE_WORDS);
+	__shared__ __align__(8) unsigned long long bar[S];
+	const int ntile = L.toff[8];
+	const int nmine = (int)blockIdx.x < ntile ? (ntile - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+	const unsigned bar0 = t_smem(bar), st0 = t_smem(stage);
+	auto issue = [&](int k) {
+		const int b = k % S;
+		const size_t tile = (size_t)blockIdx.x + (size_t)k * gridDim.x;
+		const unsigned bb = bar0 + 8 * b, dst = st0 + b * 2 * SP_BYTES;
+		asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bb), "r"(2 * SP_BYTES) : "memory");
+		asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+		             "l"(Kh + tile * CG_TILE_WORDS), "r"(SP_BYTES), "r"(bb)
+		             : "memory");
+		asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst + SP_BYTES),
+		             "l"(Kl + tile * CG_TILE_WORDS), "r"(SP_BYTES), "r"(bb)
+		             : "memory");
+	};
+	if(threadIdx.x == 0)
+	{
+		for(int b = 0; b < S; ++b)
+			asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar0 + 8 * b) : "memory");
+		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+	}
+	__syncthreads();
+	int issued = 0;
+	if(threadIdx.x == 0)
+		for(; issued < S && issued < nmine; ++issued)
+			issue(issued);
+	// the stencil is written only by the assembly, long before any launch
+	// here; the vectors are read after the wait on the preceding kernel
+	pdl_begin();
+	bool ok = true;
+	const int ln = threadIdx.x & 31, g = threadIdx.x >> 5;
+	const int dx = g % 3 - 1, dy = g / 3 - 1;
+	const int oq = threadIdx.x / 3, oi = threadIdx.x % 3;
+	struct Pre
+	{
+		int cnt, on;
+		double fi;
+		float uh[9], ul[9];  // [dz + 1][component], u = uh + ul
+	};
+	auto prefetch = [&](int k, Pre &q) {
+		q.cnt = 0;
+		if(k >= nmine)
+			return;
+		const int tile = blockIdx.x + k * gridDim.x;
+		int cc = 0;
+#pragma unroll
+		for(int m = 1; m < 8; ++m)
+			cc += (tile >= L.toff[m]);
+		const int q0 = (tile - L.toff[cc]) * TB;
+		q.cnt = min(TB, L.coff[cc + 1] - L.coff[cc] - q0);
+		q.on = 0;
+		q.fi = 0.0;
+		if((int)threadIdx.x < 3 * q.cnt)
+		{
+			int x, y, z;
+			cg_decode(L, cc, q0 + oq, x, y, z);
+			q.on = cg_node(L, x, y, z);
+			if(KIND == TK_RES)
+				q.fi = f[3 * q.on + oi];
+		}
+#pragma unroll
+		for(int e = 0; e < 9; ++e)
+			q.uh[e] = q.ul[e] = 0.f;
+		if(ln < q.cnt)
+		{
+			int x, y, z;
+			cg_decode(L, cc, q0 + ln, x, y, z);
+			const int col = cg_node(L, clampi(x + dx, 0, L.nox - 1), clampi(y + dy, 0, L.noy - 1), 0);
+#pragma unroll
+			for(int kz = 0; kz < 3; ++kz)
+			{
+				// missing neighbours are clamped onto the node: their stencil block is zero
+				const int m = col + clampi(z + kz - 1, 0, L.noz - 1);
+#pragma unroll
+				for(int c = 0; c < 3; ++c)
+				{
+					const double v = u[3 * m + c];
+					const float h = (float)v;
+					q.uh[3 * kz + c] = h;
+					q.ul[3 * kz + c] = (float)(v - (double)h);
+				}
+			}
+		}
+	};
+	Pre cur;
+	prefetch(0, cur);
+	for(int k = 0; k < nmine; ++k)
+	{
+		const int b = k % S;
+		if(ok)
+			ok = t_wait(bar0 + 8 * b, (unsigned)((k / S) & 1));
+		double *pb = part + (k & 1) * 27 * TB;
+		const int cnt = cur.cnt;
+		if(ln < cnt)
+		{
+			const float *kh = stage + (size_t)b * 2 * CG_TILE_WORDS + (9 * g * TB + ln) * 3;
+			const float *kl = kh + CG_TILE_WORDS;
+			float ah[3] = {0.f, 0.f, 0.f}, al[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+			for(int kz = 0; kz < 3; ++kz)
+#pragma unroll
+				for(int j = 0; j < 3; ++j)
+				{
+					const int w = (3 * kz + j) * TB * 3;
+#pragma unroll
+					for(int i = 0; i < 3; ++i)
+						sp_madd(ah[i], al[i], kh[w + i], kl[w + i], cur.uh[3 * kz + j], cur.ul[3 * kz + j]);
+				}
+#pragma unroll
+			for(int i = 0; i < 3; ++i)
+				pb[(g * 3 + i) * TB + ln] = (double)ah[i] + (double)al[i];
+		}
+		const int on = cur.on;
+		const double fi = cur.fi;
+		prefetch(k + 1, cur);
+		__syncthreads();  // stage b read by every thread; partials complete
+		if(threadIdx.x == 0 && ok && issued < nmine)
+		{
+			asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+			issue(issued++);
+		}
+		if((int)threadIdx.x < 3 * cnt)
+		{
+			double r = 0.0;
+#pragma unroll
+			for(int gg = 0; gg < 9; ++gg)
+				r += pb[(gg * 3 + oi) * TB + oq];
+			out[3 * on + oi] = KIND == TK_KU ? r : fi - r;
+		}
+	}
+	if(!ok)
+	{
+		g_tile_err = 1.0;
+		// no copy was issued after the wait that ran out; the earlier ones
+		// land before the CTA leaves
+		if(threadIdx.x == 0)
+			for(int k = max(0, issued - S); k < issued; ++k)
+				t_drain(bar0 + 8 * (k % S), (unsigned)((k / S) & 1));
+	}
+}
+
+int g_split_ctas = 0;
+
 template <typename T> struct TileGrid
 {
 	static int ctas;  // persistent CTAs: SMs x resident CTAs per SM
@@ -321,6 +498,16 @@ int tile_init()
 		return -1;
 	if(tile_init_t<float>(sms) != 0 || tile_init_t<double>(sms) != 0)
 		return -1;
+	int occ = 0;
+	for(auto fn : {k_tile_split<TK_KU>, k_tile_split<TK_RES>})
+	{
+		int o = 0;
+		if(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SP_SMEM) != cudaSuccess ||
+		   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, fn, TT, SP_SMEM) != cudaSuccess || o < 1)
+			return -1;
+		occ = occ ? std::min(occ, o) : o;
+	}
+	g_split_ctas = sms * occ;
 	return 0;
 }
 
@@ -362,3 +549,26 @@ template <typename T> void launch_tile_residual(cudaStream_t st, const Lvl &L, c
 	template void launch_tile_residual<T>(cudaStream_t, const Lvl &, const T *, const T *, const T *, T *);
 TILE_INST(float)
 TILE_INST(double)
+
+void launch_tile_split(cudaStream_t st, const Lvl &L, const float *Kh, const float *Kl, const double *f, const double *u,
+                       double *out)
+{
+	const int ntile = L.toff[8];
+	if(ntile <= 0)
+		return;
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim = dim3(std::min(ntile, std::max(1, g_split_ctas)));
+	cfg.blockDim = dim3(TT);
+	cfg.dynamicSmemBytes = SP_SMEM;
+	cfg.stream = st;
+	cudaLaunchAttribute attr[1];
+	attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+	attr[0].val.programmaticStreamSerializationAllowed = 1;
+	cfg.attrs = attr;
+	cfg.numAttrs = g_use_pdl ? 1 : 0;
+	if(f)
+		cudaLaunchKernelEx(&cfg, k_tile_split<TK_RES>, L, Kh, Kl, f, u, out);
+	else
+		cudaLaunchKernelEx(&cfg, k_tile_split<TK_KU>, L, Kh, Kl, f, u, out);
+	++g_kernel_launches;
+}

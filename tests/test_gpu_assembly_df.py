@@ -64,3 +64,38 @@ def test_double_float_assembly(cg, oracle_lib, aug):
     assert rel(out[1]["BI"], out[0]["BI"]) < 1e-12
     assert rel(out[1]["Kc"], out[0]["Kc"]) < 1e-6
     assert rel(out[1]["BIc"], out[0]["BIc"]) < 1e-6
+
+
+def test_split_fp64_operator(cg):
+    """The mixed box keeps the finest level's FP64 operator as its FP32
+    stencil plus the FP32 remainder and applies it in double-float
+    (k_tile_split): K u against the same operator held in FP64
+    (CITCOM_GPU_NO_SPLIT=1) to 1e-13, and a mixed Stokes solve takes the same
+    iteration counts and reaches the same solution to 1e-10."""
+    from citcomcu_gb300 import Config
+    case = Config(mgunit=(4, 4, 4), levels=3, rayleigh=1e5, tdepv=True, visc0=(1.0,), viscE=(math.log(1e3),),
+                  viscT=(0.0,), accuracy=1e-6, piterations=1000, stop_rule=1)
+    nno = case.nox * case.noy * case.noz
+    rng = np.random.Generator(np.random.PCG64(4))
+    z = np.tile(np.linspace(0.0, 1.0, case.noz), case.nox * case.noy)
+    T = np.clip(1.0 - z + 0.01 * rng.uniform(-1, 1, nno), 0.0, 1.0)
+    out = {}
+    for split in (True, False):
+        if not split:
+            os.environ["CITCOM_GPU_NO_SPLIT"] = "1"
+        try:
+            s = cg.Solver(cg.Config.like(case, precision=cg.MIXED))
+        finally:
+            os.environ.pop("CITCOM_GPU_NO_SPLIT", None)
+        s.get_system_viscosity(T)
+        s.construct_stiffness_B_matrix()
+        u = np.sin(0.37 * np.arange(s.fine["neq"]) + 0.3)
+        Ku = s.op_kmul(case.levels - 1, u)
+        U, P = np.zeros(s.fine["neq"]), np.zeros(s.fine["nel"])
+        s.general_stokes_solver(T, U, P)
+        out[split] = (Ku, U, s.stats())
+        s.close()
+    print(rel(out[True][0], out[False][0]), rel(out[True][1], out[False][1]))
+    assert rel(out[True][0], out[False][0]) < 1e-13
+    assert out[True][2]["uzawa"] == out[False][2]["uzawa"]
+    assert rel(out[True][1], out[False][1]) < 1e-10

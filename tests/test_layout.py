@@ -17,7 +17,8 @@ def test_device_index_arithmetic_on_host():
 # Kernels that start work before their wait on the predecessor, and what that
 # work reads: the tile kernels start the bulk copies of their first stencil
 # tiles (the stencil is written only by the assembly, several kernels earlier).
-EARLY_WORK = {"tile.cu:k_tile": "cp.async.bulk of stencil tiles"}
+EARLY_WORK = {"tile.cu:k_tile": "cp.async.bulk of stencil tiles",
+              "tile.cu:k_tile_split": "cp.async.bulk of stencil tiles (FP32 pair)"}
 
 
 def test_every_kernel_waits_for_its_predecessor():
