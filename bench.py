@@ -328,12 +328,13 @@ def train_warm_start(cg, case, T0_of, seeds: int, steps_per_seed: int, train_ste
             n.record()
     t1 = time.perf_counter()
     losses = [n.train(1, 4, 1e-3)]
-    for _ in range(4):
-        losses.append(n.train(train_steps // 4, 4, 1e-3))
+    for lr, k in ((1e-3, train_steps // 2), (3e-4, train_steps // 4), (1e-4, train_steps // 4)):
+        losses.append(n.train(k, 4, lr))
     t2 = time.perf_counter()
     info = {"snapshots": n.recorded, "seeds": seeds, "steps_per_seed": steps_per_seed, "adam_steps": train_steps,
             "mode": "increment" if mode else "absolute",
-            "batch": 4, "lr": 1e-3, "loss_first": losses[0], "loss_final": losses[-1], "record_s": t1 - t0,
+            "batch": 4, "lr": "1e-3, 3e-4, 1e-4 (1/2, 1/4, 1/4 of the steps)", "loss_first": losses[0],
+            "loss_final": losses[-1], "record_s": t1 - t0,
             "train_s": t2 - t1, "network_grid": list(n.grid), "params": n.n_params}
     return s, n, info
 
@@ -557,11 +558,12 @@ def main():
     ap.add_argument("--no-learned", action="store_true",
                     help="headline without the learned warm start (profiling runs)")
     ap.add_argument("--learn-seeds", type=int, default=10)
-    ap.add_argument("--learn-steps", type=int, default=20, help="time steps recorded after each seed's cold solve")
+    ap.add_argument("--learn-steps", type=int, default=40, help="time steps recorded after each seed's cold solve")
     ap.add_argument("--learn-mode", default="increment", choices=["increment", "absolute"],
                     help="increment: the network predicts the change of U, P over a time step (default); "
                          "absolute: U, P themselves")
-    ap.add_argument("--learn-adam", type=int, default=1000, help="Adam steps of the online training")
+    ap.add_argument("--learn-adam", type=int, default=4000,
+                    help="Adam steps of the online training (half at lr 1e-3, a quarter each at 3e-4 and 1e-4)")
     ap.add_argument("--learn-check", type=int, default=8,
                     help="compare the network's start with the previous step's on every k-th solve (and whenever "
                          "its initial residual grows past 4x the last winning one); 1: every solve")

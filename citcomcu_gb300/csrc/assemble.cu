@@ -147,17 +147,13 @@ __global__ void __launch_bounds__(AS_THREADS) k_assemble_df(Lvl L, const GeoDF *
 			}
 		}
 	}
-	double blk[9];
-#pragma unroll
-	for(int r = 0; r < 9; ++r)
-		blk[r] = (double)bh[r] + (double)bl[r];
 	if(s == 13)
 	{
 		// 1 / diag K from the unmasked diagonal
 #pragma unroll
 		for(int i = 0; i < 3; ++i)
 		{
-			const double bi = 1.0 / blk[4 * i];
+			const double bi = 1.0 / ((double)bh[4 * i] + (double)bl[4 * i]);
 			if(BI64)
 				BI64[3 * (size_t)p + i] = bi;
 			if(BI32)
@@ -172,21 +168,26 @@ __global__ void __launch_bounds__(AS_THREADS) k_assemble_df(Lvl L, const GeoDF *
 #pragma unroll
 			for(int j = 0; j < 3; ++j)
 				if(((fn >> i) & 1u) || ((fm >> j) & 1u))
-					blk[3 * i + j] = 0.0;
+					bh[3 * i + j] = bl[3 * i + j] = 0.f;
 	}
 #pragma unroll
 	for(int i = 0; i < 3; ++i)
 #pragma unroll
 		for(int j = 0; j < 3; ++j)
 		{
+			const int r = 3 * i + j;
 			const size_t off = cg_kidx(L, s, i, j, p);
-			const float hi = (float)blk[3 * i + j];
+			// renormalised pair, in FP32 (two-sum): hi the entry rounded to
+			// FP32, lo the exact remainder
+			const float hi = __fadd_rn(bh[r], bl[r]);
+			const float bp = __fsub_rn(hi, bh[r]);
+			const float lo = __fadd_rn(__fsub_rn(bh[r], __fsub_rn(hi, bp)), __fsub_rn(bl[r], bp));
 			if(K64)
-				K64[off] = blk[3 * i + j];
+				K64[off] = (double)bh[r] + (double)bl[r];
 			if(K32)
 				K32[off] = hi;
 			if(K32lo)
-				K32lo[off] = (float)(blk[3 * i + j] - (double)hi);
+				K32lo[off] = lo;
 		}
 }
 
