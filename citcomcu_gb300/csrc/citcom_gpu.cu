@@ -64,6 +64,7 @@ struct citcom_gpu
 	float *eta32[CITCOM_MAX_LEVELS];  // FP32 Gauss-point viscosity of the levels the matrix-free smoother relaxes, else null
 	GeoDF *geodf[CITCOM_MAX_LEVELS];  // box element kernels as FP32 pairs (mixed configuration), else null
 	float *K32lo;                     // mixed box: the finest FP64 operator's FP32 remainder (K64 = K32 + K32lo), else null
+	float2 *usplit;                   // the vector K32 + K32lo is applied to, as FP32 pairs (neq)
 	bool no_split;                    // CITCOM_GPU_NO_SPLIT: keep the finest FP64 stencil instead
 	float2 *eta2[CITCOM_MAX_LEVELS];  // Gauss-point viscosity as FP32 pairs for the double-float assembly
 	bool fp64_assembly;               // CITCOM_GPU_FP64_ASSEMBLY: the mixed configuration assembles in FP64
@@ -270,7 +271,7 @@ void fine_kmul64(citcom_gpu *h, const double *u, double *out)
 {
 	const int lmax = h->L - 1;
 	if(h->K32lo)
-		launch_tile_split(h->st, h->lv[lmax], h->K32[lmax], h->K32lo, nullptr, u, out);
+		launch_tile_split(h->st, h->lv[lmax], h->K32[lmax], h->K32lo, nullptr, u, h->usplit, out);
 	else
 		launch_kmul<double>(h->st, h->lv[lmax], h->K64[lmax], u, out);
 }
@@ -279,7 +280,7 @@ void fine_residual64(citcom_gpu *h, const double *f, const double *u, double *r)
 {
 	const int lmax = h->L - 1;
 	if(h->K32lo)
-		launch_tile_split(h->st, h->lv[lmax], h->K32[lmax], h->K32lo, f, u, r);
+		launch_tile_split(h->st, h->lv[lmax], h->K32[lmax], h->K32lo, f, u, h->usplit, r);
 	else
 		launch_residual<double>(h->st, h->lv[lmax], h->K64[lmax], f, u, r);
 }
@@ -1336,7 +1337,10 @@ int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 			if(need64)
 			{
 				if(split)
+				{
 					TRYC(dalloc(h, &h->K32lo, cg_kwords(L)));
+					TRYC(dalloc(h, &h->usplit, (size_t)L.neq));
+				}
 				else
 					TRYC(dalloc(h, &h->K64[l], cg_kwords(L)));
 				TRYC(dalloc(h, &h->BI64[l], (size_t)3 * L.npad));

@@ -180,9 +180,9 @@ void launch_mf_gs(cudaStream_t st, const Lvl &L, const float *eta, int aug, doub
 
 // The finest level's FP64 operator as two FP32 stencils K = Kh + Kl (tile
 // layout), applied in double-float arithmetic (tile.cu): out = K u (f null)
-// or out = f - K u; FP64 vectors
+// or out = f - K u; FP64 vectors; uv (neq float2) receives u as FP32 pairs
 void launch_tile_split(cudaStream_t st, const Lvl &L, const float *Kh, const float *Kl, const double *f, const double *u,
-                       double *out);
+                       float2 *uv, double *out);
 
 int tile_init();                                   // attributes and grid sizes; 0 on success
 int tile_error_async(double *host, cudaStream_t st);  // 1 in *host if a stage wait timed out since the last reset

@@ -276,7 +276,7 @@ __global__ void __launch_bounds__(TT, TileCfg<T>::MIN_CTAS) k_tile(Lvl L, const 
 // tile holding its Kh and Kl words (two bulk copies on one barrier).
 constexpr int SP_STAGES = 2;
 constexpr unsigned SP_BYTES = CG_TILE_WORDS * sizeof(float);
-constexpr size_t SP_SMEM = (size_t)SP_STAGES * 2 * CG_TILE_WORDS * sizeof(float) + 2 * 27 * TB * sizeof(double);
+constexpr size_t SP_SMEM = (size_t)SP_STAGES * 2 * CG_TILE_WORDS * sizeof(float) + 2 * 27 * TB * sizeof(float2);
 
 // (sh, sl) += (ah + al) (bh + bl), dropping al bl (two-product and two-sum)
 __device__ __forceinline__ void sp_madd(float &sh, float &sl, float ah, float al, float bh, float bl)
@@ -291,14 +291,28 @@ __device__ __forceinline__ void sp_madd(float &sh, float &sl, float ah, float al
 	sl = __fadd_rn(sl, __fadd_rn(err, pl));
 }
 
+// u (FP64) as FP32 pairs (hi, lo), once per product, so that the stencil
+// kernel below does no FP64 work per neighbour
+__global__ void k_split_vec(int n, const double *__restrict__ u, float2 *__restrict__ uv)
+{
+	pdl_begin();
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i < n)
+	{
+		const double v = u[i];
+		const float h = (float)v;
+		uv[i] = make_float2(h, (float)(v - (double)h));
+	}
+}
+
 template <int KIND>
 __global__ void __launch_bounds__(TT, 1) k_tile_split(Lvl L, const float *__restrict__ Kh, const float *__restrict__ Kl,
-                                                     const double *__restrict__ f, const double *u, double *out)
+                                                     const double *__restrict__ f, const float2 *uv, double *out)
 {
 	constexpr int S = SP_STAGES;
 	extern __shared__ __align__(128) unsigned char smem_raw[];
 	float *stage = reinterpret_cast<float *>(smem_raw);  // [stage][hi, lo][CG_TILE_WORDS]
-	double *part = reinterpret_cast<double *>(stage + S * 2 * CG_TILE_WORDS);
+	float2 *part = reinterpret_cast<float2 *>(stage + S * 2 * CG_TILE_WORDS);  // partial rows as pairs
 	__shared__ __align__(8) unsigned long long bar[S];
 	const int ntile = L.toff[8];
 	const int nmine = (int)blockIdx.x < ntile ? (ntile - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
@@ -376,10 +390,9 @@ __global__ void __launch_bounds__(TT, 1) k_tile_split(Lvl L, const float *__rest
 #pragma unroll
 				for(int c = 0; c < 3; ++c)
 				{
-					const double v = u[3 * m + c];
-					const float h = (float)v;
-					q.uh[3 * kz + c] = h;
-					q.ul[3 * kz + c] = (float)(v - (double)h);
+					const float2 v = uv[3 * m + c];
+					q.uh[3 * kz + c] = v.x;
+					q.ul[3 * kz + c] = v.y;
 				}
 			}
 		}
@@ -391,7 +404,7 @@ __global__ void __launch_bounds__(TT, 1) k_tile_split(Lvl L, const float *__rest
 		const int b = k % S;
 		if(ok)
 			ok = t_wait(bar0 + 8 * b, (unsigned)((k / S) & 1));
-		double *pb = part + (k & 1) * 27 * TB;
+		float2 *pb = part + (k & 1) * 27 * TB;
 		const int cnt = cur.cnt;
 		if(ln < cnt)
 		{
@@ -410,7 +423,7 @@ __global__ void __launch_bounds__(TT, 1) k_tile_split(Lvl L, const float *__rest
 				}
 #pragma unroll
 			for(int i = 0; i < 3; ++i)
-				pb[(g * 3 + i) * TB + ln] = (double)ah[i] + (double)al[i];
+				pb[(g * 3 + i) * TB + ln] = make_float2(ah[i], al[i]);
 		}
 		const int on = cur.on;
 		const double fi = cur.fi;
@@ -423,10 +436,17 @@ __global__ void __launch_bounds__(TT, 1) k_tile_split(Lvl L, const float *__rest
 		}
 		if((int)threadIdx.x < 3 * cnt)
 		{
-			double r = 0.0;
+			// the nine partial rows, in column order, as a pair; one FP64 sum at the end
+			float rh = 0.f, rl = 0.f;
 #pragma unroll
 			for(int gg = 0; gg < 9; ++gg)
-				r += pb[(gg * 3 + oi) * TB + oq];
+			{
+				const float2 v = pb[(gg * 3 + oi) * TB + oq];
+				const float t = __fadd_rn(rh, v.x), bp = __fsub_rn(t, rh);
+				rl = __fadd_rn(rl, __fadd_rn(__fadd_rn(__fsub_rn(rh, __fsub_rn(t, bp)), __fsub_rn(v.x, bp)), v.y));
+				rh = t;
+			}
+			const double r = (double)rh + (double)rl;
 			out[3 * on + oi] = KIND == TK_KU ? r : fi - r;
 		}
 	}
@@ -551,11 +571,24 @@ TILE_INST(float)
 TILE_INST(double)
 
 void launch_tile_split(cudaStream_t st, const Lvl &L, const float *Kh, const float *Kl, const double *f, const double *u,
-                       double *out)
+                       float2 *uv, double *out)
 {
 	const int ntile = L.toff[8];
 	if(ntile <= 0)
 		return;
+	{
+		cudaLaunchConfig_t c = {};
+		c.gridDim = dim3((L.neq + 255) / 256);
+		c.blockDim = dim3(256);
+		c.stream = st;
+		cudaLaunchAttribute a[1];
+		a[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+		a[0].val.programmaticStreamSerializationAllowed = 1;
+		c.attrs = a;
+		c.numAttrs = g_use_pdl ? 1 : 0;
+		cudaLaunchKernelEx(&c, k_split_vec, L.neq, u, uv);
+		++g_kernel_launches;
+	}
 	cudaLaunchConfig_t cfg = {};
 	cfg.gridDim = dim3(std::min(ntile, std::max(1, g_split_ctas)));
 	cfg.blockDim = dim3(TT);
@@ -567,8 +600,8 @@ void launch_tile_split(cudaStream_t st, const Lvl &L, const float *Kh, const flo
 	cfg.attrs = attr;
 	cfg.numAttrs = g_use_pdl ? 1 : 0;
 	if(f)
-		cudaLaunchKernelEx(&cfg, k_tile_split<TK_RES>, L, Kh, Kl, f, u, out);
+		cudaLaunchKernelEx(&cfg, k_tile_split<TK_RES>, L, Kh, Kl, f, (const float2 *)uv, out);
 	else
-		cudaLaunchKernelEx(&cfg, k_tile_split<TK_KU>, L, Kh, Kl, f, u, out);
+		cudaLaunchKernelEx(&cfg, k_tile_split<TK_KU>, L, Kh, Kl, f, (const float2 *)uv, out);
 	++g_kernel_launches;
 }
