@@ -30,7 +30,9 @@ solves of other seeds (training time reported, not timed into `value`).
 `e2e` runs the headline loop through the C ABI with host buffers (pinned):
 PG_timestep and general_stokes_solver per step, the copies inside the timed
 region.  `drift` runs the 64^3 box (mixed vs FP64 plain) for --drift-steps
-steps (200, as configs[1] asks) and reports the per-step Nu / Vrms drift.
+steps (200, that benchmark's run length) and reports the per-step Nu / Vrms
+drift; with --drift-workload equal to --workload it also runs the trained
+learned path against FP64 plain.
 
   python bench.py [--steps K] [--warmup W] [--gpus N] [--impl reference]
                   [--workload cfg2|cube|sphere] [--no-cpu] [--no-learned]
@@ -230,11 +232,12 @@ def rel_p(a, b):
     return rel(a - a.mean(), b - b.mean())
 
 
-def run_loop(cg, case, T0, precision, steps, warmup, solver=None, net=None):
+def run_loop(cg, case, T0, precision, steps, warmup, solver=None, net=None, zero_start=False):
     """The reference's time loop on resident state: one cold solve of the
     seeded state (untimed), then per step PG_timestep and general_stokes_solver
-    warm from the previous step's U, P.  Device time per step (CUDA events
-    inside the library), after `warmup` untimed steps."""
+    warm from the previous step's U, P (zero_start: from U = P = 0 instead).
+    Device time per step (CUDA events inside the library), after `warmup`
+    untimed steps."""
     s = solver or cg.Solver(cg.Config.like(case, precision=precision))
     if net is not None:
         net.attach(True)
@@ -245,9 +248,12 @@ def run_loop(cg, case, T0, precision, steps, warmup, solver=None, net=None):
     t = 0.0
     recs, nus, vrs = [], [], []
     l0 = None
+    zu, zp = np.zeros(f["neq"]), np.zeros(f["nel"])
     for i in range(warmup + steps):
         if i == warmup:
             l0 = s.stats()["kernel_launches"]
+        if zero_start:
+            s.load_state(U=zu, P=zp)
         adv = s.step_resident(t)
         t = adv["elapsed_time"]
         st = s.stats()
@@ -386,28 +392,50 @@ def output_step(s, reps: int = 10):
             "fields": "T, V, P, heatflux, heatflux_adv, Have (T, vrms, Vi, Rho, F, f), shflux, bhflux, Nut, Nub, Vrms"}
 
 
-def drift_run(cg, which, steps):
+def drift_run(cg, which, steps, learned=None, control=False):
     """A workload from its seeded state (`which`: "cube" the 64^3 box, eta =
     exp(-ln(1e3) T), Ra 1e5; "cfg2" the 128x128x64 box): `steps` time steps of
-    the mixed path and of the FP64 plain path; the per-step relative
-    differences of Nu and Vrms (every step, and their maxima) and the final U,
-    P, T."""
+    the mixed path and of the FP64 plain path, of the learned path when
+    `learned` = (solver, trained network) of the same workload is given, and
+    with `control` of the mixed path solving every step from U = P = 0 (the
+    same stopping rule from another start); per path against FP64 plain the
+    per-step relative differences of Nu and Vrms (every step, and their
+    maxima), the Nu differences over the RMS of FP64 plain's Nu over the run,
+    and the final U, P, T."""
     case = cfg2_workload() if which == "cfg2" else workload(64)
     T0 = seeded_T0(case)
-    r = {}
-    for name, prec in (("mixed", cg.MIXED), ("fp64_plain", cg.FP64)):
-        r[name] = run_loop(cg, case, T0, prec, steps, 0)
-    m, p = r["mixed"], r["fp64_plain"]
-    dnu = [abs(a - b) / abs(b) for a, b in zip(m["nu"], p["nu"])]
-    dvr = [abs(a - b) / abs(b) for a, b in zip(m["vrms"], p["vrms"])]
-    return {"workload": workload_name(case), "steps": steps,
-            "nu_rel_drift_per_step": dnu, "vrms_rel_drift_per_step": dvr,
-            "nu_rel_drift_max": max(dnu), "vrms_rel_drift_max": max(dvr),
-            "final_errors": {"U": rel(m["state"]["U"], p["state"]["U"]), "P": rel_p(m["state"]["P"], p["state"]["P"]),
-                             "T": rel(m["state"]["T"], p["state"]["T"])},
-            "stokes_ms_per_step": {"mixed": loop_summary(m)["stokes_ms_per_step"],
-                                   "fp64_plain": loop_summary(p)["stokes_ms_per_step"]},
-            "nu_top_final": {"mixed": m["nu"][-1], "fp64_plain": p["nu"][-1]}}
+    r = {"fp64_plain": run_loop(cg, case, T0, cg.FP64, steps, 0), "mixed": run_loop(cg, case, T0, cg.MIXED, steps, 0)}
+    if learned is not None:
+        r["learned"] = run_loop(cg, case, T0, cg.MIXED, steps, 0, solver=learned[0], net=learned[1])
+    if control:
+        r["zero_start"] = run_loop(cg, case, T0, cg.MIXED, steps, 0, zero_start=True)
+    p = r["fp64_plain"]
+    nu_scale = float(np.sqrt(np.mean(np.square(p["nu"]))))
+
+    def against_fp64(m):
+        dnu = [abs(a - b) / abs(b) for a, b in zip(m["nu"], p["nu"])]
+        dvr = [abs(a - b) / abs(b) for a, b in zip(m["vrms"], p["vrms"])]
+        dnus = [abs(a - b) / nu_scale for a, b in zip(m["nu"], p["nu"])]
+        return {"nu_rel_drift_per_step": dnu, "vrms_rel_drift_per_step": dvr,
+                "nu_rel_drift_max": max(dnu), "vrms_rel_drift_max": max(dvr),
+                "nu_drift_over_rms_per_step": dnus, "nu_drift_over_rms_max": max(dnus),
+                "final_errors": {"U": rel(m["state"]["U"], p["state"]["U"]),
+                                 "P": rel_p(m["state"]["P"], p["state"]["P"]),
+                                 "T": rel(m["state"]["T"], p["state"]["T"])}}
+
+    out = {"workload": workload_name(case), "steps": steps, "fp64_nu_per_step": p["nu"],
+           "fp64_vrms_per_step": p["vrms"], "fp64_nu_rms": nu_scale}
+    out.update(against_fp64(r["mixed"]))
+    out["stokes_ms_per_step"] = {k: loop_summary(v)["stokes_ms_per_step"] for k, v in r.items()}
+    out["nu_top_final"] = {k: v["nu"][-1] for k, v in r.items()}
+    out["uzawa_iterations_total"] = {k: int(sum(x["uzawa"] for x in v["recs"])) for k, v in r.items()}
+    if learned is not None:
+        lr = r["learned"]
+        out["learned"] = against_fp64(lr)
+        out["learned"]["warm_start_used"] = int(sum(x["warm_start"] for x in lr["recs"]))
+    if control:
+        out["zero_start"] = against_fp64(r["zero_start"])
+    return out
 
 
 # --------------------------------------------------------------- CPU side
@@ -569,8 +597,10 @@ def main():
                          "its initial residual grows past 4x the last winning one); 1: every solve")
     ap.add_argument("--cold-reps", type=int, default=2, help="cold solves per mode (0: skip)")
     ap.add_argument("--drift-steps", type=int, default=200, help="time steps of the drift run (0: skip)")
+    ap.add_argument("--drift-control", action="store_true",
+                    help="drift run: also the mixed path solving every step from U = P = 0")
     ap.add_argument("--drift-workload", default="cube", choices=["cube", "cfg2"],
-                    help="drift run: the 64^3 box (configs[1], 200 steps by default) or the 128x128x64 box")
+                    help="drift run: the 64^3 box (200 steps by default) or the 128x128x64 box")
     ap.add_argument("--ref-full-steps", type=int, default=2,
                     help="reference arm: complete time steps timed in full after the cold solve")
     args = ap.parse_args()
@@ -707,11 +737,13 @@ def main():
         line["output_step"] = output_step(es)
         if es is not ls:
             es.close()
+    if args.drift_steps > 0 and args.workload != "sphere":
+        same = ls is not None and args.drift_workload == args.workload
+        line["drift"] = drift_run(cg, args.drift_workload, args.drift_steps, (ls, ln) if same else None,
+                                  control=args.drift_control)
     if ln is not None:
         ln.close()
         ls.close()
-    if args.drift_steps > 0 and args.workload != "sphere":
-        line["drift"] = drift_run(cg, args.drift_workload, args.drift_steps)
     if not args.no_cpu and case.sphere is None:  # the oracle has no spherical geometry
         pps = float(np.mean([r["mg_passes"] for r in (fp64 or mixed)["recs"]]))
         line["cpu_baseline"] = cpu_sample(case, T0, pps)

@@ -93,6 +93,7 @@ struct citcom_gpu
 	bool stiffness_ready;
 	bool visc_ready;
 	bool verbose;
+	double last_r0;  // the start residual of the last solve_del2_u (RMS per equation)
 	bool no_graph;
 	bool level_timing;            // CITCOM_GPU_LEVEL_TIMING: time every smoother call (no graph)
 	bool no_tiny;                 // CITCOM_GPU_NO_TINY: coarsest FP32 levels use k_gs_small instead of k_gs_tiny
@@ -653,6 +654,7 @@ int solve_del2_u(citcom_gpu *h, double acc, int *valid)
 	launch_dot(h->st, neq, r, r, red_of(h), h->dscal + S_RES);
 	TRY(readback(h, S_RES, 2));
 	const double r0 = std::sqrt(h->hscal[S_RES] / neq);
+	h->last_r0 = r0;
 	double residual = r0;
 	if(r0 * h->cfg.accuracy > acc)
 		acc = r0 * h->cfg.accuracy;
@@ -719,7 +721,11 @@ int uzawa_start(citcom_gpu *h, double *V, const double *P, const double *F, doub
 	fine_kmul64(h, V, h->u1);
 	launch_sub3(st, Lf.neq, h->Ah, F, h->Ah, h->u1);
 	launch_strip(st, Lf, h->Ah);
+	const int passes0 = h->stats.mg_passes;
 	TRY(solve_del2_u(h, acc, &valid));
+	if(h->verbose)
+		fprintf(stderr, "AhatP head: |F - GP - KV| %9.3e, %d multigrid passes to %9.3e\n", h->last_r0,
+		        h->stats.mg_passes - passes0, acc);
 	launch_strip(st, Lf, h->u1);
 	launch_axpby(st, Lf.neq, V, 1.0, h->u1, 1.0);
 	launch_div(st, Lf, geo, V, r1);
@@ -865,6 +871,8 @@ int uzawa(citcom_gpu *h, double *V, double *P, const double *F, double imp, int 
 				const double mom = std::sqrt(rr / (ff > 0.0 ? ff : 1.0));
 				h->stats.final_momentum = mom;
 				h->stats.final_continuity = cont;
+				if(h->verbose)
+					fprintf(stderr, "AhatP check after %d iterations: continuity %9.3e momentum %9.3e\n", count, cont, mom);
 				if(mom <= imp || h->stats.corrections >= 8)
 					break;
 				// velocity correction to half the tolerance, then B V afresh
