@@ -232,6 +232,21 @@ def rel_p(a, b):
     return rel(a - a.mean(), b - b.mean())
 
 
+def nvtx_range(push: bool, pop: bool = False, name: str = "timed_step"):
+    """Marks each timed step as an NVTX range, so that a kernel profiler can
+    capture exactly those launches (ncu --nvtx --nvtx-include timed_step/)."""
+    if not (push or pop):
+        return
+    try:
+        import torch
+        if push:
+            torch.cuda.nvtx.range_push(name)
+        else:
+            torch.cuda.nvtx.range_pop()
+    except Exception:
+        pass
+
+
 def run_loop(cg, case, T0, precision, steps, warmup, solver=None, net=None, zero_start=False):
     """The reference's time loop on resident state: one cold solve of the
     seeded state (untimed), then per step PG_timestep and general_stokes_solver
@@ -254,7 +269,9 @@ def run_loop(cg, case, T0, precision, steps, warmup, solver=None, net=None, zero
             l0 = s.stats()["kernel_launches"]
         if zero_start:
             s.load_state(U=zu, P=zp)
+        nvtx_range(i >= warmup)
         adv = s.step_resident(t)
+        nvtx_range(False, i >= warmup)
         t = adv["elapsed_time"]
         st = s.stats()
         if i >= warmup:

@@ -257,6 +257,40 @@ void make_level(const citcom_gpu_config &c, int l, Lvl &L)
 	L.J = L.h[0] * L.h[1] * L.h[2] / 8.0;
 }
 
+// L2 residency of the tile-major stencils (level.h: l2hint, l2keep).  A
+// colour sweep streams its slice of the stencil once, so plain LRU keeps
+// nothing of a level larger than the L2 from one sweep to the next.  The
+// finest level is read a few times per pass and streams with evict_first;
+// the coarser tile-major levels, smoothed many times per pass, keep a share
+// with evict_last, from the coarsest up, until CITCOM_GPU_L2KEEP_MB (default
+// 64 MB of the 129 MB L2; the rest holds the vectors) is spent.
+// CITCOM_GPU_L2HINT=0 issues the copies without hints.
+void set_l2_policy(citcom_gpu *h)
+{
+	const char *e = getenv("CITCOM_GPU_L2HINT");
+	const bool on = !(e && e[0] == '0');
+	const char *m = getenv("CITCOM_GPU_L2KEEP_MB");
+	double budget = 1e6 * ((m && m[0]) ? atof(m) : 64.0);
+	const int lmax = h->L - 1;
+	const double word = h->cfg.precision == CITCOM_GPU_FP64 ? 8.0 : 4.0;
+	for(int l = 0; l <= lmax; ++l)
+	{
+		Lvl &L = h->lv[l];
+		L.l2hint = 0;
+		L.l2keep = 0;
+		// small levels and those of the cluster program are not tile-streamed
+		if(!on || L.aos || l <= h->co_LC)
+			continue;
+		L.l2hint = 1;
+		if(l == lmax)
+			continue;
+		const double bytes = word * (double)cg_kwords(L);
+		const double frac = std::min(1.0, std::max(0.0, budget / bytes));
+		L.l2keep = (int)(1000.0 * frac);
+		budget -= frac * bytes;
+	}
+}
+
 Red red_of(citcom_gpu *h) { return h->red; }
 
 int readback(citcom_gpu *h, int slot, int n)
@@ -1294,6 +1328,7 @@ int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 			cudaGetLastError();
 			h->co_prog.n = 0;
 		}
+		set_l2_policy(h);
 		for(int l = 0; l < h->L; ++l)
 		{
 			const Lvl &L = h->lv[l];

@@ -28,6 +28,12 @@ struct Lvl
 	double J;        // Jacobian determinant hx*hy*hz/8 (box only)
 	int sphere;      // 1: regional spherical shell segment, x, y, z = theta, phi, r (Geometry=Rsphere)
 	double org[3];   // coordinates of node (0, 0, 0): 0, 0, 0 in the box; theta_north, phi_west (radians), r_inner
+	// L2 residency of the tile-major stencil (tile.cu): with l2hint set, the
+	// bulk copies of the first l2keep per mille of each colour's tiles carry
+	// the evict_last priority and the others evict_first, so that the share
+	// of a level that fits in L2 stays there across its sweeps while the
+	// rest streams through without displacing it; l2hint 0: no hint
+	int l2hint, l2keep;
 };
 
 

@@ -57,6 +57,42 @@ __device__ __forceinline__ void t_issue(unsigned bar, unsigned dst, const void *
 	             : "memory");
 }
 
+// the same copy with an L2 eviction priority (a createpolicy word)
+__device__ __forceinline__ void t_issue_hint(unsigned bar, unsigned dst, const void *src, unsigned bytes,
+                                             unsigned long long pol)
+{
+	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+	asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(dst),
+	             "l"(src), "r"(bytes), "r"(bar), "l"(pol)
+	             : "memory");
+}
+
+__device__ __forceinline__ unsigned long long t_policy_last()
+{
+	unsigned long long p;
+	asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+	return p;
+}
+
+__device__ __forceinline__ unsigned long long t_policy_first()
+{
+	unsigned long long p;
+	asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+	return p;
+}
+
+// the L2 priority of the stencil copy of `tile` (level.h: l2hint, l2keep)
+__device__ __forceinline__ unsigned long long t_tile_policy(const Lvl &L, int tile, unsigned long long last,
+                                                            unsigned long long first)
+{
+	int c = 0;
+#pragma unroll
+	for(int m = 1; m < 8; ++m)
+		c += (tile >= L.toff[m]);
+	const int n = L.toff[c + 1] - L.toff[c];
+	return 1000LL * (tile - L.toff[c]) < (long long)L.l2keep * n ? last : first;
+}
+
 // bounded wait (about a second at most) for the phase of `bar` with this parity
 __device__ __forceinline__ bool t_wait(unsigned bar, unsigned parity)
 {
@@ -106,10 +142,20 @@ __global__ void __launch_bounds__(TT, TileCfg<T>::MIN_CTAS) k_tile(Lvl L, const 
 	const int ntile = t1 - t0;
 	const int nmine = (int)blockIdx.x < ntile ? (ntile - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
 	const unsigned bar0 = t_smem(bar), st0 = t_smem(stage);
+	unsigned long long pol_last = 0, pol_first = 0;
+	if(L.l2hint && threadIdx.x == 0)
+	{
+		pol_last = t_policy_last();
+		pol_first = t_policy_first();
+	}
 	auto issue = [&](int k) {
 		const int b = k % S;
 		const size_t tile = (size_t)t0 + blockIdx.x + (size_t)k * gridDim.x;
-		t_issue(bar0 + 8 * b, st0 + b * TileCfg<T>::BYTES, K + tile * CG_TILE_WORDS, TileCfg<T>::BYTES);
+		if(L.l2hint)
+			t_issue_hint(bar0 + 8 * b, st0 + b * TileCfg<T>::BYTES, K + tile * CG_TILE_WORDS, TileCfg<T>::BYTES,
+			             t_tile_policy(L, (int)tile, pol_last, pol_first));
+		else
+			t_issue(bar0 + 8 * b, st0 + b * TileCfg<T>::BYTES, K + tile * CG_TILE_WORDS, TileCfg<T>::BYTES);
 	};
 	if(threadIdx.x == 0)
 	{
@@ -317,11 +363,28 @@ __global__ void __launch_bounds__(TT, 1) k_tile_split(Lvl L, const float *__rest
 	const int ntile = L.toff[8];
 	const int nmine = (int)blockIdx.x < ntile ? (ntile - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
 	const unsigned bar0 = t_smem(bar), st0 = t_smem(stage);
+	unsigned long long pol_last = 0, pol_first = 0;
+	if(L.l2hint && threadIdx.x == 0)
+	{
+		pol_last = t_policy_last();
+		pol_first = t_policy_first();
+	}
 	auto issue = [&](int k) {
 		const int b = k % S;
 		const size_t tile = (size_t)blockIdx.x + (size_t)k * gridDim.x;
 		const unsigned bb = bar0 + 8 * b, dst = st0 + b * 2 * SP_BYTES;
 		asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bb), "r"(2 * SP_BYTES) : "memory");
+		if(L.l2hint)
+		{
+			const unsigned long long pol = t_tile_policy(L, (int)tile, pol_last, pol_first);
+			asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(dst),
+			             "l"(Kh + tile * CG_TILE_WORDS), "r"(SP_BYTES), "r"(bb), "l"(pol)
+			             : "memory");
+			asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(dst + SP_BYTES),
+			             "l"(Kl + tile * CG_TILE_WORDS), "r"(SP_BYTES), "r"(bb), "l"(pol)
+			             : "memory");
+			return;
+		}
 		asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
 		             "l"(Kh + tile * CG_TILE_WORDS), "r"(SP_BYTES), "r"(bb)
 		             : "memory");
