@@ -233,8 +233,10 @@ def rel_p(a, b):
 
 
 def nvtx_range(push: bool, pop: bool = False, name: str = "timed_step"):
-    """Marks each timed step as an NVTX range, so that a kernel profiler can
-    capture exactly those launches (ncu --nvtx --nvtx-include timed_step/)."""
+    """Marks each timed step as an NVTX range (timed_learned, timed_mixed,
+    timed_fp64, ...), so that a kernel profiler can capture exactly the
+    launches of one mode's timed steps (ncu --nvtx --nvtx-include
+    timed_learned/)."""
     if not (push or pop):
         return
     try:
@@ -247,7 +249,7 @@ def nvtx_range(push: bool, pop: bool = False, name: str = "timed_step"):
         pass
 
 
-def run_loop(cg, case, T0, precision, steps, warmup, solver=None, net=None, zero_start=False):
+def run_loop(cg, case, T0, precision, steps, warmup, solver=None, net=None, zero_start=False, tag="step"):
     """The reference's time loop on resident state: one cold solve of the
     seeded state (untimed), then per step PG_timestep and general_stokes_solver
     warm from the previous step's U, P (zero_start: from U = P = 0 instead).
@@ -269,7 +271,7 @@ def run_loop(cg, case, T0, precision, steps, warmup, solver=None, net=None, zero
             l0 = s.stats()["kernel_launches"]
         if zero_start:
             s.load_state(U=zu, P=zp)
-        nvtx_range(i >= warmup)
+        nvtx_range(i >= warmup, name=f"timed_{tag}")
         adv = s.step_resident(t)
         nvtx_range(False, i >= warmup)
         t = adv["elapsed_time"]
@@ -657,9 +659,9 @@ def main():
         t0 = time.perf_counter()
         if ls is not None:
             ln.set_check_interval(args.learn_check)
-            learned = run_loop(cg, case, T0, cg.MIXED, args.steps, args.warmup, solver=ls, net=ln)
-        mixed = run_loop(cg, case, T0, cg.MIXED, args.steps, args.warmup)
-        fp64 = run_loop(cg, case, T0, cg.FP64, args.steps, args.warmup) if args.modes == "all" else None
+            learned = run_loop(cg, case, T0, cg.MIXED, args.steps, args.warmup, solver=ls, net=ln, tag="learned")
+        mixed = run_loop(cg, case, T0, cg.MIXED, args.steps, args.warmup, tag="mixed")
+        fp64 = run_loop(cg, case, T0, cg.FP64, args.steps, args.warmup, tag="fp64") if args.modes == "all" else None
         t1 = time.perf_counter()
     barrier()
 
@@ -728,7 +730,7 @@ def main():
         # the same loop comparing the two starts on every solve (the fallback
         # decided afresh each step, at the price of a second head per step)
         ln.set_check_interval(1)
-        strict = run_loop(cg, case, T0, cg.MIXED, args.steps, args.warmup, solver=ls, net=ln)
+        strict = run_loop(cg, case, T0, cg.MIXED, args.steps, args.warmup, solver=ls, net=ln, tag="learned_every")
         ln.set_check_interval(args.learn_check)
         d = loop_summary(strict, ref)
         d["speedup_vs_mixed"] = line["mixed"]["stokes_ms_per_step"] / d["stokes_ms_per_step"]

@@ -368,33 +368,63 @@ __global__ void __launch_bounds__(SLOT_THREADS) k_kmul(Lvl L, const T *__restric
 
 // a.b and a.a in FP64 (a = AU, b = res for the line search of multi_grid,
 // General_matrix_functions.c:626-630): out2[0] = a.b, out2[1] = a.a
+// FP32 vectors: each thread sums its products in FP32 over runs of 8 of its
+// elements and adds each run's sums in FP64.  Converting and accumulating
+// every element in FP64 would make GB300's FP64 pipe, not HBM, the bound
+// (four FP64 operations per element: about 20 us on the finest level).
 template <typename T>
 __global__ void k_dot2(int n, const T *__restrict__ a, const T *__restrict__ b, Red red, double *out2)
 {
 	pdl_begin();
 	double v[2] = {0.0, 0.0};
-	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+	const int stride = gridDim.x * blockDim.x;
+	if constexpr(sizeof(T) == 4)
 	{
-		const double x = a[i];
-		v[0] += x * (double)b[i];
-		v[1] += x * x;
+		int i = blockIdx.x * blockDim.x + threadIdx.x;
+		while(i < n)
+		{
+			float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+			for(int k = 0; k < 8; ++k, i += stride)
+				if(i < n)
+				{
+					const float x = a[i];
+					s0 = fmaf(x, b[i], s0);
+					s1 = fmaf(x, x, s1);
+				}
+			v[0] += (double)s0;
+			v[1] += (double)s1;
+		}
 	}
+	else
+		for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+		{
+			const double x = a[i];
+			v[0] += x * (double)b[i];
+			v[1] += x * x;
+		}
 	block_reduce_store<2>(v, red, out2);
 }
 
-// vel += alpha del ; res -= alpha AU (finest level only); alpha = num/den
+// vel += alpha del ; res -= alpha AU (finest level only); alpha = num/den,
+// formed once per block (an FP64 division per element would cost more than
+// the kernel's memory traffic on GB300) and applied in the vectors' precision
 template <typename T>
 __global__ void k_vel_update(int n, T *__restrict__ vel, const T *__restrict__ del, T *__restrict__ res, const T *__restrict__ AU,
                              const double *__restrict__ nd, int update_res)
 {
 	pdl_begin();
+	__shared__ double s_alpha;
+	if(threadIdx.x == 0)
+		s_alpha = nd[0] / nd[1];
+	__syncthreads();
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i >= n)
 		return;
-	const double alpha = nd[0] / nd[1];
-	vel[i] += (T)(alpha * (double)del[i]);
+	const T alpha = (T)s_alpha;
+	vel[i] += alpha * del[i];
 	if(update_res)
-		res[i] -= (T)(alpha * (double)AU[i]);
+		res[i] -= alpha * AU[i];
 }
 
 // One Gauss-Seidel colour: d_n += (F_n - sum_m K_{n,m} d_m) o BI_n.  The three
@@ -1273,6 +1303,56 @@ __global__ void k_forces(Lvl L, const Geo *__restrict__ geo, const double *__res
 	F[3 * n + 2] = (f & 4u) ? 0.0 : fn[2];
 }
 
+// The same forces for the box.  There the force is vertical and an element
+// contributes J sum_k N_ka N_kb b_b to node a: its consistent mass matrix,
+// which for 2x2x2 Gauss points is the tensor product of the 1D matrix
+// [[c0, c1], [c1, c0]], c0 = P^2 + Q^2 = 2/3, c1 = 2 P Q = 1/3 (P, Q the 1D
+// shape function values at the Gauss points).  Summed over the elements
+// around a node it stays a product of 1D weights: (c1, 2 c0, c1) inside,
+// (c0, c1) at a wall.  27 FMA per node instead of about a thousand.
+__global__ void k_forces_box(Lvl L, const Geo *__restrict__ geo, const double *__restrict__ buoy, double *__restrict__ F)
+{
+	pdl_begin();
+	const int n = blockIdx.x * blockDim.x + threadIdx.x;
+	if(n >= L.nno)
+		return;
+	const int z = n % L.noz, x = (n / L.noz) % L.nox, y = n / (L.noz * L.nox);
+	constexpr double P = 0.5 * (1.0 + 0.57735026918962576451), Q = 0.5 * (1.0 - 0.57735026918962576451);
+	const double c0 = P * P + Q * Q, c1 = 2.0 * P * Q;
+	auto w1 = [&](int i, int ni, int d) {
+		// 1D weight of neighbour offset d (-1, 0, 1) at index i of ni
+		if(d < 0)
+			return i > 0 ? c1 : 0.0;
+		if(d > 0)
+			return i < ni - 1 ? c1 : 0.0;
+		return (i > 0 ? c0 : 0.0) + (i < ni - 1 ? c0 : 0.0);
+	};
+	double s = 0.0;
+	for(int dy = -1; dy <= 1; ++dy)
+	{
+		const double wy = w1(y, L.noy, dy);
+		if(wy == 0.0)
+			continue;
+		for(int dx = -1; dx <= 1; ++dx)
+		{
+			const double wxy = wy * w1(x, L.nox, dx);
+			if(wxy == 0.0)
+				continue;
+			const int col = cg_node(L, x + dx, y + dy, 0);
+			for(int dz = -1; dz <= 1; ++dz)
+			{
+				const double wz = w1(z, L.noz, dz);
+				if(wz != 0.0)
+					s += wxy * wz * buoy[col + z + dz];
+			}
+		}
+	}
+	const unsigned f = cg_vflag(L, x, y, z);
+	F[3 * n] = 0.0;
+	F[3 * n + 1] = 0.0;
+	F[3 * n + 2] = (f & 4u) ? 0.0 : geo->gda[0] * s;
+}
+
 // v_from_vector (Stokes_flow_Incomp.c:530-553): V[d*nno + n]; constrained dofs take VB = 0
 __global__ void k_v_from_vector(Lvl L, const double *__restrict__ U, double *__restrict__ V)
 {
@@ -1363,6 +1443,180 @@ __global__ void k_pg_residual(Lvl L, const Geo *__restrict__ geo, const double *
 #pragma unroll
 	for(int a = 0; a < 8; ++a)
 		Eres[8 * (size_t)e + a] = er[a];
+}
+
+// The same residual for the box, sum-factorised.  A box element's shape
+// functions are products of 1D factors, (1 + s xi)/2 along each axis: P =
+// (1 + beta)/2 where the Gauss point (xi = +-beta) and the node (s = +-1) lie
+// on the same side, Q = (1 - beta)/2 otherwise, and dN/dx_d has +-1/h_d in
+// place of the factor along d.  So
+//  * values at the 2x2x2 Gauss points are three passes of 1D interpolation
+//    (ip3), and the test sum over the Gauss points against N_a is the same
+//    operator (the 1D factor matrix is symmetric);
+//  * the derivative along d is the difference of the two d-faces, bilinearly
+//    interpolated to the other two axes' Gauss points: the same at both Gauss
+//    points along d;
+//  * the test against dN_a/dx_d sums the Gauss points along d first.
+// With jk = |J| w constant, er[a] = -jk (sum_k N_ka A_k + sum_d sum_k
+// dN_a/dx_d(k) B_kd), A_k = dT - Q0 + v.grad T (the advection residual),
+// B_kd = adiff A_k v_d + diff dT/dx_d (the upwind and diffusion fluxes).
+// About 550 FP64 operations per element instead of about 1,750: the kernel
+// is bound by GB300's FP64 rate.  Index q = x + 2 y + 4 z of the element's
+// nodes and Gauss points.
+namespace pgbox {
+constexpr double P = 0.5 * (1.0 + 0.57735026918962576451), Q = 0.5 * (1.0 - 0.57735026918962576451);
+
+// f at the Gauss points (in place): 1D passes along x, y, z
+__device__ __forceinline__ void ip3(double f[8])
+{
+#pragma unroll
+	for(int s = 1; s <= 4; s <<= 1)
+#pragma unroll
+		for(int q = 0; q < 8; ++q)
+			if(!(q & s))
+			{
+				const double a = f[q], b = f[q + s];
+				f[q] = P * a + Q * b;
+				f[q + s] = Q * a + P * b;
+			}
+}
+
+// 2x2 bilinear pass (in place), stride s1 then s2 within a 4-array
+__device__ __forceinline__ void ip2(double g[4])
+{
+#pragma unroll
+	for(int s = 1; s <= 2; s <<= 1)
+#pragma unroll
+		for(int q = 0; q < 4; ++q)
+			if(!(q & s))
+			{
+				const double a = g[q], b = g[q + s];
+				g[q] = P * a + Q * b;
+				g[q + s] = Q * a + P * b;
+			}
+}
+
+// the two axes other than d, in increasing order, and their strides in q
+__device__ __forceinline__ int q_of(int d, int lo, int hi, int side)
+{
+	// node/Gauss point with coordinate `side` along d, lo along the lower
+	// other axis, hi along the higher one
+	const int a1 = d == 0 ? 1 : 0, a2 = d == 2 ? 1 : 2;
+	return (side << d) | (lo << a1) | (hi << a2);
+}
+} // namespace pgbox
+
+__global__ void __launch_bounds__(128) k_pg_residual_box(Lvl L, const Geo *__restrict__ geo, const double *__restrict__ T,
+                                                         const double *__restrict__ Tdot, const double *__restrict__ V,
+                                                         double Q0, double *__restrict__ Eres)
+{
+	pdl_begin();
+	using namespace pgbox;
+	const int e = blockIdx.x * blockDim.x + threadIdx.x;
+	if(e >= L.nel)
+		return;
+	const int ez = e % L.elz, ex = (e / L.elz) % L.elx, ey = e / (L.elz * L.elx);
+	const Geo *G = geo;
+	const double diff = 1.0, twodiff = 2.0 * diff;
+	const double jk = G->gda[0];
+	const double ih[3] = {1.0 / L.h[0], 1.0 / L.h[1], 1.0 / L.h[2]};
+	const int n0 = cg_node(L, ex, ey, ez);
+	const int sx = L.noz, sy = L.noz * L.nox;  // node strides along x and y (z: 1)
+	auto node = [&](int q) { return n0 + (q & 1) * sx + ((q >> 1) & 1) * sy + ((q >> 2) & 1); };
+	// grad T at the Gauss points: gt[d][lo + 2 hi] (the same at both Gauss points along d)
+	double gt[3][4];
+	{
+		double tn[8];
+#pragma unroll
+		for(int q = 0; q < 8; ++q)
+			tn[q] = T[node(q)];
+#pragma unroll
+		for(int d = 0; d < 3; ++d)
+		{
+#pragma unroll
+			for(int m = 0; m < 4; ++m)
+				gt[d][m] = (tn[q_of(d, m & 1, m >> 1, 1)] - tn[q_of(d, m & 1, m >> 1, 0)]) * ih[d];
+			ip2(gt[d]);
+		}
+	}
+	// dT/dt at the Gauss points (fixed-temperature nodes contribute 0)
+	double dt[8];
+#pragma unroll
+	for(int q = 0; q < 8; ++q)
+	{
+		const int n = node(q);
+		dt[q] = t_dirichlet(L, n) ? 0.0 : Tdot[n];
+	}
+	ip3(dt);
+	// velocity at the nodes, its element mean (the upwind parameter), then at the Gauss points
+	double vk[3][8];
+#pragma unroll
+	for(int q = 0; q < 8; ++q)
+	{
+		const int n = node(q);
+		vk[0][q] = V[n];
+		vk[1][q] = V[(size_t)L.nno + n];
+		vk[2][q] = V[2 * (size_t)L.nno + n];
+	}
+	double uc[3];
+#pragma unroll
+	for(int d = 0; d < 3; ++d)
+	{
+		double s = 0.0;
+#pragma unroll
+		for(int q = 0; q < 8; ++q)
+			s += vk[d][q];
+		uc[d] = 0.125 * s;
+	}
+	double us[3], up[3];
+#pragma unroll
+	for(int d = 0; d < 3; ++d)
+	{
+		us[d] = fabs(uc[d] * G->size[d]);
+		up[d] = (us[d] > twodiff) ? (1.0 - twodiff / us[d]) : 0.0;
+	}
+	const double unorm = uc[0] * uc[0] + uc[1] * uc[1] + uc[2] * uc[2];
+	const double adiff = (unorm > 0.000001) ? ((us[0] * up[0] + us[1] * up[1] + us[2] * up[2]) / (2.0 * unorm)) : 0.0;
+#pragma unroll
+	for(int d = 0; d < 3; ++d)
+		ip3(vk[d]);
+	// A_k in dt (in place); the fluxes B_kd summed over the Gauss points along d: sb[d][lo + 2 hi]
+	double sb[3][4];
+#pragma unroll
+	for(int d = 0; d < 3; ++d)
+#pragma unroll
+		for(int m = 0; m < 4; ++m)
+			sb[d][m] = 0.0;
+#pragma unroll
+	for(int q = 0; q < 8; ++q)
+	{
+		const int x = q & 1, y = (q >> 1) & 1, z = q >> 2;
+		const double gx = gt[0][y + 2 * z], gy = gt[1][x + 2 * z], gz = gt[2][x + 2 * y];
+		const double A = dt[q] - Q0 + vk[0][q] * gx + vk[1][q] * gy + vk[2][q] * gz;
+		dt[q] = A;
+		const double aa = adiff * A;
+		sb[0][y + 2 * z] += aa * vk[0][q] + diff * gx;
+		sb[1][x + 2 * z] += aa * vk[1][q] + diff * gy;
+		sb[2][x + 2 * y] += aa * vk[2][q] + diff * gz;
+	}
+	ip3(dt);  // sum_k N_ka A_k at the nodes
+#pragma unroll
+	for(int d = 0; d < 3; ++d)
+		ip2(sb[d]);
+	double er[8];
+#pragma unroll
+	for(int q = 0; q < 8; ++q)
+	{
+		const int x = q & 1, y = (q >> 1) & 1, z = q >> 2;
+		const double fx = x ? sb[0][y + 2 * z] : -sb[0][y + 2 * z];
+		const double fy = y ? sb[1][x + 2 * z] : -sb[1][x + 2 * z];
+		const double fz = z ? sb[2][x + 2 * y] : -sb[2][x + 2 * y];
+		er[q] = -jk * (dt[q] + fx * ih[0] + fy * ih[1] + fz * ih[2]);
+	}
+	// element-local node order a (cg_loc) of the residual vector
+#pragma unroll
+	for(int a = 0; a < 8; ++a)
+		Eres[8 * (size_t)e + a] = er[cg_loc(a, 0) + 2 * cg_loc(a, 1) + 4 * cg_loc(a, 2)];
 }
 
 // DTdot = (sum of element residuals at the node) / lumped mass
@@ -2110,7 +2364,10 @@ void launch_horiz_ave(cudaStream_t st, const Lvl &L, const Geo *geo, const doubl
 
 void launch_forces(cudaStream_t st, const Lvl &L, const Geo *geo, const double *buoy, double *F)
 {
-	launch_k(k_forces, nblocks(L.nno), TPB, st, L, geo, buoy, F);
+	if(L.sphere)
+		launch_k(k_forces, nblocks(L.nno), TPB, st, L, geo, buoy, F);
+	else
+		launch_k(k_forces_box, nblocks(L.nno), TPB, st, L, geo, buoy, F);
 }
 
 void launch_v_from_vector(cudaStream_t st, const Lvl &L, const double *U, double *V)
@@ -2121,7 +2378,10 @@ void launch_v_from_vector(cudaStream_t st, const Lvl &L, const double *U, double
 void launch_pg_residual(cudaStream_t st, const Lvl &L, const Geo *geo, const double *T, const double *Tdot, const double *V, double Q0,
                         double *Eres)
 {
-	launch_k(k_pg_residual, nblocks(L.nel, 128), 128, st, L, geo, T, Tdot, V, Q0, Eres);
+	if(L.sphere)
+		launch_k(k_pg_residual, nblocks(L.nel, 128), 128, st, L, geo, T, Tdot, V, Q0, Eres);
+	else
+		launch_k(k_pg_residual_box, nblocks(L.nel, 128), 128, st, L, geo, T, Tdot, V, Q0, Eres);
 }
 
 void launch_pg_gather(cudaStream_t st, const Lvl &L, const Geo *geo, const double *Eres, double *DTdot)
