@@ -437,14 +437,24 @@ class Solver:
                                                                  ctypes.byref(r0)))
         return r0.value, steps.value
 
-    def solve_constrained_flow_iterative(self, U, P, F):
-        V = np.zeros(3 * self.fine["nno"])
+    def _out_V(self, V):
+        """The nodal velocity output (3 nno): the caller's buffer (e.g. pinned
+        host memory, written in place like the reference's E->V) or a new one."""
+        n = 3 * self.fine["nno"]
+        if V is None:
+            return np.zeros(n)
+        if V.shape != (n,):
+            raise ValueError(f"V must have shape ({n},)")
+        return V
+
+    def solve_constrained_flow_iterative(self, U, P, F, V=None):
+        V = self._out_V(V)
         self._check(self.lib.citcom_gpu_solve_constrained_flow_iterative(
             self.h, _dp(U), _dp(P), _dp(np.ascontiguousarray(F, dtype=np.float64)), _dp(V)))
         return V
 
-    def general_stokes_solver(self, T, U, P):
-        V = np.zeros(3 * self.fine["nno"])
+    def general_stokes_solver(self, T, U, P, V=None):
+        V = self._out_V(V)
         self._check(self.lib.citcom_gpu_general_stokes_solver(self.h, _dp(np.ascontiguousarray(T, dtype=np.float64)),
                                                               _dp(U), _dp(P), _dp(V)))
         return V
