@@ -1446,7 +1446,6 @@ int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 			{
 				const size_t n = (size_t)h->lv[1].neq;
 				TRYC(dalloc(h, &h->co_dense1, n * n));
-				TRYC(dalloc(h, &h->co_dense1_work, n * n));
 			}
 		}
 		for(int l = 0; l < CO_MAX_LEV; ++l)

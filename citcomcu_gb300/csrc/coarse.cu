@@ -708,31 +708,39 @@ __global__ void k_co_dense_t(int n, const float *cols, float *N)
 	N[t] = cols[(size_t)j * n + i];
 }
 
-// column j of a level's smoother matrix: `cycles` zero-start sweeps of the
-// 8 colours (each node of a colour: r = f - K d over its 27 neighbours, then
-// d += r o 1/diag, the update of gauss_seidel) against f = e_j, d in
-// work[j n ..]; N[i n + j] = d_i.  The rows of a colour are formed before any
-// of its nodes is updated (a node's own block reads its old values).
+// columns j0 .. j0+nb-1 of a level's smoother matrix: `cycles` zero-start
+// sweeps of the 8 colours (each node of a colour: r = f - K d over its 27
+// neighbours, then d += r o 1/diag, the update of gauss_seidel) against f =
+// e_j; N[i n + j] = d_i.  The rows of a colour are formed before any of its
+// nodes is updated (a node's own block reads its old values).  A CTA relaxes
+// nb columns at once, their d in shared memory: the threads of one row and
+// its nb columns are adjacent, so each stencil word is read from L2 once per
+// CTA for all of them (one column per CTA read the level's stencil once per
+// column).  Each entry keeps the per-column summation order.
 __global__ void __launch_bounds__(256) k_dense_build_gs(Lvl L, const float *__restrict__ K, const float *__restrict__ BI,
-                                                        int cycles, float *work, float *N)
+                                                        int cycles, int ncols, int maxrows, float *N)
 {
 	pdl_begin();
-	__shared__ float rs[3 * CO_DENSE1_MAX_COLOUR];
-	const int n = L.neq, j = blockIdx.x;
-	float *d = work + (size_t)j * n;
-	for(int i = threadIdx.x; i < n; i += blockDim.x)
+	extern __shared__ __align__(16) float db_smem[];
+	const int n = L.neq, j0 = blockIdx.x * ncols;
+	const int nb = min(ncols, n - j0);
+	float *d = db_smem;             // [b][n]
+	float *rs = db_smem + ncols * n;  // [b][maxrows]
+	for(int i = threadIdx.x; i < ncols * n; i += blockDim.x)
 		d[i] = 0.f;
 	__syncthreads();
 	for(int cyc = 0; cyc < cycles; ++cyc)
 		for(int c = 0; c < 8; ++c)
 		{
 			const int cnt = L.coff[c + 1] - L.coff[c];
-			for(int t = threadIdx.x; t < 3 * cnt; t += blockDim.x)
+			for(int t = threadIdx.x; t < 3 * cnt * nb; t += blockDim.x)
 			{
-				const int q = t / 3, i = t - 3 * q, p = L.coff[c] + q;
+				const int row = t / nb, b = t - nb * row;
+				const int q = row / 3, i = row - 3 * q, p = L.coff[c] + q;
 				int x, y, z;
 				cg_decode(L, c, q, x, y, z);
-				float r = (3 * cg_node(L, x, y, z) + i == j) ? 1.f : 0.f;
+				const float *db = d + (size_t)b * n;
+				float r = (3 * cg_node(L, x, y, z) + i == j0 + b) ? 1.f : 0.f;
 				for(int s = 0; s < 27; ++s)
 				{
 					const int mz = z + s % 3 - 1, mx = x + (s / 3) % 3 - 1, my = y + s / 9 - 1;
@@ -741,29 +749,42 @@ __global__ void __launch_bounds__(256) k_dense_build_gs(Lvl L, const float *__re
 					const int m = cg_node(L, mx, my, mz);
 #pragma unroll
 					for(int jj = 0; jj < 3; ++jj)
-						r -= K[cg_kidx(L, s, i, jj, p)] * d[3 * m + jj];
+						r -= K[cg_kidx(L, s, i, jj, p)] * db[3 * m + jj];
 				}
-				rs[t] = r * BI[3 * (size_t)p + i];
+				rs[(size_t)b * maxrows + row] = r * BI[3 * (size_t)p + i];
 			}
 			__syncthreads();
-			for(int t = threadIdx.x; t < 3 * cnt; t += blockDim.x)
+			for(int t = threadIdx.x; t < 3 * cnt * nb; t += blockDim.x)
 			{
-				const int q = t / 3, i = t - 3 * q;
+				const int row = t / nb, b = t - nb * row;
+				const int q = row / 3, i = row - 3 * q;
 				int x, y, z;
 				cg_decode(L, c, q, x, y, z);
-				d[3 * cg_node(L, x, y, z) + i] += rs[t];
+				d[(size_t)b * n + 3 * cg_node(L, x, y, z) + i] += rs[(size_t)b * maxrows + row];
 			}
 			__syncthreads();
 		}
-	for(int i = threadIdx.x; i < n; i += blockDim.x)
-		N[(size_t)i * n + j] = d[i];
+	for(int t = threadIdx.x; t < n * nb; t += blockDim.x)
+	{
+		const int i = t / nb, b = t - nb * i;
+		N[(size_t)i * n + j0 + b] = d[(size_t)b * n + i];
+	}
 }
 
 } // namespace
 
 void launch_dense_build_gs(cudaStream_t st, const Lvl &L, const float *K, const float *BI, int cycles, float *work, float *N)
 {
-	k_dense_build_gs<<<L.neq, 256, 0, st>>>(L, K, BI, cycles, work, N);
+	(void)work;
+	int maxc = 0;
+	for(int c = 0; c < 8; ++c)
+		maxc = std::max(maxc, L.coff[c + 1] - L.coff[c]);
+	const int maxrows = 3 * maxc;
+	// as many columns per CTA as fit in the shared memory the kernel may use
+	const size_t per_col = sizeof(float) * (size_t)(L.neq + maxrows);
+	const int ncols = (int)std::max<size_t>(1, std::min<size_t>(8, (size_t)CO_SMEM_MAX / per_col));
+	const size_t smem = per_col * ncols;
+	k_dense_build_gs<<<(L.neq + ncols - 1) / ncols, 256, smem, st>>>(L, K, BI, cycles, ncols, maxrows, N);
 	++g_kernel_launches;
 }
 
@@ -771,7 +792,8 @@ int coarse_init(int *cluster_size)
 {
 	*cluster_size = 0;
 	if(cudaFuncSetAttribute(k_coarse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CO_SMEM_MAX) != cudaSuccess ||
-	   cudaFuncSetAttribute(k_co_dense_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CO_SMEM_MAX) != cudaSuccess)
+	   cudaFuncSetAttribute(k_co_dense_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CO_SMEM_MAX) != cudaSuccess ||
+	   cudaFuncSetAttribute(k_dense_build_gs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CO_SMEM_MAX) != cudaSuccess)
 		return -1;
 	cudaFuncSetAttribute(k_coarse, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
 	for(int cs = CO_MAX_CLUSTER; cs >= 8; cs /= 2)

@@ -724,23 +724,29 @@ __global__ void k_nn_guess_u(Lvl Lc, const float *y, double su, const double *wo
 __global__ void k_nn_guess_p(Lvl Lf, Lvl Lc, int r, const float *y, double sp, double mp, const double *work, double *P)
 {
 	pdl_begin();
+	// the scale once per block; the interpolation of the FP32 network output
+	// in FP32 (per-element FP64 divisions and products ran at GB300's FP64 rate)
+	__shared__ double s_sc;
+	if(threadIdx.x == 0)
+		s_sc = sp * anomaly_rms(work, Lc.nno, Lc.noz);
+	__syncthreads();
 	const int e = blockIdx.x * blockDim.x + threadIdx.x;
 	if(e >= Lf.nel)
 		return;
-	const double sc = sp * anomaly_rms(work, Lc.nno, Lc.noz);
 	const int ez = e % Lf.elz, q = e / Lf.elz, ex = q % Lf.elx, ey = q / Lf.elx;
 	// element centre in coarse-node units
-	const double cxp = (ex + 0.5) / r, cyp = (ey + 0.5) / r, czp = (ez + 0.5) / r;
+	const float ir = 1.0f / (float)r;
+	const float cxp = (ex + 0.5f) * ir, cyp = (ey + 0.5f) * ir, czp = (ez + 0.5f) * ir;
 	const int x0 = min((int)cxp, Lc.nox - 2), y0 = min((int)cyp, Lc.noy - 2), z0 = min((int)czp, Lc.noz - 2);
-	const double fx = cxp - x0, fy = cyp - y0, fz = czp - z0;
-	double s = 0.0;
+	const float fx = cxp - x0, fy = cyp - y0, fz = czp - z0;
+	float s = 0.f;
 	for(int b = 0; b < 8; ++b)
 	{
 		const int dx = b & 1, dy = (b >> 1) & 1, dz = b >> 2;
-		const double w = (dx ? fx : 1.0 - fx) * (dy ? fy : 1.0 - fy) * (dz ? fz : 1.0 - fz);
-		s += w * (double)y[(size_t)cg_node(Lc, x0 + dx, y0 + dy, z0 + dz) * NN_CH + 3];
+		const float w = (dx ? fx : 1.f - fx) * (dy ? fy : 1.f - fy) * (dz ? fz : 1.f - fz);
+		s += w * y[(size_t)cg_node(Lc, x0 + dx, y0 + dy, z0 + dz) * NN_CH + 3];
 	}
-	P[e] = s * sc + mp;
+	P[e] = (double)s * s_sc + mp;
 }
 
 } // namespace
