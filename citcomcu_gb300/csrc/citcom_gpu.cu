@@ -112,7 +112,6 @@ struct citcom_gpu
 	// the same for level 1 (its sweeps of `co_dense1_cycles`, zero start or
 	// with a start through d0 + N (f - K d0)) when it runs in the cluster program
 	float *co_dense1;
-	float *co_dense1_work;
 	int co_dense1_cycles;
 	CoLevels co_lv;
 	CoProg co_prog;
@@ -988,8 +987,7 @@ int construct_stiffness(citcom_gpu *h)
 			launch_coarse_dense_build(h->st, h->lv[0], h->Kt32[0], h->BI32[0], c.vlowstep, h->co_dense_work, h->co_dense,
 			                          h->dscal + S_ERR);
 		if(l == 1 && h->co_dense1)
-			launch_dense_build_gs(h->st, h->lv[1], h->K32[1], h->BI32[1], h->co_dense1_cycles, h->co_dense1_work,
-			                      h->co_dense1);
+			launch_dense_build_gs(h->st, h->lv[1], h->K32[1], h->BI32[1], h->co_dense1_cycles, h->co_dense1);
 	}
 	launch_bpi(h->st, h->lv[lmax], h->geo[lmax], h->BI64[lmax], h->BPI, c.precond);
 	CK(cudaGetLastError());
@@ -1435,7 +1433,6 @@ int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 			}
 		}
 		h->co_dense1 = nullptr;
-		h->co_dense1_work = nullptr;
 		h->co_dense1_cycles = cfg->down_heavy;
 		if(h->co_dense && h->co_LC >= 1 && !h->co_local[1] && h->L > 2 && h->lv[1].neq <= CO_DENSE1_MAX_EQ)
 		{

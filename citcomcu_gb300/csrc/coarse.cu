@@ -773,9 +773,8 @@ __global__ void __launch_bounds__(256) k_dense_build_gs(Lvl L, const float *__re
 
 } // namespace
 
-void launch_dense_build_gs(cudaStream_t st, const Lvl &L, const float *K, const float *BI, int cycles, float *work, float *N)
+void launch_dense_build_gs(cudaStream_t st, const Lvl &L, const float *K, const float *BI, int cycles, float *N)
 {
-	(void)work;
 	int maxc = 0;
 	for(int c = 0; c < 8; ++c)
 		maxc = std::max(maxc, L.coff[c + 1] - L.coff[c]);

@@ -147,12 +147,13 @@ void launch_coarse_dense_build(cudaStream_t st, const Lvl &L, const float4 *Kt, 
                                double *err);
 // The same matrix for a level above the one-CTA smoother's size (level 1 of
 // the cluster program): column j is `cycles` zero-start colour sweeps against
-// e_j, one CTA per column, with the level's FP32 stencil K (cg_kidx layout)
-// and 1/diag BI (position order).  A smoother with a start d0 is then
-// d = d0 + N (f - K d0), the same N.  work: neq^2 floats; N: neq^2 floats.
+// e_j, up to 8 columns per CTA with their vectors in shared memory, with the
+// level's FP32 stencil K (cg_kidx layout) and 1/diag BI (position order).  A
+// smoother with a start d0 is then d = d0 + N (f - K d0), the same N.
+// N: neq^2 floats, row-major.
 #define CO_DENSE1_MAX_EQ 4096
 #define CO_DENSE1_MAX_COLOUR 1024   // nodes of the largest colour
-void launch_dense_build_gs(cudaStream_t st, const Lvl &L, const float *K, const float *BI, int cycles, float *work, float *N);
+void launch_dense_build_gs(cudaStream_t st, const Lvl &L, const float *K, const float *BI, int cycles, float *N);
 
 // Stencil kernels of the tiled (large) levels, tile.cu: persistent CTAs
 // streaming tiles through shared memory with bulk copies
