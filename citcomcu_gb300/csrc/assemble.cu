@@ -20,10 +20,15 @@
 //
 // Work split: one warp per (tile of 32 colour positions, slot); lane = node,
 // so the nine words a lane writes per slot are consecutive with its
-// neighbours' in the tile-major stencil (level.h, cg_kidx) and every lane of
-// a warp reads the same element-kernel word (a broadcast).  The Gauss-point
-// viscosities are pre-split into (hi, lo) pairs once per assembly.
+// neighbours' in the tile-major stencil (level.h, cg_kidx).  In the box every
+// lane of a warp reads the same element-kernel word (a broadcast); in the
+// spherical segment the lanes' elements lie in neighbouring (theta, r)
+// columns, and the word-major table (kernels.h, GeoDF) puts their words next
+// to each other.  The Gauss-point viscosities are pre-split into (hi, lo)
+// pairs once per assembly.
 #include <cuda_runtime.h>
+
+#include <cstddef>
 
 #include "kernels.h"
 
@@ -62,8 +67,19 @@ __global__ void k_eta_split(int n, const double *__restrict__ evi, float2 *__res
 }
 
 constexpr int AS_THREADS = 256;
+// the word offsets the kernel uses: mh, ml, lgh, lgl of GeoDF
+static_assert(GEODF_WORDS == 2 * 4608 + 2 * 576, "GeoDF layout");
+static_assert(offsetof(GeoDF, ml) == 4608 * sizeof(float) && offsetof(GeoDF, lgh) == 9216 * sizeof(float) &&
+                  offsetof(GeoDF, lgl) == 9792 * sizeof(float),
+              "GeoDF layout");
 
-__global__ void __launch_bounds__(AS_THREADS) k_assemble_df(Lvl L, const GeoDF *__restrict__ G,
+// YLANE (the spherical segment): the lanes of a warp are 32 nodes of one
+// (x, z) line with the same y parity, so that all of them read the same
+// column's element kernels (a broadcast, as in the box), at the price of
+// stencil writes spread over 32 tiles.  Otherwise (the box) the lanes are the
+// 32 positions of one stencil tile.
+template <bool YLANE>
+__global__ void __launch_bounds__(AS_THREADS) k_assemble_df(Lvl L, const float *__restrict__ G,
                                                            const float2 *__restrict__ eta2, int aug,
                                                            double *__restrict__ K64, float *__restrict__ K32,
                                                            float *__restrict__ K32lo, double *__restrict__ BI64,
@@ -71,20 +87,42 @@ __global__ void __launch_bounds__(AS_THREADS) k_assemble_df(Lvl L, const GeoDF *
 {
 	pdl_begin();
 	const int lane = threadIdx.x & 31;
-	const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-	const int tile = w / 27, s = w - 27 * (w / 27);
-	if(tile >= L.toff[8])
-		return;
-	int c = 0;
+	const long w = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+	const int s = (int)(w % 27);
+	int p, x, y, z;
+	if constexpr(YLANE)
+	{
+		// warp (line, y parity, chunk of 32 y values of that parity, slot)
+		const int nch = (L.cnt[1][0] + 31) / 32;
+		long r = w / 27;
+		const int chunk = (int)(r % nch);
+		r /= nch;
+		const int py = (int)(r % 2);
+		r /= 2;
+		if(r >= (long)L.nox * L.noz)
+			return;
+		z = (int)(r % L.noz);
+		x = (int)(r / L.noz);
+		y = py + 2 * (32 * chunk + lane);
+		if(y >= L.noy)
+			return;
+		p = cg_pos(L, x, y, z);
+	}
+	else
+	{
+		const int tile = (int)(w / 27);
+		if(tile >= L.toff[8])
+			return;
+		int c = 0;
 #pragma unroll
-	for(int k = 1; k < 8; ++k)
-		c += (tile >= L.toff[k]);
-	const int q = (tile - L.toff[c]) * CG_TILE + lane;
-	if(q >= L.coff[c + 1] - L.coff[c])
-		return;
-	const int p = L.coff[c] + q;
-	int x, y, z;
-	cg_decode(L, c, q, x, y, z);
+		for(int k = 1; k < 8; ++k)
+			c += (tile >= L.toff[k]);
+		const int q = (tile - L.toff[c]) * CG_TILE + lane;
+		if(q >= L.coff[c + 1] - L.coff[c])
+			return;
+		p = L.coff[c] + q;
+		cg_decode(L, c, q, x, y, z);
+	}
 	const int dz = s % 3 - 1, dx = (s / 3) % 3 - 1, dy = s / 9 - 1;
 	float bh[9], bl[9];
 #pragma unroll
@@ -121,13 +159,17 @@ __global__ void __launch_bounds__(AS_THREADS) k_assemble_df(Lvl L, const GeoDF *
 						eh[2 * k + 1] = v.z;
 						el[2 * k + 1] = v.w;
 					}
+					// word w of this element's column: Gc[w * ncol]
+					const int ncol = L.sphere ? L.elx * L.elz : 1;  // geo_count(L)
+					const float *Gc = G + cg_col(L, x - ox, z - oz);
 #pragma unroll
 					for(int k = 0; k < 8; ++k)
 					{
-						const float *mh = G->mh[k][a][b], *ml = G->ml[k][a][b];
+						const size_t w0 = (size_t)(((k * 8 + a) * 8 + b) * 9);
 #pragma unroll
 						for(int r = 0; r < 9; ++r)
-							df_madd(bh[r], bl[r], eh[k], el[k], mh[r], ml[r]);
+							df_madd(bh[r], bl[r], eh[k], el[k], Gc[(w0 + r) * ncol],
+							        Gc[(4608 + w0 + r) * ncol]);
 					}
 					if(aug)
 					{
@@ -138,10 +180,10 @@ __global__ void __launch_bounds__(AS_THREADS) k_assemble_df(Lvl L, const GeoDF *
 							df_add(sh, sl, eh[k], el[k]);
 						sh *= 0.125f;
 						sl *= 0.125f;
-						const float *gh = G->lgh[a][b], *gl = G->lgl[a][b];
+						const size_t g0 = (size_t)(9216 + (a * 8 + b) * 9);
 #pragma unroll
 						for(int r = 0; r < 9; ++r)
-							df_madd(bh[r], bl[r], sh, sl, gh[r], gl[r]);
+							df_madd(bh[r], bl[r], sh, sl, Gc[(g0 + r) * ncol], Gc[(576 + g0 + r) * ncol]);
 					}
 				}
 			}
@@ -226,12 +268,19 @@ void geo_df_fill(const Geo &g, int aug, double lambda, GeoDF *out)
 				split(aug ? lambda * g.g[3 * a + r / 3] * g.g[3 * b + r % 3] : 0.0, out->lgh[a][b][r], out->lgl[a][b][r]);
 }
 
-void launch_assemble_df(cudaStream_t st, const Lvl &L, const GeoDF *G, const double *evi, float2 *eta2, int aug,
+void launch_assemble_df(cudaStream_t st, const Lvl &L, const float *G, const double *evi, float2 *eta2, int aug,
                         double *K64, float *K32, float *K32lo, double *BI64, float *BI32)
 {
 	const int n = 8 * L.nel;
 	as_launch(k_eta_split, (n + 255) / 256, 256, st, n, evi, eta2);
+	if(L.sphere)
+	{
+		const long warps = 27L * 2 * ((L.cnt[1][0] + 31) / 32) * L.nox * L.noz;
+		as_launch(k_assemble_df<true>, (int)((warps * 32 + AS_THREADS - 1) / AS_THREADS), AS_THREADS, st, L, G,
+		          (const float2 *)eta2, aug, K64, K32, K32lo, BI64, BI32);
+		return;
+	}
 	const long warps = 27L * L.toff[8];
-	as_launch(k_assemble_df, (int)((warps * 32 + AS_THREADS - 1) / AS_THREADS), AS_THREADS, st, L, G,
+	as_launch(k_assemble_df<false>, (int)((warps * 32 + AS_THREADS - 1) / AS_THREADS), AS_THREADS, st, L, G,
 	          (const float2 *)eta2, aug, K64, K32, K32lo, BI64, BI32);
 }

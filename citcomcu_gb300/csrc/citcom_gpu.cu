@@ -62,7 +62,7 @@ struct citcom_gpu
 	float *BI32[CITCOM_MAX_LEVELS];
 	float4 *Kt32[CITCOM_MAX_LEVELS];  // padded FP32 stencil of the levels k_gs_tiny smooths, else null
 	float *eta32[CITCOM_MAX_LEVELS];  // FP32 Gauss-point viscosity of the levels the matrix-free smoother relaxes, else null
-	GeoDF *geodf[CITCOM_MAX_LEVELS];  // box element kernels as FP32 pairs (mixed configuration), else null
+	float *geodf[CITCOM_MAX_LEVELS];  // element kernels as FP32 pairs, word-major over the columns (mixed), else null
 	float *K32lo;                     // mixed box: the finest FP64 operator's FP32 remainder (K64 = K32 + K32lo), else null
 	float2 *usplit;                   // the vector K32 + K32lo is applied to, as FP32 pairs (neq)
 	bool no_split;                    // CITCOM_GPU_NO_SPLIT: keep the finest FP64 stencil instead
@@ -1341,14 +1341,24 @@ int citcom_gpu_create(const citcom_gpu_config *cfg, citcom_gpu **out)
 				}
 				h->geodf[l] = nullptr;
 				h->eta2[l] = nullptr;
-				if(cfg->precision == CITCOM_GPU_MIXED && !L.sphere && !h->fp64_assembly)
+				if(cfg->precision == CITCOM_GPU_MIXED && !h->fp64_assembly)
 				{
-					// the mixed configuration assembles the box levels in double-float
-					std::vector<GeoDF> gd(1);
-					geo_df_fill(g[0], cfg->aug_lagr, cfg->aug_number, gd.data());
-					TRYC(dalloc(h, &h->geodf[l], 1));
+					// the mixed configuration assembles in double-float: the
+					// element kernels of every geometry column as FP32 pairs,
+					// word-major (word w of column c at w * ncol + c)
+					const size_t ncol = g.size();
+					std::vector<float> gt((size_t)GEODF_WORDS * ncol);
+					GeoDF one;
+					for(size_t cc = 0; cc < ncol; ++cc)
+					{
+						geo_df_fill(g[cc], cfg->aug_lagr, cfg->aug_number, &one);
+						const float *wv = reinterpret_cast<const float *>(&one);
+						for(int wd = 0; wd < GEODF_WORDS; ++wd)
+							gt[(size_t)wd * ncol + cc] = wv[wd];
+					}
+					TRYC(dalloc(h, &h->geodf[l], gt.size()));
 					TRYC(dalloc(h, &h->eta2[l], (size_t)8 * L.nel));
-					if(cudaMemcpy(h->geodf[l], gd.data(), sizeof(GeoDF), cudaMemcpyHostToDevice) != cudaSuccess)
+					if(cudaMemcpy(h->geodf[l], gt.data(), sizeof(float) * gt.size(), cudaMemcpyHostToDevice) != cudaSuccess)
 					{
 						r = fail(h, CITCOM_GPU_ERR_CUDA, "geometry upload failed");
 						goto failed;

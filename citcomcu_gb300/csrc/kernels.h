@@ -157,19 +157,25 @@ void launch_dense_build_gs(cudaStream_t st, const Lvl &L, const float *K, const 
 
 // Stencil kernels of the tiled (large) levels, tile.cu: persistent CTAs
 // streaming tiles through shared memory with bulk copies
-// Box-level element kernels as (hi, lo) FP32 pairs for the double-float
-// assembly (assemble.cu): Mk of Geo, and lambda g_a,i g_b,j of the augmented
-// term (zero without it)
+// Element kernels as (hi, lo) FP32 pairs for the double-float assembly
+// (assemble.cu): Mk of Geo, and lambda g_a,i g_b,j of the augmented term (zero
+// without it).  On the device the table of a level is stored word-major over
+// its geometry columns: word w of column c at [w * ncol + c] (GEODF_WORDS
+// words per column, in the order of this struct).  The box has one column, so
+// its table is this struct; in the spherical segment neighbouring lanes of a
+// warp read neighbouring columns.
 struct GeoDF
 {
 	float mh[8][8][8][9], ml[8][8][8][9];
 	float lgh[8][8][9], lgl[8][8][9];
 };
+constexpr int GEODF_WORDS = (int)(sizeof(GeoDF) / sizeof(float));
 void geo_df_fill(const Geo &g, int aug, double lambda, GeoDF *out);
-// construct_node_ks of a box level in double-float arithmetic: splits evi into
+// construct_node_ks of a level in double-float arithmetic: splits evi into
 // eta2 (8 nel float2), then K64 / K32 / K32lo (the FP32 remainder entry - K32;
-// any may be null) and BI64 / BI32
-void launch_assemble_df(cudaStream_t st, const Lvl &L, const GeoDF *G, const double *evi, float2 *eta2, int aug,
+// any may be null) and BI64 / BI32.  G: the word-major table of the level's
+// geo_count(L) columns
+void launch_assemble_df(cudaStream_t st, const Lvl &L, const float *G, const double *evi, float2 *eta2, int aug,
                         double *K64, float *K32, float *K32lo, double *BI64, float *BI32);
 
 // matrix-free FP32 Gauss-Seidel colour of a box level (mf.cu): eta = the
