@@ -214,9 +214,12 @@ def bytes_per_sweep(nno: int, word: int) -> int:
 
 
 # DRAM bytes (read + write) of one finest-level FP32 Gauss-Seidel colour launch
-# of the stored-stencil kernel (k_tile<float, 0>, 274,625-node level), median
-# of three launches of an ncu --set full capture; scaled by nodes elsewhere.
-TRAFFIC_PER_LAUNCH_64 = 38.57e6
+# of the stored-stencil kernel (k_tile<float, 0>) on the 1,081,665-node level
+# of the 128x128x64 box: median of the 48 finest launches of one time step
+# captured by ncu (dram__bytes_read.sum + dram__bytes_write.sum, cold caches);
+# scaled by nodes for other levels.
+TRAFFIC_PER_LAUNCH_NODES = 1081665
+TRAFFIC_PER_LAUNCH = 150.02e6
 
 
 # --------------------------------------------------------------- GPU arm
@@ -712,7 +715,7 @@ def main():
         "roofline": {"bound": "hbm", "kernel": "k_tile<float, 0> (finest-level Gauss-Seidel colour)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None,
-                     "traffic": TRAFFIC_PER_LAUNCH_64 * nno / 274625 if nno >= 274625 else None,
+                     "traffic": TRAFFIC_PER_LAUNCH * nno / TRAFFIC_PER_LAUNCH_NODES if nno >= 274625 else None,
                      "peak_kind": peak_kind, "bytes_per_launch": alg_bytes,
                      "bytes_kind": "algorithmic (per colour: F, d, 1/diag K, Gauss-point viscosity, flags)",
                      "launch_us": per_launch_s * 1e6,

@@ -159,9 +159,11 @@ __global__ void __launch_bounds__(AS_THREADS) k_assemble_df(Lvl L, const float *
 						eh[2 * k + 1] = v.z;
 						el[2 * k + 1] = v.w;
 					}
-					// word w of this element's column: Gc[w * ncol]
-					const int ncol = L.sphere ? L.elx * L.elz : 1;  // geo_count(L)
-					const float *Gc = G + cg_col(L, x - ox, z - oz);
+					// word w of this element's column: Gc[w * ncol].  The box has
+					// one column: constant strides and a warp-uniform address, so
+					// its loads stay broadcasts
+					const int ncol = YLANE ? L.elx * L.elz : 1;  // geo_count(L)
+					const float *Gc = YLANE ? G + cg_col(L, x - ox, z - oz) : G;
 #pragma unroll
 					for(int k = 0; k < 8; ++k)
 					{
@@ -273,7 +275,7 @@ void launch_assemble_df(cudaStream_t st, const Lvl &L, const float *G, const dou
 {
 	const int n = 8 * L.nel;
 	as_launch(k_eta_split, (n + 255) / 256, 256, st, n, evi, eta2);
-	if(L.sphere)
+	if(L.sphere)  // one geometry column per (theta, r) element column: lanes along y
 	{
 		const long warps = 27L * 2 * ((L.cnt[1][0] + 31) / 32) * L.nox * L.noz;
 		as_launch(k_assemble_df<true>, (int)((warps * 32 + AS_THREADS - 1) / AS_THREADS), AS_THREADS, st, L, G,
