@@ -30,12 +30,19 @@ Fixtures
                    (0 - T)), Ra 1e4, seeded T0 (1 - (r - ri)/(ro - ri) plus
                    noise), accuracy 1e-8.  Operator probes on every level plus
                    3 time steps (FP64-promoted build).
+  box32_tdep.npz   the physics of the 64^3 benchmark box on 32^3 elements (4
+                   levels): eta = exp(-ln(1e3) T), Ra 1e5, seeded T0 = 1 - z +
+                   U(-0.01, 0.01) (PCG64 seed 0), the reference's stopping rule
+                   at accuracy 1e-6, 2 time steps (FP64-promoted build; per-step
+                   scalars, the fields after step 2).  `python
+                   tests/golden/make_golden.py box32` regenerates it alone.
 small_tdep, sdepv_box and sphere_tdep also hold, per step, the fields of an
 output step after heat_flux (s<k>_Have: the six .ave layer profiles T, vrms,
 Vi, Rho, F, f; s<k>_surf: shflux, bhflux; s<k>_heatflux, s<k>_heatflux_adv).
 """
 from __future__ import annotations
 
+import math
 import os
 import sys
 import tempfile
@@ -75,6 +82,23 @@ def knobs_case() -> Case:
                 vhighstep=2, accuracy=1e-8, maxstep=3)
 
 
+def box32_case() -> Case:
+    return Case(name="box32_tdep", mgunit=(4, 4, 4), levels=4, rayleigh=1e5, tdepv=True, visc0=(1.0,),
+                viscE=(math.log(1e3),), viscT=(0.0,), accuracy=1e-6, maxstep=2)
+
+
+def make_box32(tmp):
+    c = box32_case()
+    T0 = conductive_T0(c, amp=0.01, seed=0)
+    R = run_reference(c, os.path.join(tmp, "box32"), nsteps=2, T0=T0)
+    keep = {"dims": R["dims"], "T0_input": T0}
+    for s in range(3):
+        keep[f"s{s}_scalars"] = R[f"s{s}_scalars"]
+    for k in ("T", "V1", "V2", "V3", "P"):
+        keep[f"s2_{k}"] = R[f"s2_{k}"]
+    np.savez_compressed(os.path.join(HERE, "box32_tdep.npz"), **keep)
+
+
 def cfg1_case() -> Case:
     return Case(name="cfg1_16", mgunit=(4, 4, 4), levels=3, rayleigh=1e4, accuracy=1e-6,
                 perturbmag=0.01, perturbk=1.0, maxstep=50)
@@ -97,7 +121,13 @@ def _steps(R, n, keys=("T", "V1", "V2", "V3", "U", "P", "Tdot") + OUTPUT_KEYS):
 def main():
     if not build_reference(quiet=True):
         raise SystemExit("reference sources not present; fixtures cannot be regenerated here")
+    if sys.argv[1:] == ["box32"]:
+        with tempfile.TemporaryDirectory() as tmp:
+            make_box32(tmp)
+        print("box32_tdep.npz", os.path.getsize(os.path.join(HERE, "box32_tdep.npz")), "bytes")
+        return
     with tempfile.TemporaryDirectory() as tmp:
+        make_box32(tmp)
         c = small_case()
         T0 = conductive_T0(c, amp=0.01, seed=0)
         R = run_reference(c, os.path.join(tmp, "small"), nsteps=3, T0=T0, probe=True)
@@ -141,7 +171,7 @@ def main():
             for k in ("T", "V1", "V2", "V3", "P"):
                 keep[f"s{st}_{k}"] = R[f"s{st}_{k}"]
         np.savez_compressed(os.path.join(HERE, "cfg1_16.npz"), **keep)
-    for f in ("small_tdep.npz", "cfg1_16.npz", "sphere_tdep.npz", "sdepv_box.npz", "knobs_box.npz"):
+    for f in ("small_tdep.npz", "cfg1_16.npz", "sphere_tdep.npz", "sdepv_box.npz", "knobs_box.npz", "box32_tdep.npz"):
         print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")
 
 

@@ -207,3 +207,30 @@ def test_residual_rule_on_the_oracle(oracle_lib):
     o2.setup_operators()
     info2 = o2.solve_Ahat_p_fhat(case.accuracy, case.piterations)
     assert info["uzawa"] < info2["uzawa"]
+
+
+def test_box32_run(oracle_lib):
+    """The physics of the 64^3 benchmark box on 32^3 elements (4 levels, eta =
+    exp(-ln(1e3) T), Ra 1e5, seeded T0, the reference's stopping rule at
+    1e-6; tests/golden/box32_tdep.npz): the oracle in the reference's own
+    (lexicographic) order against the reference's run, a cold solve (375
+    Uzawa iterations, the cap) and 2 time steps: the same solve_del2_u calls
+    per solve, Nu and Vrms to 1e-10, T and V after step 2 to 1e-9."""
+    from tests.golden.make_golden import box32_case
+    G = dict(np.load(os.path.join(GOLD, "box32_tdep.npz")))
+    o = oracle_lib.Oracle(box32_case())
+    o.set_T(G["T0_input"])
+    o.thermal_buoyancy()
+    for s in range(3):
+        if s:
+            o.pg_timestep()
+        info = o.stokes()
+        nut, nub = o.heat_flux()
+        sc = G[f"s{s}_scalars"]
+        print(s, info["del2_calls"], int(sc[6]), nut - sc[0], o.vrms() / sc[2] - 1)
+        assert info["del2_calls"] == int(sc[6])
+        assert abs(nut - sc[0]) < 1e-10 and abs(nub - sc[1]) < 1e-10
+        assert abs(o.vrms() - sc[2]) < 1e-10 * sc[2]
+    assert rel(o.T(), G["s2_T"]) < 1e-9
+    for d in range(3):
+        assert rel(o.V(d), G[f"s2_V{d + 1}"]) < 1e-9
